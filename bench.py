@@ -1,0 +1,403 @@
+#!/usr/bin/env python3
+"""Benchmark of the xc_fast hot path on one GB300 (replicas on N GPUs).
+
+Workload (the precision configuration): 64 stations x 3 components x 30 days
+at delta 0.1 s, win_len 3600 s -> 720 windows of 36 000 samples, output
+spectra of nspec = 18 523 bins (output_nfft 37 044), all 2016 station pairs
+x 9 component pairs = 18 144 pairs, 5 % of windows zeroed as gaps, linear
+stack over all windows, max_lag 100 s -> 2001 lags per NCF.
+
+One step = correlate + stack all 18 144 pairs over the 720 windows, then the
+C2R + lag cut: 13 063 680 pair-windows. Inputs (20.5 GB of spectra) are
+resident in HBM and larger than L2 (no L2 flush needed).
+
+Metric: pair-windows/s. `value` is the device-resident throughput of the
+selected method (tensor-core BF16 hi/lo when built, else plain FP32);
+`e2e` runs the same step through the host-buffer C-ABI call
+(fxc_xc_run_host) with the H2D copy of the spectra and the D2H copy of the
+NCFs inside the timed region.
+
+`--impl reference` times the FP64 CPU oracle (the reference algorithm
+restated; the reference itself has no CPU path and its CUDA sources do not
+exist on the GPU host) on a bounded sample of the same workload, using all
+host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NSTA, NCOMP, NDAYS, NSTEP = 64, 3, 30, 24
+DT, CC_LEN = 0.1, 100.0
+NSPEC = 18523  # output_nfft 37044 / 2 + 1 for win_len 3600 s, lag 100 s at 10 Hz
+GAP_FRAC = 0.05
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="auto", choices=["auto", "plain", "tensor"])
+    ap.add_argument("--days", type=int, default=NDAYS)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(seconds_target=15.0, threads=1):
+    """FP64 oracle on a bounded sample: 16 stations (48 channels), whole days
+    of 24 windows, all 9 x 120 component pairs; returns pair-windows/s."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from fastxc_gb300.synthetic import cross_station_pairs
+    from oracle import xc_oracle as xo
+
+    rng = np.random.default_rng(1)
+    nsta, nwin = 16, NSTEP
+    nchan = nsta * NCOMP
+    spec = (rng.standard_normal((nwin, nchan, NSPEC)) + 1j * rng.standard_normal((nwin, nchan, NSPEC))).astype(np.complex64)
+    src, rec = cross_station_pairs(nsta)
+    shape = xo.finalize_shape(NSPEC, nwin, DT, CC_LEN)
+    chunks = np.array_split(np.arange(src.size), max(1, threads))
+
+    def work(idx):
+        xo.xc_run(spec, src[idx], rec[idx], 1.0 / nwin, shape)
+
+    done_pw = 0
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        if threads == 1:
+            work(np.arange(src.size))
+        else:
+            with ThreadPoolExecutor(threads) as ex:
+                list(ex.map(work, chunks))
+        reps += 1
+        done_pw += src.size * nwin
+        if time.perf_counter() - t0 > seconds_target:
+            break
+    el = time.perf_counter() - t0
+    return done_pw / el, f"{reps} x (16 stations x 3 comps, 1 day = 24 windows, {src.size} pairs, nspec {NSPEC}), FP64 numpy"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    per_step = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        v, sample = cpu_baseline(seconds_target=4.0, threads=cores)
+        if i >= args.warmup:
+            per_step.append(v)
+    value = statistics.median(per_step)
+    line = {
+        "impl": "reference",
+        "metric": "pair-windows/s",
+        "value": value,
+        "unit": "pair-windows/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "xc linear stack, 64 sta x 3 comp x 30 days (sampled)", "nspec": NSPEC,
+                   "pairs": 18144, "windows": NSTEP * NDAYS},
+        "cpu_baseline": {"value": value, "unit": "pair-windows/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "pair-windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from fastxc_gb300 import lib
+    from fastxc_gb300._lib import FXC_XC_PLAIN, FXC_XC_TENSOR, FxcError
+    from fastxc_gb300.core import Context, PairPlan, xc_shape
+    from fastxc_gb300.synthetic import cross_station_pairs, spectra_device, station_array
+
+    nwin = NSTEP * args.days
+    arr = station_array(NSTA, seed=0)
+    nchan = arr.nchan
+    src, rec = cross_station_pairs(NSTA)
+    npairs = src.size
+    stream = torch.cuda.current_stream(dev)
+    ctx = Context(local, stream.cuda_stream)
+    plan = PairPlan(ctx, src, rec, nchan)
+    shape = xc_shape(NSPEC, NSTEP, DT, CC_LEN)
+    spec, mask = spectra_device(torch, nwin, arr, NSPEC, DT, seed=rank, gap_frac=GAP_FRAC, device=dev)
+    scale = 1.0 / nwin  # mean over days of per-day stacks with 1/nstep each
+    pitch_stack = (NSPEC + 3) // 4 * 4
+    d_stack = torch.empty((npairs, pitch_stack), dtype=torch.complex64, device=dev)
+    d_ncf = torch.empty((npairs, shape.cc_size), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    methods = {"plain": FXC_XC_PLAIN}
+    try:
+        ctx.xc_stack(plan, spec, nwin, nchan, NSPEC, NSPEC, None, scale, d_stack, pitch_stack, FXC_XC_TENSOR)
+        torch.cuda.synchronize()
+        methods["tensor"] = FXC_XC_TENSOR
+    except FxcError:
+        pass
+    if args.method == "auto":
+        head = "tensor" if "tensor" in methods else "plain"
+    else:
+        head = args.method
+        if head not in methods:
+            raise SystemExit(f"method {head} not available")
+
+    def step(method, ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        ctx.xc_stack(plan, spec, nwin, nchan, NSPEC, NSPEC, None, scale, d_stack, pitch_stack, method)
+        if ev is not None:
+            ev[1].record(stream)
+        ctx.xc_finalize(d_stack, npairs, pitch_stack, shape, d_ncf)
+        if ev is not None:
+            ev[2].record(stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    results = {}
+    sampler = ClockSampler(local)
+    for name in (["plain", "tensor"] if "tensor" in methods else ["plain"]):
+        m = methods[name]
+        for _ in range(args.warmup):
+            step(m)
+        torch.cuda.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        barrier()
+        torch.cuda.synchronize()
+        if name == head:
+            sampler.start()
+        lib().fxc_launch_count_reset()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(args.steps):
+            step(m, evs[i])
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        launches = lib().fxc_launch_count()
+        barrier()
+        if name == head:
+            clocks = sampler.stop()
+        total_ms = t_start.elapsed_time(t_end)
+        if world > 1:
+            t = torch.tensor([total_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(t.item())
+        stack_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+        fin_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+        ncf_snapshot = d_ncf[:16].float().cpu().numpy().copy()
+        results[name] = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps, "stack_ms": stack_ms,
+                         "finalize_ms": fin_ms, "launches": launches, "ncf16": ncf_snapshot}
+
+    # parity sample: 16 pairs over all windows against the FP64 oracle
+    from oracle import xc_oracle as xo
+
+    sel = np.arange(16)
+    chans = np.unique(np.concatenate([src[sel], rec[sel]]))
+    remap = {c: i for i, c in enumerate(chans)}
+    host_spec = spec[:, torch.tensor(chans, device=dev), :].cpu().numpy()
+    oshape = xo.finalize_shape(NSPEC, NSTEP, DT, CC_LEN)
+    ref = xo.xc_run(host_spec, np.array([remap[c] for c in src[sel]]), np.array([remap[c] for c in rec[sel]]),
+                    scale, oshape)
+    rel = {}
+    for name, r in results.items():
+        e = np.linalg.norm(r["ncf16"] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        rel[name] = float(e.max())
+    if "tensor" in results:
+        a, b = results["tensor"]["ncf16"], results["plain"]["ncf16"]
+        rel["tensor_vs_plain"] = float((np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)).max())
+
+    pw = npairs * nwin
+    hr = results[head]
+    value = pw * world / (hr["total_ms"] / args.steps / 1e3)
+
+    # roofline of the dominant kernel (the stack kernel)
+    import json as _json
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = _json.loads(pk.read_text())
+    useful_flop = 8.0 * NSPEC * pw  # complex MAC per pair-window-bin
+    if head == "tensor":
+        issued = None
+        bound, unit = "tensor", "TFLOP/s"
+        achieved = useful_flop / (hr["stack_ms"] / 1e3) / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
+    else:
+        bound, unit = "fp32", "TFLOP/s"
+        achieved = useful_flop / (hr["stack_ms"] / 1e3) / 1e12
+        sm_max = peaks.get("sm_max_mhz", 2070.0)
+        peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # FP32 FMA lanes x 2 flop x max SM clock
+        peak_src = "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)"
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                "traffic": None, "peak_source": peak_src, "kernel": "k_xc_stack_plain" if head == "plain" else "xc tensor",
+                "algorithmic": "8 flop x nspec x pair-windows (useful complex MAC flops)",
+                "finalize_ms": hr["finalize_ms"], "stack_ms": hr["stack_ms"]}
+
+    line = {
+        "metric": "pair-windows/s",
+        "value": value,
+        "unit": "pair-windows/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": hr["ms_per_step"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16x3->f32" if head == "tensor" else "f32",
+        "data": "synthetic (seeded whitened-like spectra, coherent 0.1-2 Hz source, 5% gap windows)",
+        "method": head,
+        "config": {"workload": f"xc linear stack: {NSTA} sta x {NCOMP} comp x {args.days} days, delta {DT}s, "
+                               f"win 3600s -> {nwin} windows, nspec {NSPEC}, {npairs} pairs, lag {CC_LEN}s",
+                   "pairs": npairs, "windows": nwin, "nspec": NSPEC, "cc_size": shape.cc_size,
+                   "l2": "inputs (20.5 GB) larger than L2, no flush", "parallelism": f"replicas x{world}"},
+        "rel_l2_vs_fp64": rel,
+        "per_method": {k: {"pair_windows_per_s": pw / (v["ms_per_step"] / 1e3), "ms_per_step": v["ms_per_step"],
+                           "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"]} for k, v in results.items()},
+        "roofline": roofline,
+        "gpu_launches": hr["launches"],
+        "clocks": clocks,
+    }
+    if "tensor" in results:
+        line["tensor_vs_plain_speedup"] = results["plain"]["ms_per_step"] / results["tensor"]["ms_per_step"]
+
+    # end-to-end through the host-buffer C-ABI call
+    if not args.no_e2e:
+        host_spec = torch.empty(spec.shape, dtype=torch.complex64, pin_memory=True)
+        host_spec.copy_(spec)
+        host_ncf = torch.empty((npairs, shape.cc_size), dtype=torch.float32, pin_memory=True)
+        del d_stack
+        hs = host_spec.numpy()
+        hn = host_ncf.numpy()
+        m = methods[head]
+        ctx.xc_run_host(plan, hs, nwin, nchan, NSPEC, None, scale, shape, hn, m)
+        barrier()
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 5))
+        for _ in range(e2e_steps):
+            ctx.xc_run_host(plan, hs, nwin, nchan, NSPEC, None, scale, shape, hn, m)
+        el = (time.perf_counter() - t0) / e2e_steps
+        if world > 1:
+            t = torch.tensor([el], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        line["e2e"] = {"value": pw * world / el, "unit": "pair-windows/s",
+                       "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
+                       "ms_per_step": el * 1e3, "steps": e2e_steps}
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, sample = cpu_baseline(seconds_target=12.0, threads=1)
+        line["cpu_baseline"] = {"value": v, "unit": "pair-windows/s", "cores": 1, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

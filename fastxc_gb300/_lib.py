@@ -1,0 +1,134 @@
+"""ctypes binding of ``libfastxc_gb300.so`` (the C ABI in ``include/fastxc_gb300.h``).
+
+The binding is thin on purpose: every call goes straight to the CUDA library,
+and a missing library raises ``FxcLibraryMissing`` — there is no Python or
+CPU fallback for any compute entry point.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "lib" / "libfastxc_gb300.so"
+
+FXC_OK = 0
+FXC_ERR_INVALID = -1
+FXC_ERR_CUDA = -2
+FXC_ERR_UNSUPPORTED = -3
+FXC_ERR_NOMEM = -4
+FXC_ERR_IO = -5
+FXC_ERR_NODEVICE = -6
+
+FXC_XC_PLAIN = 0
+FXC_XC_TENSOR = 1
+
+
+class FxcError(RuntimeError):
+    def __init__(self, status: int, message: str, func: str):
+        super().__init__(f"{func} failed with status {status}: {message}")
+        self.status = status
+        self.message = message
+        self.func = func
+
+
+class FxcLibraryMissing(ImportError):
+    pass
+
+
+class XcShape(C.Structure):
+    _fields_ = [
+        ("nspec", C.c_int32),
+        ("nstep", C.c_int32),
+        ("nfft", C.c_int32),
+        ("half_cc", C.c_int32),
+        ("cc_size", C.c_int32),
+        ("dt", C.c_float),
+    ]
+
+
+_vp = C.c_void_p
+_i32 = C.c_int32
+_i64 = C.c_int64
+_int = C.c_int
+_f32 = C.c_float
+
+# name -> (restype, argtypes); every int-returning function is status-checked.
+_SIGNATURES: dict[str, tuple] = {
+    "fxc_last_error": (C.c_char_p, []),
+    "fxc_version": (_int, []),
+    "fxc_launch_count": (_i64, []),
+    "fxc_launch_count_reset": (None, []),
+    "fxc_ctx_create": (_int, [_int, _vp, C.POINTER(_vp)]),
+    "fxc_ctx_destroy": (_int, [_vp]),
+    "fxc_ctx_set_stream": (_int, [_vp, _vp]),
+    "fxc_ctx_synchronize": (_int, [_vp]),
+    "fxc_fft_c2c": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64, _int]),
+    "fxc_fft_r2c": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64]),
+    "fxc_fft_c2r": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64]),
+    "fxc_fft_supported": (_int, [_int, _int]),
+    "fxc_xc_shape_init": (_int, [_i32, _i32, _f32, _f32, C.POINTER(XcShape)]),
+    "fxc_pairplan_create": (_int, [_vp, _vp, _vp, _i64, _i32, C.POINTER(_vp)]),
+    "fxc_pairplan_destroy": (_int, [_vp]),
+    "fxc_pairplan_npairs": (_i64, [_vp]),
+    "fxc_pairplan_ntiles": (_i64, [_vp]),
+    "fxc_xc_stack": (_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, _vp, _f32, _vp, _i64, _int]),
+    "fxc_xc_finalize": (_int, [_vp, _vp, _i64, _i64, C.POINTER(XcShape), _vp]),
+    "fxc_xc_run": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
+    "fxc_xc_run_host": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
+}
+
+# Functions whose int return value is a count/flag, not a status.
+_NOT_STATUS = {"fxc_version", "fxc_fft_supported", "fxc_launch_count", "fxc_pairplan_npairs", "fxc_pairplan_ntiles"}
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+class _Lib:
+    def __init__(self, path: Path):
+        if not path.exists():
+            raise FxcLibraryMissing(
+                f"{path} not found: build it with `python -m fastxc_gb300.build` "
+                "(the GPU path has no fallback)"
+            )
+        self.path = path
+        self.cdll = C.CDLL(str(path), mode=C.RTLD_GLOBAL)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(self.cdll, name)
+            fn.restype = res
+            fn.argtypes = args
+            setattr(self, "_raw_" + name, fn)
+
+    def last_error(self) -> str:
+        msg = self._raw_fxc_last_error()
+        return msg.decode("utf-8", "replace") if msg else ""
+
+    def __getattr__(self, name: str):
+        raw = self.__dict__.get("_raw_" + name)
+        if raw is None:
+            raise AttributeError(name)
+        if raw.restype is not _int or name in _NOT_STATUS:
+            return raw
+
+        def checked(*args):
+            st = raw(*args)
+            if st != FXC_OK:
+                raise FxcError(st, self.last_error(), name)
+            return st
+
+        checked.__name__ = name
+        return checked
+
+
+_LIB: _Lib | None = None
+
+
+def lib() -> _Lib:
+    global _LIB
+    if _LIB is None:
+        _LIB = _Lib(Path(os.environ.get("FXC_LIB", LIB_PATH)))
+    return _LIB

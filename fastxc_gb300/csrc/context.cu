@@ -1,0 +1,142 @@
+// Library runtime: error reporting, contexts, scratch memory, launch counting.
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "context.cuh"
+
+namespace fxc {
+
+static thread_local std::string g_last_error;
+static thread_local int64_t g_launches = 0;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+void count_launch(int n) { g_launches += n; }
+
+int num_sms() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (cached[dev] == 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = 148;
+    cached[dev] = v;
+  }
+  return cached[dev];
+}
+
+int Scratch::reserve(size_t need) {
+  if (need <= bytes) return FXC_OK;
+  if (ptr) {
+    cudaError_t e = cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (e != cudaSuccess) {
+      set_error("cudaFree(scratch) failed: %s", cudaGetErrorString(e));
+      return FXC_ERR_CUDA;
+    }
+  }
+  size_t rounded = (need + (1u << 20) - 1) & ~size_t((1u << 20) - 1);
+  cudaError_t e = cudaMalloc(&ptr, rounded);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    ptr = nullptr;
+    set_error("cudaMalloc(%zu bytes of scratch) failed: %s", rounded, cudaGetErrorString(e));
+    return FXC_ERR_NOMEM;
+  }
+  bytes = rounded;
+  return FXC_OK;
+}
+
+void Scratch::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+int ctx_enter(fxc_ctx* ctx) {
+  FXC_CHECK_ARG(ctx != nullptr, "null context");
+  FXC_CUDA_TRY(cudaSetDevice(ctx->device));
+  return FXC_OK;
+}
+
+}  // namespace fxc
+
+using namespace fxc;
+
+extern "C" {
+
+const char* fxc_last_error(void) { return g_last_error.c_str(); }
+
+int fxc_version(void) { return 100; }
+
+int64_t fxc_launch_count(void) { return g_launches; }
+
+void fxc_launch_count_reset(void) { g_launches = 0; }
+
+int fxc_ctx_create(int device, void* stream, fxc_ctx** out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "out is null");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    (void)cudaGetLastError();
+    set_error("no CUDA device available (%s)", cudaGetErrorString(e));
+    return FXC_ERR_NODEVICE;
+  }
+  FXC_CHECK_ARG(device >= 0 && device < count, "device %d out of range [0,%d)", device, count);
+  FXC_CUDA_TRY(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  FXC_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) {
+    set_error("device %d is sm_%d%d; this library is built for sm_103a only", device, prop.major,
+              prop.minor);
+    return FXC_ERR_UNSUPPORTED;
+  }
+  fxc_ctx* c = new (std::nothrow) fxc_ctx();
+  if (!c) {
+    set_error("host allocation of context failed");
+    return FXC_ERR_NOMEM;
+  }
+  c->device = device;
+  c->stream = (cudaStream_t)stream;
+  c->num_sms = prop.multiProcessorCount;
+  *out = c;
+  return FXC_OK;
+}
+
+int fxc_ctx_destroy(fxc_ctx* ctx) {
+  if (!ctx) return FXC_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->scratch.release();
+  ctx->scratch2.release();
+  delete ctx;
+  return FXC_OK;
+}
+
+int fxc_ctx_set_stream(fxc_ctx* ctx, void* stream) {
+  FXC_CHECK_ARG(ctx != nullptr, "null context");
+  ctx->stream = (cudaStream_t)stream;
+  return FXC_OK;
+}
+
+int fxc_ctx_synchronize(fxc_ctx* ctx) {
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
+}
+
+}  // extern "C"

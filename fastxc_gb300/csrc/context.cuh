@@ -1,0 +1,27 @@
+// Context object behind the opaque fxc_ctx handle.
+#pragma once
+
+#include "fxc_common.cuh"
+
+namespace fxc {
+
+// A device buffer grown on demand and reused across calls on one context.
+struct Scratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t need);
+  void release();
+};
+
+void count_launch(int n = 1);
+int ctx_enter(fxc_ctx* ctx);
+
+}  // namespace fxc
+
+struct fxc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 148;
+  fxc::Scratch scratch;   // per-pair stacked spectra between stack and finalize
+  fxc::Scratch scratch2;  // host-call staging (device copies of host inputs)
+};

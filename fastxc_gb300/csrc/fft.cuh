@@ -1,0 +1,337 @@
+// Device-side mixed-radix FFT used by every stage of the library.
+//
+// The reference delegates every transform to cuFFT (plans at
+// native/sac2spec/device_memory.cu:23-31, native/xc/memory/memory.cu:478-483,
+// native/pws/worker/gpu.cu:196-227, native/tfpws/core/tfpws_workspace.cu).
+// This file replaces them with one in-shared-memory mixed-radix FFT:
+//   * the whole transform of one row lives in one CTA's shared memory
+//     (18 522 complex points = 148 KB for the 37 044-point real transform of
+//     the xc stage), so each row costs exactly one HBM read and one write;
+//   * every stage is an in-place Cooley-Tukey pass (decimation in frequency
+//     with digit-reversed output, or its transpose, decimation in time with
+//     digit-reversed input), one barrier per stage;
+//   * radices 2, 4, 8 are hand-written; odd primes up to 31 use the
+//     symmetric real-coefficient DFT; twiddles come from a per-length table
+//     computed in double precision on the host and rounded once to float.
+// Inverse transforms are forward transforms on conjugated data (the
+// conjugation is folded into the first load and the last store).
+#pragma once
+
+#include "fxc_common.cuh"
+
+namespace fxc {
+
+constexpr int kFftMaxStages = 24;
+
+struct FftPlan {
+  int n;                     // complex transform length
+  int nstages;
+  int radix[kFftMaxStages];  // radix of each stage, in DIF execution order
+  const float2* tw;          // tw[k] = exp(-2*pi*i*k/(n*tw_stride)), k < n*tw_stride
+  int tw_stride;             // 1 for a plain complex table, 2 when the table is the real length
+  const int* perm;           // perm[k] = point holding frequency k after fft_dif (n entries)
+};
+
+// Host side (fft_plan.cu)
+int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out);
+// Cached device table perm[k] = fft_digit_pos(k) for the plan's radix order.
+int fft_perm_table(const FftPlan& p, const int** out);
+// Returns a cached device table of exp(-2*pi*i*k/len), k in [0,len), for the
+// current device. The table lives until process exit.
+int fft_twiddles(int len, const float2** out);
+bool fft_length_supported(int n);
+
+// cos(2*pi*m/R), sin(2*pi*m/R) for m in [0,R), R in {3,5,7,11,13,17,19,23,29,31}
+__constant__ float kOddCos[158] = {
+    +1.000000000e+00f, -5.000000000e-01f, -5.000000000e-01f, +1.000000000e+00f,
+    +3.090169944e-01f, -8.090169944e-01f, -8.090169944e-01f, +3.090169944e-01f,
+    +1.000000000e+00f, +6.234898019e-01f, -2.225209340e-01f, -9.009688679e-01f,
+    -9.009688679e-01f, -2.225209340e-01f, +6.234898019e-01f, +1.000000000e+00f,
+    +8.412535328e-01f, +4.154150130e-01f, -1.423148383e-01f, -6.548607339e-01f,
+    -9.594929736e-01f, -9.594929736e-01f, -6.548607339e-01f, -1.423148383e-01f,
+    +4.154150130e-01f, +8.412535328e-01f, +1.000000000e+00f, +8.854560257e-01f,
+    +5.680647467e-01f, +1.205366803e-01f, -3.546048870e-01f, -7.485107482e-01f,
+    -9.709418174e-01f, -9.709418174e-01f, -7.485107482e-01f, -3.546048870e-01f,
+    +1.205366803e-01f, +5.680647467e-01f, +8.854560257e-01f, +1.000000000e+00f,
+    +9.324722294e-01f, +7.390089172e-01f, +4.457383558e-01f, +9.226835946e-02f,
+    -2.736629901e-01f, -6.026346364e-01f, -8.502171357e-01f, -9.829730997e-01f,
+    -9.829730997e-01f, -8.502171357e-01f, -6.026346364e-01f, -2.736629901e-01f,
+    +9.226835946e-02f, +4.457383558e-01f, +7.390089172e-01f, +9.324722294e-01f,
+    +1.000000000e+00f, +9.458172417e-01f, +7.891405094e-01f, +5.469481581e-01f,
+    +2.454854871e-01f, -8.257934547e-02f, -4.016954247e-01f, -6.772815716e-01f,
+    -8.794737512e-01f, -9.863613034e-01f, -9.863613034e-01f, -8.794737512e-01f,
+    -6.772815716e-01f, -4.016954247e-01f, -8.257934547e-02f, +2.454854871e-01f,
+    +5.469481581e-01f, +7.891405094e-01f, +9.458172417e-01f, +1.000000000e+00f,
+    +9.629172873e-01f, +8.544194045e-01f, +6.825531432e-01f, +4.600650377e-01f,
+    +2.034560131e-01f, -6.824241336e-02f, -3.348796122e-01f, -5.766803221e-01f,
+    -7.757112907e-01f, -9.172113015e-01f, -9.906859460e-01f, -9.906859460e-01f,
+    -9.172113015e-01f, -7.757112907e-01f, -5.766803221e-01f, -3.348796122e-01f,
+    -6.824241336e-02f, +2.034560131e-01f, +4.600650377e-01f, +6.825531432e-01f,
+    +8.544194045e-01f, +9.629172873e-01f, +1.000000000e+00f, +9.766205557e-01f,
+    +9.075754197e-01f, +7.960930657e-01f, +6.473862848e-01f, +4.684084407e-01f,
+    +2.675283385e-01f, +5.413890859e-02f, -1.617819966e-01f, -3.701381553e-01f,
+    -5.611870654e-01f, -7.259954919e-01f, -8.568571762e-01f, -9.476531712e-01f,
+    -9.941379572e-01f, -9.941379572e-01f, -9.476531712e-01f, -8.568571762e-01f,
+    -7.259954919e-01f, -5.611870654e-01f, -3.701381553e-01f, -1.617819966e-01f,
+    +5.413890859e-02f, +2.675283385e-01f, +4.684084407e-01f, +6.473862848e-01f,
+    +7.960930657e-01f, +9.075754197e-01f, +9.766205557e-01f, +1.000000000e+00f,
+    +9.795299413e-01f, +9.189578116e-01f, +8.207634412e-01f, +6.889669191e-01f,
+    +5.289640103e-01f, +3.473052528e-01f, +1.514277775e-01f, -5.064916884e-02f,
+    -2.506525323e-01f, -4.403941516e-01f, -6.121059825e-01f, -7.587581227e-01f,
+    -8.743466161e-01f, -9.541392564e-01f, -9.948693234e-01f, -9.948693234e-01f,
+    -9.541392564e-01f, -8.743466161e-01f, -7.587581227e-01f, -6.121059825e-01f,
+    -4.403941516e-01f, -2.506525323e-01f, -5.064916884e-02f, +1.514277775e-01f,
+    +3.473052528e-01f, +5.289640103e-01f, +6.889669191e-01f, +8.207634412e-01f,
+    +9.189578116e-01f, +9.795299413e-01f};
+__constant__ float kOddSin[158] = {
+    +0.000000000e+00f, +8.660254038e-01f, -8.660254038e-01f, +0.000000000e+00f,
+    +9.510565163e-01f, +5.877852523e-01f, -5.877852523e-01f, -9.510565163e-01f,
+    +0.000000000e+00f, +7.818314825e-01f, +9.749279122e-01f, +4.338837391e-01f,
+    -4.338837391e-01f, -9.749279122e-01f, -7.818314825e-01f, +0.000000000e+00f,
+    +5.406408175e-01f, +9.096319954e-01f, +9.898214419e-01f, +7.557495744e-01f,
+    +2.817325568e-01f, -2.817325568e-01f, -7.557495744e-01f, -9.898214419e-01f,
+    -9.096319954e-01f, -5.406408175e-01f, +0.000000000e+00f, +4.647231720e-01f,
+    +8.229838659e-01f, +9.927088741e-01f, +9.350162427e-01f, +6.631226582e-01f,
+    +2.393156643e-01f, -2.393156643e-01f, -6.631226582e-01f, -9.350162427e-01f,
+    -9.927088741e-01f, -8.229838659e-01f, -4.647231720e-01f, +0.000000000e+00f,
+    +3.612416662e-01f, +6.736956436e-01f, +8.951632914e-01f, +9.957341763e-01f,
+    +9.618256432e-01f, +7.980172273e-01f, +5.264321629e-01f, +1.837495178e-01f,
+    -1.837495178e-01f, -5.264321629e-01f, -7.980172273e-01f, -9.618256432e-01f,
+    -9.957341763e-01f, -8.951632914e-01f, -6.736956436e-01f, -3.612416662e-01f,
+    +0.000000000e+00f, +3.246994692e-01f, +6.142127127e-01f, +8.371664783e-01f,
+    +9.694002659e-01f, +9.965844930e-01f, +9.157733267e-01f, +7.357239107e-01f,
+    +4.759473930e-01f, +1.645945903e-01f, -1.645945903e-01f, -4.759473930e-01f,
+    -7.357239107e-01f, -9.157733267e-01f, -9.965844930e-01f, -9.694002659e-01f,
+    -8.371664783e-01f, -6.142127127e-01f, -3.246994692e-01f, +0.000000000e+00f,
+    +2.697967712e-01f, +5.195839500e-01f, +7.308359643e-01f, +8.878852184e-01f,
+    +9.790840877e-01f, +9.976687692e-01f, +9.422609221e-01f, +8.169698930e-01f,
+    +6.310879443e-01f, +3.984010898e-01f, +1.361666491e-01f, -1.361666491e-01f,
+    -3.984010898e-01f, -6.310879443e-01f, -8.169698930e-01f, -9.422609221e-01f,
+    -9.976687692e-01f, -9.790840877e-01f, -8.878852184e-01f, -7.308359643e-01f,
+    -5.195839500e-01f, -2.697967712e-01f, +0.000000000e+00f, +2.149704402e-01f,
+    +4.198891016e-01f, +6.051742152e-01f, +7.621620551e-01f, +8.835120444e-01f,
+    +9.635499925e-01f, +9.985334139e-01f, +9.868265225e-01f, +9.289767198e-01f,
+    +8.276889982e-01f, +6.876994589e-01f, +5.155538572e-01f, +3.193015301e-01f,
+    +1.081190184e-01f, -1.081190184e-01f, -3.193015301e-01f, -5.155538572e-01f,
+    -6.876994589e-01f, -8.276889982e-01f, -9.289767198e-01f, -9.868265225e-01f,
+    -9.985334139e-01f, -9.635499925e-01f, -8.835120444e-01f, -7.621620551e-01f,
+    -6.051742152e-01f, -4.198891016e-01f, -2.149704402e-01f, +0.000000000e+00f,
+    +2.012985201e-01f, +3.943558551e-01f, +5.712682151e-01f, +7.247927872e-01f,
+    +8.486442575e-01f, +9.377521321e-01f, +9.884683243e-01f, +9.987165072e-01f,
+    +9.680771189e-01f, +8.978045396e-01f, +7.907757369e-01f, +6.513724827e-01f,
+    +4.853019625e-01f, +2.993631230e-01f, +1.011683220e-01f, -1.011683220e-01f,
+    -2.993631230e-01f, -4.853019625e-01f, -6.513724827e-01f, -7.907757369e-01f,
+    -8.978045396e-01f, -9.680771189e-01f, -9.987165072e-01f, -9.884683243e-01f,
+    -9.377521321e-01f, -8.486442575e-01f, -7.247927872e-01f, -5.712682151e-01f,
+    -3.943558551e-01f, -2.012985201e-01f};
+// offsets: R3:0, R5:3, R7:8, R11:15, R13:26, R17:39, R19:56, R23:75, R29:98, R31:127
+
+template <int R>
+struct OddRadixOffset;
+template <> struct OddRadixOffset<3> { static constexpr int v = 0; };
+template <> struct OddRadixOffset<5> { static constexpr int v = 3; };
+template <> struct OddRadixOffset<7> { static constexpr int v = 8; };
+template <> struct OddRadixOffset<11> { static constexpr int v = 15; };
+template <> struct OddRadixOffset<13> { static constexpr int v = 26; };
+template <> struct OddRadixOffset<17> { static constexpr int v = 39; };
+template <> struct OddRadixOffset<19> { static constexpr int v = 56; };
+template <> struct OddRadixOffset<23> { static constexpr int v = 75; };
+template <> struct OddRadixOffset<29> { static constexpr int v = 98; };
+template <> struct OddRadixOffset<31> { static constexpr int v = 127; };
+
+// ---- in-register forward DFT kernels -------------------------------------
+
+__device__ __forceinline__ void dft2(float2 (&x)[2]) {
+  float2 a = x[0], b = x[1];
+  x[0] = cadd(a, b);
+  x[1] = csub(a, b);
+}
+
+__device__ __forceinline__ void dft4_vals(float2& b0, float2& b1, float2& b2, float2& b3) {
+  float2 t0 = cadd(b0, b2), t1 = csub(b0, b2), t2 = cadd(b1, b3), t3 = csub(b1, b3);
+  b0 = cadd(t0, t2);
+  b2 = csub(t0, t2);
+  b1 = cadd(t1, mul_mi(t3));
+  b3 = cadd(t1, mul_pi(t3));
+}
+
+__device__ __forceinline__ void dft4(float2 (&x)[4]) { dft4_vals(x[0], x[1], x[2], x[3]); }
+
+__device__ __forceinline__ void dft8(float2 (&x)[8]) {
+  const float h = 0.70710678118654752f;
+  float2 a0 = cadd(x[0], x[4]), a4 = csub(x[0], x[4]);
+  float2 a1 = cadd(x[1], x[5]), a5 = csub(x[1], x[5]);
+  float2 a2 = cadd(x[2], x[6]), a6 = csub(x[2], x[6]);
+  float2 a3 = cadd(x[3], x[7]), a7 = csub(x[3], x[7]);
+  // a5 *= exp(-i pi/4), a6 *= -i, a7 *= exp(-3 i pi/4)
+  a5 = make_float2(h * (a5.x + a5.y), h * (a5.y - a5.x));
+  a6 = mul_mi(a6);
+  a7 = make_float2(h * (a7.y - a7.x), -h * (a7.x + a7.y));
+  dft4_vals(a0, a1, a2, a3);
+  dft4_vals(a4, a5, a6, a7);
+  x[0] = a0; x[2] = a1; x[4] = a2; x[6] = a3;
+  x[1] = a4; x[3] = a5; x[5] = a6; x[7] = a7;
+}
+
+// Odd-length DFT through the symmetric form
+//   y_k = x0 + sum_j (x_j + x_{R-j}) cos(2 pi jk/R) - i (x_j - x_{R-j}) sin(2 pi jk/R)
+template <int R>
+__device__ __forceinline__ void dft_odd(float2 (&x)[R]) {
+  constexpr int H = (R - 1) / 2;
+  constexpr int OFF = OddRadixOffset<R>::v;
+  float2 a[H], b[H];
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    a[j - 1] = cadd(x[j], x[R - j]);
+    b[j - 1] = csub(x[j], x[R - j]);
+  }
+  float2 y0 = x[0];
+#pragma unroll
+  for (int j = 0; j < H; ++j) y0 = cadd(y0, a[j]);
+  float2 y[R];
+#pragma unroll
+  for (int k = 1; k <= H; ++k) {
+    float2 A = x[0];
+    float2 B = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+      const int m = (j * k) % R;
+      const float c = kOddCos[OFF + m];
+      const float s = kOddSin[OFF + m];
+      A.x = fmaf(a[j - 1].x, c, A.x);
+      A.y = fmaf(a[j - 1].y, c, A.y);
+      B.x = fmaf(b[j - 1].x, s, B.x);
+      B.y = fmaf(b[j - 1].y, s, B.y);
+    }
+    y[k] = make_float2(A.x + B.y, A.y - B.x);
+    y[R - k] = make_float2(A.x - B.y, A.y + B.x);
+  }
+  x[0] = y0;
+#pragma unroll
+  for (int k = 1; k < R; ++k) x[k] = y[k];
+}
+
+template <int R>
+__device__ __forceinline__ void dft_any(float2 (&x)[R]) {
+  if constexpr (R == 2) {
+    dft2(x);
+  } else if constexpr (R == 4) {
+    dft4(x);
+  } else if constexpr (R == 8) {
+    dft8(x);
+  } else {
+    dft_odd<R>(x);
+  }
+}
+
+// ---- in-place mixed-radix stages -----------------------------------------
+// Stage s (radix r = p.radix[s]) works on blocks of B = r * L points, where
+// L = n / (r_0 ... r_s). Butterfly (block, j), j < L, owns the points
+// block*B + j + t*L (t < r) and writes its results back to the same points,
+// so only one butterfly is live per thread and one barrier ends a stage.
+//   DIF (natural order in, digit-reversed out):  y_t = w_B^{t j} * DFT_r(x)_t
+//   DIT (digit-reversed in, natural order out):  y = DFT_r(w_B^{t j} * x_t)
+// The DIT stages are the transposes of the DIF stages run in reverse order,
+// so DIT(DIF(x)) with one of them inverse returns n*x. The point that holds
+// frequency k after a DIF is fft_digit_pos(k) (table fft_perm).
+
+template <int R, int T, bool DIT>
+__device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float2* __restrict__ tw,
+                                          int tw_step, bool conj_in, bool conj_out) {
+  const int nb = n / R;
+  const int B = L * R;
+  for (int b = threadIdx.x; b < nb; b += T) {
+    const int blk = b / L;
+    const int j = b - blk * L;
+    const int base = blk * B + j;
+    float2 x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) {
+      float2 e = buf[base + t * L];
+      x[t] = conj_in ? conjf2(e) : e;
+    }
+    if (DIT && j != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], __ldg(tw + t * j * tw_step));
+    }
+    dft_any<R>(x);
+    if (!DIT && j != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], __ldg(tw + t * j * tw_step));
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[base + t * L] = conj_out ? conjf2(x[t]) : x[t];
+  }
+  __syncthreads();
+}
+
+template <int T, bool DIT>
+__device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, int R, int L,
+                                              int tw_step, bool ci, bool co) {
+  switch (R) {
+    case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 8: fft_stage_ip<8, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 3: fft_stage_ip<3, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 5: fft_stage_ip<5, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 7: fft_stage_ip<7, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 11: fft_stage_ip<11, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 13: fft_stage_ip<13, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 17: fft_stage_ip<17, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 19: fft_stage_ip<19, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 23: fft_stage_ip<23, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 29: fft_stage_ip<29, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 31: fft_stage_ip<31, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    default: break;  // rejected by fft_make_plan
+  }
+}
+
+// Natural-order input, digit-reversed output. All T threads must call it
+// after buf is written and the CTA synchronised; the result is visible to
+// the CTA on return.
+template <int T>
+__device__ void fft_dif(float2* buf, const FftPlan& p, bool inverse) {
+  int L = p.n;
+  int Rprod = 1;  // r_0 ... r_{s-1}
+  for (int s = 0; s < p.nstages; ++s) {
+    const int R = p.radix[s];
+    L /= R;
+    // block length B = L*R = n / Rprod; twiddle w_B^{tj} = w_n^{t j Rprod}
+    const int tw_step = Rprod * p.tw_stride;
+    fft_run_stage<T, false>(buf, p, R, L, tw_step, inverse && s == 0,
+                            inverse && s == p.nstages - 1);
+    Rprod *= R;
+  }
+}
+
+// Digit-reversed input (the layout fft_dif produces), natural-order output.
+template <int T>
+__device__ void fft_dit(float2* buf, const FftPlan& p, bool inverse) {
+  int L = 1;
+  int Rprod = p.n;
+  for (int s = p.nstages - 1; s >= 0; --s) {
+    const int R = p.radix[s];
+    Rprod /= R;
+    const int tw_step = Rprod * p.tw_stride;
+    fft_run_stage<T, true>(buf, p, R, L, tw_step, inverse && s == p.nstages - 1,
+                           inverse && s == 0);
+    L *= R;
+  }
+}
+
+// Position of natural-order frequency k in the digit-reversed layout:
+// k = d_0 + r_0 d_1 + r_0 r_1 d_2 + ...  ->  pos = d_0 L_0 + d_1 L_1 + ...
+__host__ __device__ inline int fft_digit_pos(const FftPlan& p, int k) {
+  int pos = 0;
+  int L = p.n;
+  for (int s = 0; s < p.nstages; ++s) {
+    const int R = p.radix[s];
+    L /= R;
+    const int d = k % R;
+    k /= R;
+    pos += d * L;
+  }
+  return pos;
+}
+
+}  // namespace fxc

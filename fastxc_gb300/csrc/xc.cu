@@ -1,0 +1,421 @@
+// xc_fast hot path: per-pair conjugate spectral product stacked over windows,
+// then the inverse real FFT and the +-max_lag cut.
+//
+// Reference behaviour reproduced here:
+//   accumulateStepXc2DKernel    native/xc/kernels/cuda.kernels.cu:16-36
+//   per-step launch loop        native/xc/worker/async_workers.cu:61-83
+//   finalize_xc_batch           native/xc/worker/executor.cu:6-55
+//   finalize_shape              native/xc/io/input.cu:1033-1054
+//
+// GB300 design:
+//   * the reference launches one kernel per window and read-modify-writes the
+//     whole [pair][freq] stack in HBM each time; here one launch keeps the
+//     stack of a register tile of 8 x 8 pairs in registers across all windows
+//     and writes each stacked bin once;
+//   * pairs are grouped into 16 x 16 channel tiles so every loaded spectrum
+//     value feeds 8 pairs from registers (2 flop per loaded byte);
+//   * the finalize kernel fuses the (-1)^f phase shift (folded into the lag
+//     index), the C2R transform, the 1/(nfft*dt) scaling and the lag cut:
+//     one CTA per pair, the half-length complex row in shared memory, only
+//     cc_size samples written back.
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "context.cuh"
+#include "fft.cuh"
+#include "fft_launch.cuh"
+#include "xc.cuh"
+
+namespace fxc {
+
+// ---------------------------------------------------------------------------
+// Pair plan
+// ---------------------------------------------------------------------------
+
+int pairplan_build(const int32_t* src, const int32_t* rec, int64_t npairs, int32_t nchan,
+                   std::vector<XcTile>* tiles, std::vector<int32_t>* maps) {
+  tiles->clear();
+  maps->clear();
+  // (src_block, rec_block) -> tile index; a slot collision (a duplicate pair)
+  // spills the pair into a further layer of tiles.
+  std::vector<std::map<std::pair<int32_t, int32_t>, int32_t>> layers(1);
+  for (int64_t p = 0; p < npairs; ++p) {
+    const int32_t s = src[p], r = rec[p];
+    if (s < 0 || s >= nchan || r < 0 || r >= nchan) {
+      set_error("pair %lld has channel (%d,%d) outside [0,%d)", (long long)p, s, r, nchan);
+      return FXC_ERR_INVALID;
+    }
+    const int32_t sb = s / kXcTile, rb = r / kXcTile;
+    const int slot = (s % kXcTile) * kXcTile + (r % kXcTile);
+    for (size_t layer = 0;; ++layer) {
+      if (layer == layers.size()) layers.emplace_back();
+      auto key = std::make_pair(sb, rb);
+      auto it = layers[layer].find(key);
+      int32_t t;
+      if (it == layers[layer].end()) {
+        t = (int32_t)tiles->size();
+        layers[layer][key] = t;
+        XcTile tile;
+        tile.a_base = sb * kXcTile;
+        tile.b_base = rb * kXcTile;
+        tile.map_offset = t * kXcTile * kXcTile;
+        tile.npairs = 0;
+        tiles->push_back(tile);
+        maps->insert(maps->end(), kXcTile * kXcTile, -1);
+      } else {
+        t = it->second;
+      }
+      int32_t& cell = (*maps)[(size_t)(*tiles)[t].map_offset + slot];
+      if (cell < 0) {
+        cell = (int32_t)p;
+        (*tiles)[t].npairs++;
+        break;
+      }
+    }
+  }
+  // Order tiles by (a_base, b_base) so consecutive CTAs share channels in L2.
+  std::vector<int32_t> order(tiles->size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int32_t)i;
+  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+    const XcTile &a = (*tiles)[x], &b = (*tiles)[y];
+    if (a.a_base != b.a_base) return a.a_base < b.a_base;
+    return a.b_base < b.b_base;
+  });
+  std::vector<XcTile> t2(tiles->size());
+  std::vector<int32_t> m2(maps->size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    XcTile t = (*tiles)[order[i]];
+    std::copy(maps->begin() + t.map_offset, maps->begin() + t.map_offset + kXcTile * kXcTile,
+              m2.begin() + i * kXcTile * kXcTile);
+    t.map_offset = (int32_t)(i * kXcTile * kXcTile);
+    t2[i] = t;
+  }
+  tiles->swap(t2);
+  maps->swap(m2);
+  return FXC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP32 stack kernel
+// ---------------------------------------------------------------------------
+// CTA = one 16x16 channel tile x kXcFreqChunk consecutive bins.
+// Thread (f = tid % 64, quadrant q = tid / 64): 8 src x 8 rec pairs for bin f.
+
+__device__ __forceinline__ void xc_load8(float2 (&v)[8], const float2* __restrict__ spec,
+                                         int64_t row0, int64_t pitch, int f, int ch0, int nchan,
+                                         const uint8_t* __restrict__ mrow, bool fok) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int ch = ch0 + i;
+    bool ok = fok && ch < nchan;
+    if (mrow != nullptr && ok) ok = mrow[ch] != 0;
+    v[i] = ok ? __ldg(spec + (row0 + ch) * pitch + f) : make_float2(0.f, 0.f);
+  }
+}
+
+__global__ void __launch_bounds__(256, 1)
+    k_xc_stack_plain(const float2* __restrict__ spec, int64_t nwin, int nchan, int nspec,
+                     int64_t spec_pitch, const uint8_t* __restrict__ mask,
+                     const XcTile* __restrict__ tiles, const int32_t* __restrict__ maps,
+                     float scale, float2* __restrict__ stack, int64_t stack_pitch) {
+  const XcTile tile = tiles[blockIdx.x];
+  const int f = blockIdx.y * kXcFreqChunk + (threadIdx.x % kXcFreqChunk);
+  const int q = threadIdx.x / kXcFreqChunk;
+  const int qa = q & 1, qb = q >> 1;
+  const int a0 = tile.a_base + qa * 8;
+  const int b0 = tile.b_base + qb * 8;
+  const bool fok = f < nspec;
+
+  float acc_re[8][8], acc_im[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      acc_re[i][j] = 0.f;
+      acc_im[i][j] = 0.f;
+    }
+
+  float2 ya[8], yb[8], na[8], nb[8];
+  if (nwin > 0) {
+    const uint8_t* m0 = mask ? mask : nullptr;
+    xc_load8(ya, spec, 0, spec_pitch, f, a0, nchan, m0, fok);
+    xc_load8(yb, spec, 0, spec_pitch, f, b0, nchan, m0, fok);
+  }
+  for (int64_t w = 0; w < nwin; ++w) {
+    if (w + 1 < nwin) {
+      const int64_t row = (w + 1) * nchan;
+      const uint8_t* mr = mask ? mask + row : nullptr;
+      xc_load8(na, spec, row, spec_pitch, f, a0, nchan, mr, fok);
+      xc_load8(nb, spec, row, spec_pitch, f, b0, nchan, mr, fok);
+    }
+    // conj(a) * b = (ar*br + ai*bi) + i (ar*bi - ai*br)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        acc_re[i][j] = fmaf(ya[i].x, yb[j].x, acc_re[i][j]);
+        acc_re[i][j] = fmaf(ya[i].y, yb[j].y, acc_re[i][j]);
+        acc_im[i][j] = fmaf(ya[i].x, yb[j].y, acc_im[i][j]);
+        acc_im[i][j] = fmaf(-ya[i].y, yb[j].x, acc_im[i][j]);
+      }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      ya[i] = na[i];
+      yb[i] = nb[i];
+    }
+  }
+  if (!fok) return;
+  const int32_t* map = maps + tile.map_offset;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int32_t p = __ldg(map + (qa * 8 + i) * kXcTile + qb * 8 + j);
+      if (p >= 0)
+        stack[(int64_t)p * stack_pitch + f] = make_float2(acc_re[i][j] * scale, acc_im[i][j] * scale);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Finalize: (-1)^f shift, C2R(nfft), 1/(nfft*dt), lag cut
+// ---------------------------------------------------------------------------
+// out[j] = x[(nfft - half_cc + j) mod nfft] * inv_norm, where x is the
+// unshifted C2R result; multiplying bin f by (-1)^f shifts the series by
+// nfft/2, so the reference's cut start nfft/2 - half_cc lands here.
+
+template <int T, int NMAX>
+__global__ void __launch_bounds__(T, 1)
+    k_xc_finalize(const float2* __restrict__ stack, int64_t stack_pitch, FftPlan p,
+                  const float2* __restrict__ twn, int half_cc, int cc_size, float inv_norm_f,
+                  double inv_norm, float* __restrict__ ncf) {
+  extern __shared__ float2 buf[];
+  const int M = p.n;
+  const int N = 2 * M;
+  const float2* X = stack + (int64_t)blockIdx.x * stack_pitch;
+  for (int k = threadIdx.x; k < M; k += T) buf[k] = c2r_pre(X, M, k, twn);
+  __syncthreads();
+  fft_dif<T>(buf, p, true);
+  float* out = ncf + (int64_t)blockIdx.x * cc_size;
+  for (int j = threadIdx.x; j < cc_size; j += T) {
+    int m = N - half_cc + j;
+    if (m >= N) m -= N;
+    const float2 v = buf[__ldg(p.perm + (m >> 1))];
+    const float x = (m & 1) ? v.y : v.x;
+    // InvNormalize2DKernel: float data times a double weight
+    out[j] = (float)((double)x * inv_norm);
+  }
+  (void)inv_norm_f;
+}
+
+int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin,
+                    int nchan, int nspec, int64_t spec_pitch, const uint8_t* mask, float scale,
+                    float2* stack, int64_t stack_pitch, int method) {
+  if (plan->npairs == 0 || nspec == 0) return FXC_OK;
+  if (method == FXC_XC_TENSOR) return xc_stack_tensor_launch(ctx, plan, spec, nwin, nchan, nspec,
+                                                             spec_pitch, mask, scale, stack,
+                                                             stack_pitch);
+  FXC_CHECK_ARG(method == FXC_XC_PLAIN, "unknown xc method %d", method);
+  const int64_t nchunks = ceil_div(nspec, kXcFreqChunk);
+  FXC_CHECK_ARG(nchunks <= 65535, "nspec %d too large for the grid", nspec);
+  dim3 grid((unsigned)plan->ntiles, (unsigned)nchunks);
+  k_xc_stack_plain<<<grid, 256, 0, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch, mask,
+                                                  plan->d_tiles, plan->d_maps, scale, stack,
+                                                  stack_pitch);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_t stack_pitch,
+                       const fxc_xc_shape* s, float* ncf) {
+  if (npairs == 0) return FXC_OK;
+  const int N = s->nfft;
+  FXC_CHECK_ARG(N % 2 == 0 && N >= 2, "nfft %d must be even", N);
+  const int M = N / 2;
+  FXC_CHECK_ARG(M <= kFftLargeNmax, "nfft %d above the in-CTA FFT limit %d", N, 2 * kFftLargeNmax);
+  FXC_CHECK_ARG(npairs <= 0x7fffffff, "too many pairs for one launch");
+  const float2* twn = nullptr;
+  FXC_TRY(fft_twiddles(N, &twn));
+  FftPlan p;
+  FXC_TRY(fft_make_plan(M, twn, 2, &p));
+  // 1/(width*dt) with width*dt in float, as InvNormalize2DKernel computes it
+  const float wdt = (float)N * s->dt;
+  const double inv_norm = 1.0 / (double)wdt;
+  const size_t smem = sizeof(float2) * (size_t)M;
+  if (M <= kFftSmallNmax) {
+    k_xc_finalize<kFftSmallT, kFftSmallNmax><<<(unsigned)npairs, kFftSmallT, smem, ctx->stream>>>(
+        stack, stack_pitch, p, twn, s->half_cc, s->cc_size, (float)inv_norm, inv_norm, ncf);
+  } else {
+    FXC_TRY(set_smem_limit(k_xc_finalize<kFftLargeT, kFftLargeNmax>, smem));
+    k_xc_finalize<kFftLargeT, kFftLargeNmax><<<(unsigned)npairs, kFftLargeT, smem, ctx->stream>>>(
+        stack, stack_pitch, p, twn, s->half_cc, s->cc_size, (float)inv_norm, inv_norm, ncf);
+  }
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+int64_t xc_stack_pitch(int nspec) { return (int64_t)((nspec + 3) / 4) * 4; }
+
+}  // namespace fxc
+
+using namespace fxc;
+
+extern "C" {
+
+int fxc_xc_shape_init(int32_t nspec, int32_t nstep, float dt, float cc_length, fxc_xc_shape* out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "out is null");
+  FXC_CHECK_ARG(nspec >= 2 && nstep > 0 && dt > 0.0f && cc_length > 0.0f,
+                "invalid shape nspec=%d nstep=%d dt=%g cc_length=%g", nspec, nstep, dt, cc_length);
+  fxc_xc_shape s;
+  s.nspec = nspec;
+  s.nstep = nstep;
+  s.dt = dt;
+  s.nfft = 2 * (nspec - 1);
+  s.half_cc = (int32_t)llround((double)cc_length / (double)dt);
+  if (s.half_cc >= nspec) s.half_cc = nspec - 1;
+  s.cc_size = 2 * s.half_cc + 1;
+  FXC_CHECK_ARG(s.cc_size > 0 && s.cc_size <= s.nfft, "cc_size %d invalid for nfft %d", s.cc_size,
+                s.nfft);
+  *out = s;
+  return FXC_OK;
+}
+
+int fxc_pairplan_create(fxc_ctx* ctx, const int32_t* h_src, const int32_t* h_rec, int64_t npairs,
+                        int32_t nchan, fxc_pairplan** out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "out is null");
+  *out = nullptr;
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0 && nchan > 0, "npairs=%lld nchan=%d", (long long)npairs, nchan);
+  FXC_CHECK_ARG(npairs == 0 || (h_src && h_rec), "null pair arrays");
+  FXC_CHECK_ARG(npairs < 0x7fffffff, "npairs exceeds int32 range");
+  std::vector<XcTile> tiles;
+  std::vector<int32_t> maps;
+  FXC_TRY(pairplan_build(h_src, h_rec, npairs, nchan, &tiles, &maps));
+  fxc_pairplan* p = new (std::nothrow) fxc_pairplan();
+  if (!p) {
+    set_error("host allocation failed");
+    return FXC_ERR_NOMEM;
+  }
+  p->device = ctx->device;
+  p->npairs = npairs;
+  p->nchan = nchan;
+  p->ntiles = (int64_t)tiles.size();
+  p->h_src.assign(h_src, h_src + npairs);
+  p->h_rec.assign(h_rec, h_rec + npairs);
+  if (!tiles.empty()) {
+    cudaError_t e1 = cudaMalloc(&p->d_tiles, sizeof(XcTile) * tiles.size());
+    cudaError_t e2 = cudaMalloc(&p->d_maps, sizeof(int32_t) * maps.size());
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      (void)cudaGetLastError();
+      fxc_pairplan_destroy(p);
+      set_error("cudaMalloc of pair plan failed");
+      return FXC_ERR_NOMEM;
+    }
+    cudaError_t e3 = cudaMemcpy(p->d_tiles, tiles.data(), sizeof(XcTile) * tiles.size(),
+                                cudaMemcpyHostToDevice);
+    cudaError_t e4 = cudaMemcpy(p->d_maps, maps.data(), sizeof(int32_t) * maps.size(),
+                                cudaMemcpyHostToDevice);
+    if (e3 != cudaSuccess || e4 != cudaSuccess) {
+      fxc_pairplan_destroy(p);
+      set_error("upload of pair plan failed: %s", cudaGetErrorString(e3 != cudaSuccess ? e3 : e4));
+      return FXC_ERR_CUDA;
+    }
+  }
+  FXC_TRY(xc_tensor_plan_init(ctx, p));
+  *out = p;
+  return FXC_OK;
+}
+
+int fxc_pairplan_destroy(fxc_pairplan* plan) {
+  if (!plan) return FXC_OK;
+  cudaSetDevice(plan->device);
+  if (plan->d_tiles) cudaFree(plan->d_tiles);
+  if (plan->d_maps) cudaFree(plan->d_maps);
+  xc_tensor_plan_free(plan);
+  delete plan;
+  return FXC_OK;
+}
+
+int64_t fxc_pairplan_npairs(const fxc_pairplan* plan) { return plan ? plan->npairs : -1; }
+int64_t fxc_pairplan_ntiles(const fxc_pairplan* plan) { return plan ? plan->ntiles : -1; }
+
+int fxc_xc_stack(fxc_ctx* ctx, const fxc_pairplan* plan, const float* d_spec, int64_t nwin,
+                 int32_t nchan, int32_t nspec, int64_t spec_pitch, const uint8_t* d_mask,
+                 float scale, float* d_stack, int64_t stack_pitch, int method) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(plan != nullptr, "null pair plan");
+  FXC_CHECK_ARG(nchan == plan->nchan, "nchan %d differs from the plan's %d", nchan, plan->nchan);
+  FXC_CHECK_ARG(nwin >= 0 && nspec >= 1 && spec_pitch >= nspec && stack_pitch >= nspec,
+                "invalid shape nwin=%lld nspec=%d spec_pitch=%lld stack_pitch=%lld",
+                (long long)nwin, nspec, (long long)spec_pitch, (long long)stack_pitch);
+  FXC_CHECK_ARG(plan->npairs == 0 || (d_spec && d_stack), "null data pointer");
+  return xc_stack_launch(ctx, plan, reinterpret_cast<const float2*>(d_spec), nwin, nchan, nspec,
+                         spec_pitch, d_mask, scale, reinterpret_cast<float2*>(d_stack), stack_pitch,
+                         method);
+}
+
+int fxc_xc_finalize(fxc_ctx* ctx, const float* d_stack, int64_t npairs, int64_t stack_pitch,
+                    const fxc_xc_shape* shape, float* d_ncf) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(shape != nullptr, "null shape");
+  FXC_CHECK_ARG(npairs >= 0 && stack_pitch >= shape->nspec, "invalid npairs/pitch");
+  FXC_CHECK_ARG(npairs == 0 || (d_stack && d_ncf), "null data pointer");
+  FXC_CHECK_ARG(shape->nfft == 2 * (shape->nspec - 1) && shape->cc_size == 2 * shape->half_cc + 1,
+                "inconsistent shape");
+  return xc_finalize_launch(ctx, reinterpret_cast<const float2*>(d_stack), npairs, stack_pitch,
+                            shape, d_ncf);
+}
+
+int fxc_xc_run(fxc_ctx* ctx, const fxc_pairplan* plan, const float* d_spec, int64_t nwin,
+               int32_t nchan, int64_t spec_pitch, const uint8_t* d_mask, float scale,
+               const fxc_xc_shape* shape, float* d_ncf, int method) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(plan != nullptr && shape != nullptr, "null plan or shape");
+  if (plan->npairs == 0) return FXC_OK;
+  const int64_t pitch = xc_stack_pitch(shape->nspec);
+  FXC_TRY(ctx->scratch.reserve(sizeof(float2) * (size_t)pitch * (size_t)plan->npairs));
+  float* stack = reinterpret_cast<float*>(ctx->scratch.ptr);
+  FXC_TRY(fxc_xc_stack(ctx, plan, d_spec, nwin, nchan, shape->nspec, spec_pitch, d_mask, scale,
+                       stack, pitch, method));
+  return fxc_xc_finalize(ctx, stack, plan->npairs, pitch, shape, d_ncf);
+}
+
+int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec, int64_t nwin,
+                    int32_t nchan, int64_t spec_pitch, const uint8_t* h_mask, float scale,
+                    const fxc_xc_shape* shape, float* h_ncf, int method) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(plan != nullptr && shape != nullptr, "null plan or shape");
+  FXC_CHECK_ARG(h_spec != nullptr && h_ncf != nullptr, "null host pointer");
+  if (plan->npairs == 0) return FXC_OK;
+  const size_t spec_bytes = sizeof(float2) * (size_t)nwin * (size_t)nchan * (size_t)spec_pitch;
+  const size_t mask_bytes = h_mask ? (size_t)nwin * (size_t)nchan : 0;
+  const size_t ncf_bytes = sizeof(float) * (size_t)plan->npairs * (size_t)shape->cc_size;
+  const size_t a = 256;
+  const size_t off_mask = (spec_bytes + a - 1) / a * a;
+  const size_t off_ncf = off_mask + (mask_bytes + a - 1) / a * a;
+  FXC_TRY(ctx->scratch2.reserve(off_ncf + ncf_bytes));
+  char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
+  FXC_CUDA_TRY(cudaMemcpyAsync(base, h_spec, spec_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  const uint8_t* d_mask = nullptr;
+  if (h_mask) {
+    FXC_CUDA_TRY(
+        cudaMemcpyAsync(base + off_mask, h_mask, mask_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    d_mask = reinterpret_cast<const uint8_t*>(base + off_mask);
+  }
+  float* d_ncf = reinterpret_cast<float*>(base + off_ncf);
+  FXC_TRY(fxc_xc_run(ctx, plan, reinterpret_cast<const float*>(base), nwin, nchan, spec_pitch,
+                     d_mask, scale, shape, d_ncf, method));
+  FXC_CUDA_TRY(cudaMemcpyAsync(h_ncf, d_ncf, ncf_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,47 @@
+// Internal declarations of the xc stage (correlation + stack + finalize).
+#pragma once
+
+#include <vector>
+
+#include "context.cuh"
+
+namespace fxc {
+
+constexpr int kXcTile = 16;       // channels per tile side
+constexpr int kXcFreqChunk = 64;  // bins per CTA of the plain kernel
+
+struct XcTile {
+  int32_t a_base;      // first src channel of the tile
+  int32_t b_base;      // first rec channel of the tile
+  int32_t map_offset;  // offset of the 16x16 pair-index map in the map array
+  int32_t npairs;      // pairs mapped into the tile
+};
+
+struct XcTensorPlan;
+
+int pairplan_build(const int32_t* src, const int32_t* rec, int64_t npairs, int32_t nchan,
+                   std::vector<XcTile>* tiles, std::vector<int32_t>* maps);
+int64_t xc_stack_pitch(int nspec);
+
+}  // namespace fxc
+
+struct fxc_pairplan {
+  int device = 0;
+  int64_t npairs = 0;
+  int32_t nchan = 0;
+  int64_t ntiles = 0;
+  std::vector<int32_t> h_src, h_rec;
+  fxc::XcTile* d_tiles = nullptr;
+  int32_t* d_maps = nullptr;
+  fxc::XcTensorPlan* tensor = nullptr;
+};
+
+namespace fxc {
+
+int xc_tensor_plan_init(fxc_ctx* ctx, fxc_pairplan* plan);
+void xc_tensor_plan_free(fxc_pairplan* plan);
+int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
+                           int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
+                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch);
+
+}  // namespace fxc

@@ -1,0 +1,150 @@
+/*
+ * fastxc_gb300 -- C ABI of the GB300 (sm_103a) ambient-noise correlation
+ * library.
+ *
+ * The reference (wangkingh/FastXC) has no library ABI: its boundary is
+ * "Python builds an argv string -> native executable -> files + exit code"
+ * (fastxc/runtime/command_runner.py:97-210). This header is the thin library
+ * that sits under drop-in replacements for those executables. Every entry
+ * point below names the reference function or kernel whose behaviour it
+ * reproduces.
+ *
+ * Conventions
+ *   - Every function returns FXC_OK (0) or a negative FXC_ERR_* status; the
+ *     message of the last failure on the calling thread is fxc_last_error().
+ *     Nothing in the library calls exit().
+ *   - Complex arrays are interleaved float pairs (re, im), the layout of
+ *     cuComplex / numpy complex64. Pitches of complex arrays count complex
+ *     elements; pitches of real arrays count floats.
+ *   - "d_" pointers are device pointers on the context's device; "h_"
+ *     pointers are host pointers (pinned memory gives full copy speed,
+ *     pageable memory works).
+ *   - Work is enqueued on the context's stream; functions return once the
+ *     work is enqueued unless documented as synchronous (the *_host calls).
+ *   - A context is used by one thread at a time; distinct contexts may be
+ *     used concurrently.
+ */
+#ifndef FASTXC_GB300_H
+#define FASTXC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FXC_OK 0
+#define FXC_ERR_INVALID (-1)     /* bad argument or shape */
+#define FXC_ERR_CUDA (-2)        /* CUDA runtime error (message has the name) */
+#define FXC_ERR_UNSUPPORTED (-3) /* transform length / shape not supported */
+#define FXC_ERR_NOMEM (-4)       /* device or host allocation failed */
+#define FXC_ERR_IO (-5)          /* file format or I/O error */
+#define FXC_ERR_NODEVICE (-6)    /* no CUDA device / driver */
+
+#define FXC_XC_PLAIN 0  /* FP32 CUDA-core per-pair product, register blocked */
+#define FXC_XC_TENSOR 1 /* BF16 hi/lo split tcgen05 contraction S(f)=Y^H Y */
+
+typedef struct fxc_ctx fxc_ctx;
+typedef struct fxc_pairplan fxc_pairplan;
+
+/* ---- library / context --------------------------------------------------- */
+
+/* Message of the last failure on this thread ("" when none). */
+const char *fxc_last_error(void);
+/* ABI version: major*10000 + minor*100 + patch. */
+int fxc_version(void);
+/* Number of kernel launches the library made on this thread since the last
+ * reset; lets callers attribute device work to the library. */
+int64_t fxc_launch_count(void);
+void fxc_launch_count_reset(void);
+
+/* Create a context bound to `device`. `stream` is a cudaStream_t (NULL = the
+ * legacy default stream). The context owns its scratch buffers and FFT
+ * tables. */
+int fxc_ctx_create(int device, void *stream, fxc_ctx **out);
+int fxc_ctx_destroy(fxc_ctx *ctx);
+int fxc_ctx_set_stream(fxc_ctx *ctx, void *stream);
+int fxc_ctx_synchronize(fxc_ctx *ctx);
+
+/* ---- FFT (replaces every cuFFT plan of the reference, SURVEY table 2.4) --- */
+
+/* Batched complex transform of length n, unnormalised (cuFFT convention:
+ * forward exp(-2 pi i jk/n), inverse exp(+2 pi i jk/n)). Row r of the input
+ * starts at d_in + 2*r*in_pitch floats. In-place is allowed. */
+int fxc_fft_c2c(fxc_ctx *ctx, const float *d_in, float *d_out, int n, int batch,
+                int64_t in_pitch, int64_t out_pitch, int inverse);
+/* Batched real-to-complex transform: n reals -> n/2+1 complex bins
+ * (cufftExecR2C). */
+int fxc_fft_r2c(fxc_ctx *ctx, const float *d_in, float *d_out, int n, int batch,
+                int64_t in_pitch, int64_t out_pitch);
+/* Batched complex-to-real transform: n/2+1 bins -> n reals, unnormalised
+ * (cufftExecC2R; the imaginary parts of the DC and Nyquist bins are
+ * ignored). n must be even. */
+int fxc_fft_c2r(fxc_ctx *ctx, const float *d_in, float *d_out, int n, int batch,
+                int64_t in_pitch, int64_t out_pitch);
+/* 1 if the length is supported by the fused in-CTA transforms. */
+int fxc_fft_supported(int n, int real_transform);
+
+/* ---- xc_fast: correlation + within-window linear stack ------------------ */
+
+typedef struct fxc_xc_shape {
+  int32_t nspec;   /* spectrum bins per window (output_nfft/2+1) */
+  int32_t nstep;   /* windows per timestamp */
+  int32_t nfft;    /* 2*(nspec-1) */
+  int32_t half_cc; /* llround(cc_length/dt), capped at nspec-1 */
+  int32_t cc_size; /* 2*half_cc+1 */
+  float dt;
+} fxc_xc_shape;
+
+/* finalize_shape (native/xc/io/input.cu:1033-1054). */
+int fxc_xc_shape_init(int32_t nspec, int32_t nstep, float dt, float cc_length,
+                      fxc_xc_shape *out);
+
+/* Build a correlation plan for the pair list (src[p], rec[p]) over channel
+ * indices in [0, nchan). The list order is the output order (the order of
+ * the reference's XcTask list, native/xc/worker/scheduler.cu:65-167). The
+ * plan groups pairs into register tiles of up to 16 x 16 channels. Host
+ * arrays; the plan uploads what the kernels need. */
+int fxc_pairplan_create(fxc_ctx *ctx, const int32_t *h_src, const int32_t *h_rec, int64_t npairs,
+                        int32_t nchan, fxc_pairplan **out);
+int fxc_pairplan_destroy(fxc_pairplan *plan);
+int64_t fxc_pairplan_npairs(const fxc_pairplan *plan);
+int64_t fxc_pairplan_ntiles(const fxc_pairplan *plan);
+
+/* stack[p, f] = scale * sum_w conj(Y[w, src_p, f]) * Y[w, rec_p, f]
+ * for f < nspec. d_spec is [nwin][nchan][spec_pitch] complex (the stepack
+ * payload layout, native/sac2spec/io/stepack_writer.c); d_stack is
+ * [npairs][stack_pitch] complex. Optional d_mask (NULL = none) is
+ * [nwin][nchan] uint8: a window with mask 0 contributes exactly zero.
+ * Replaces the nstep launches of accumulateStepXc2DKernel
+ * (native/xc/kernels/cuda.kernels.cu:16-36, loop at
+ * native/xc/worker/async_workers.cu:66-83). */
+int fxc_xc_stack(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, int64_t nwin,
+                 int32_t nchan, int32_t nspec, int64_t spec_pitch, const uint8_t *d_mask,
+                 float scale, float *d_stack, int64_t stack_pitch, int method);
+
+/* ncf[p, j] = C2R(stack[p] * (-1)^f)[nfft/2 - half_cc + j] / (nfft * dt),
+ * j < cc_size. d_ncf is [npairs][cc_size] float. Replaces
+ * finalize_xc_batch (native/xc/worker/executor.cu:6-55). */
+int fxc_xc_finalize(fxc_ctx *ctx, const float *d_stack, int64_t npairs, int64_t stack_pitch,
+                    const fxc_xc_shape *shape, float *d_ncf);
+
+/* fxc_xc_stack + fxc_xc_finalize with the stack in context scratch memory.
+ * scale is normally 1/nstep (async_workers.cu:66). */
+int fxc_xc_run(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, int64_t nwin,
+               int32_t nchan, int64_t spec_pitch, const uint8_t *d_mask, float scale,
+               const fxc_xc_shape *shape, float *d_ncf, int method);
+
+/* Host-buffer variant of fxc_xc_run: copies h_spec ([nwin][nchan][spec_pitch]
+ * complex) to the device, runs, copies the NCFs back to h_ncf
+ * ([npairs][cc_size]) and synchronises. */
+int fxc_xc_run_host(fxc_ctx *ctx, const fxc_pairplan *plan, const float *h_spec, int64_t nwin,
+                    int32_t nchan, int64_t spec_pitch, const uint8_t *h_mask, float scale,
+                    const fxc_xc_shape *shape, float *h_ncf, int method);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTXC_GB300_H */

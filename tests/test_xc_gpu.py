@@ -1,0 +1,158 @@
+"""xc_fast parity: library correlation + stack + finalize against the FP64 oracle.
+
+Tolerance: every NCF within relative L2 1e-5 of the FP64 restatement (the
+spec bound); the stacked spectra within 2e-6.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import xc_oracle as xo
+
+pytestmark = pytest.mark.gpu
+
+NCF_RTOL = 1e-5
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def per_row_rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    num = np.linalg.norm(a - b, axis=-1)
+    den = np.maximum(np.linalg.norm(b, axis=-1), 1e-300)
+    return num / den
+
+
+def station_pairs(nsta, ncomp=3, auto=False):
+    src, rec = [], []
+    for s in range(nsta):
+        for t in range(s if auto else s + 1, nsta):
+            for i in range(ncomp):
+                for j in range(ncomp):
+                    src.append(s * ncomp + i)
+                    rec.append(t * ncomp + j)
+    return np.array(src, np.int32), np.array(rec, np.int32)
+
+
+def make_spec(rng, nwin, nchan, nspec, coherent=True):
+    y = rng.standard_normal((nwin, nchan, nspec)) + 1j * rng.standard_normal((nwin, nchan, nspec))
+    if coherent:
+        common = rng.standard_normal((nwin, 1, nspec)) + 1j * rng.standard_normal((nwin, 1, nspec))
+        y = y + 2.0 * common
+    return y.astype(np.complex64)
+
+
+def run_xc(ctx, torch, spec, src, rec, shape, scale, mask=None, method=0):
+    from fastxc_gb300.core import PairPlan
+
+    nwin, nchan, pitch = spec.shape
+    plan = PairPlan(ctx, src, rec, nchan)
+    d_spec = torch.from_numpy(spec).cuda()
+    d_mask = torch.from_numpy(mask).cuda() if mask is not None else None
+    d_ncf = torch.empty((len(src), shape.cc_size), dtype=torch.float32, device="cuda")
+    ctx.xc_run(plan, d_spec, nwin, nchan, pitch, d_mask, scale, shape, d_ncf, method)
+    ctx.synchronize()
+    return d_ncf.cpu().numpy(), plan
+
+
+@pytest.mark.parametrize("nspec,nwin,nsta", [(1001, 5, 4), (18523, 24, 4)])
+def test_xc_ncf_matches_oracle(ctx, torch_cuda, nspec, nwin, nsta):
+    rng = np.random.default_rng(nspec + nwin)
+    nchan = 3 * nsta
+    spec = make_spec(rng, nwin, nchan, nspec)
+    src, rec = station_pairs(nsta)
+    shape = ctx_shape(nspec, nwin, 0.1, 100.0 if nspec > 5000 else 20.0)
+    scale = 1.0 / nwin
+    got, _ = run_xc(ctx, torch_cuda, spec, src, rec, shape, scale)
+    oshape = xo.finalize_shape(nspec, nwin, 0.1, 100.0 if nspec > 5000 else 20.0)
+    assert (shape.nfft, shape.half_cc, shape.cc_size) == (oshape.nfft, oshape.half_cc, oshape.cc_size)
+    ref = xo.xc_run(spec, src, rec, scale, oshape)
+    assert got.shape == ref.shape
+    assert per_row_rel_l2(got, ref).max() < NCF_RTOL
+
+
+def ctx_shape(nspec, nstep, dt, cc):
+    from fastxc_gb300.core import xc_shape
+
+    return xc_shape(nspec, nstep, dt, cc)
+
+
+def test_stack_matches_oracle_with_mask_and_ragged_tiles(ctx, torch_cuda):
+    """nchan not a multiple of the tile, masked windows, autocorrelations,
+    duplicate and unordered pairs."""
+    torch = torch_cuda
+    from fastxc_gb300.core import PairPlan
+
+    rng = np.random.default_rng(3)
+    nwin, nchan, nspec, pitch = 7, 37, 300, 304
+    spec = make_spec(rng, nwin, nchan, pitch)
+    src, rec = station_pairs(12, auto=True)
+    src = np.concatenate([src, [36, 5, 5, 0]]).astype(np.int32)
+    rec = np.concatenate([rec, [0, 5, 5, 36]]).astype(np.int32)
+    perm = rng.permutation(src.size)
+    src, rec = src[perm], rec[perm]
+    mask = (rng.random((nwin, nchan)) > 0.2).astype(np.uint8)
+    plan = PairPlan(ctx, src, rec, nchan)
+    d_spec = torch.from_numpy(spec).cuda()
+    d_mask = torch.from_numpy(mask).cuda()
+    spitch = 304
+    d_stack = torch.zeros((src.size, spitch), dtype=torch.complex64, device="cuda")
+    ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, pitch, d_mask, 0.25, d_stack, spitch)
+    ctx.synchronize()
+    got = d_stack.cpu().numpy()[:, :nspec]
+    ref = xo.xc_stack(spec[:, :, :nspec], src, rec, 0.25, mask)
+    assert rel_l2(got, ref) < 2e-6
+    assert np.all(d_stack.cpu().numpy()[:, nspec:] == 0)
+
+
+def test_zero_windows_contribute_zero(ctx, torch_cuda):
+    """A gap window (all-zero spectrum) changes nothing but the divisor stays nstep."""
+    rng = np.random.default_rng(11)
+    nwin, nsta, nspec = 6, 3, 1001
+    spec = make_spec(rng, nwin, 3 * nsta, nspec)
+    spec[2] = 0
+    src, rec = station_pairs(nsta)
+    shape = ctx_shape(nspec, nwin, 0.1, 20.0)
+    got, _ = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin)
+    keep = np.array([0, 1, 3, 4, 5])
+    ref = xo.xc_run(spec[keep], src, rec, 1.0 / nwin, xo.finalize_shape(nspec, nwin, 0.1, 20.0))
+    assert per_row_rel_l2(got, ref).max() < NCF_RTOL
+
+
+def test_empty_pair_list(ctx, torch_cuda):
+    torch = torch_cuda
+    from fastxc_gb300.core import PairPlan
+
+    plan = PairPlan(ctx, np.zeros(0, np.int32), np.zeros(0, np.int32), 6)
+    shape = ctx_shape(1001, 2, 0.1, 20.0)
+    d_spec = torch.zeros((2, 6, 1001), dtype=torch.complex64, device="cuda")
+    d_ncf = torch.zeros((1,), dtype=torch.float32, device="cuda")
+    ctx.xc_run(plan, d_spec, 2, 6, 1001, None, 0.5, shape, d_ncf)
+    ctx.synchronize()
+
+
+def test_host_entry_matches_device_entry(ctx, torch_cuda):
+    rng = np.random.default_rng(5)
+    nwin, nsta, nspec = 4, 4, 1001
+    spec = make_spec(rng, nwin, 3 * nsta, nspec)
+    src, rec = station_pairs(nsta)
+    shape = ctx_shape(nspec, nwin, 0.1, 20.0)
+    dev, plan = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin)
+    host = np.zeros_like(dev)
+    ctx.xc_run_host(plan, spec, nwin, 3 * nsta, nspec, None, 1.0 / nwin, shape, host)
+    assert np.array_equal(host, dev)
+
+
+def test_bad_arguments_raise(ctx, torch_cuda):
+    from fastxc_gb300 import FxcError
+    from fastxc_gb300.core import PairPlan
+
+    with pytest.raises(FxcError):
+        PairPlan(ctx, np.array([0], np.int32), np.array([9], np.int32), 6)
+    with pytest.raises(FxcError):
+        ctx_shape(1, 1, 0.1, 1.0)
