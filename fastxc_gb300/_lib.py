@@ -78,6 +78,7 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_xc_finalize": (_int, [_vp, _vp, _i64, _i64, C.POINTER(XcShape), _vp]),
     "fxc_xc_run": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
     "fxc_xc_run_host": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
+    "fxc_xc_run_noalloc": (_int, [_vp, _vp, _vp, _i64, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp]),
 }
 
 # Functions whose int return value is a count/flag, not a status.

@@ -36,6 +36,13 @@ struct FftPlan {
 int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out);
 // Cached device table perm[k] = fft_digit_pos(k) for the plan's radix order.
 int fft_perm_table(const FftPlan& p, const int** out);
+// Plan whose twiddle and digit-reversal tables are supplied by the caller
+// (no device allocation).
+int fft_make_plan_with(int n, const float2* tw, int tw_stride, const int* perm, FftPlan* out);
+// Host values of the twiddle table exp(-2*pi*i*k/len), k in [0,len), and of
+// the digit-reversal table of a plan, as the cached device tables hold them.
+void fft_twiddle_values(int len, float2* out);
+void fft_perm_values(const FftPlan& p, int* out);
 // Returns a cached device table of exp(-2*pi*i*k/len), k in [0,len), for the
 // current device. The table lives until process exit.
 int fft_twiddles(int len, const float2** out);

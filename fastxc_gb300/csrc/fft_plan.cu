@@ -62,6 +62,35 @@ int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out) {
   return FXC_OK;
 }
 
+int fft_make_plan_with(int n, const float2* tw, int tw_stride, const int* perm, FftPlan* out) {
+  std::vector<int> f;
+  if (!factorize(n, &f)) {
+    set_error("FFT length %d has a prime factor above 31 (not supported by the in-CTA FFT)", n);
+    return FXC_ERR_UNSUPPORTED;
+  }
+  FftPlan p{};
+  p.n = n;
+  p.nstages = (int)f.size();
+  for (int i = 0; i < p.nstages; ++i) p.radix[i] = f[i];
+  p.tw = tw;
+  p.tw_stride = tw_stride;
+  p.perm = perm;
+  *out = p;
+  return FXC_OK;
+}
+
+void fft_twiddle_values(int len, float2* out) {
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int k = 0; k < len; ++k) {
+    double a = two_pi * (double)k / (double)len;
+    out[k] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
+  }
+}
+
+void fft_perm_values(const FftPlan& p, int* out) {
+  for (int k = 0; k < p.n; ++k) out[k] = fft_digit_pos(p, k);
+}
+
 int fft_perm_table(const FftPlan& p, const int** out) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, int*> cache;

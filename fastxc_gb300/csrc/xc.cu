@@ -256,6 +256,35 @@ int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_
   return FXC_OK;
 }
 
+// Same launch as xc_finalize_launch, with the twiddle and digit-reversal
+// tables supplied by the caller instead of the per-device table cache.
+int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
+                              int64_t stack_pitch, const fxc_xc_shape* s, const float2* twn,
+                              const int* perm, float* ncf) {
+  if (npairs == 0) return FXC_OK;
+  const int N = s->nfft;
+  FXC_CHECK_ARG(N % 2 == 0 && N >= 2, "nfft %d must be even", N);
+  const int M = N / 2;
+  FXC_CHECK_ARG(M <= kFftLargeNmax, "nfft %d above the in-CTA FFT limit %d", N, 2 * kFftLargeNmax);
+  FXC_CHECK_ARG(npairs <= 0x7fffffff, "too many pairs for one launch");
+  FftPlan p;
+  FXC_TRY(fft_make_plan_with(M, twn, 2, perm, &p));
+  const float wdt = (float)N * s->dt;
+  const double inv_norm = 1.0 / (double)wdt;
+  const size_t smem = sizeof(float2) * (size_t)M;
+  if (M <= kFftSmallNmax) {
+    k_xc_finalize<kFftSmallT, kFftSmallNmax><<<(unsigned)npairs, kFftSmallT, smem, ctx->stream>>>(
+        stack, stack_pitch, p, twn, s->half_cc, s->cc_size, (float)inv_norm, inv_norm, ncf);
+  } else {
+    FXC_TRY(set_smem_limit(k_xc_finalize<kFftLargeT, kFftLargeNmax>, smem));
+    k_xc_finalize<kFftLargeT, kFftLargeNmax><<<(unsigned)npairs, kFftLargeT, smem, ctx->stream>>>(
+        stack, stack_pitch, p, twn, s->half_cc, s->cc_size, (float)inv_norm, inv_norm, ncf);
+  }
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
 int64_t xc_stack_pitch(int nspec) { return (int64_t)((nspec + 3) / 4) * 4; }
 
 }  // namespace fxc

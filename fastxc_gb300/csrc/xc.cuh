@@ -38,6 +38,13 @@ struct fxc_pairplan {
 
 namespace fxc {
 
+int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin,
+                    int nchan, int nspec, int64_t spec_pitch, const uint8_t* mask, float scale,
+                    float2* stack, int64_t stack_pitch, int method);
+int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
+                              int64_t stack_pitch, const fxc_xc_shape* s, const float2* twn,
+                              const int* perm, float* ncf);
+
 int xc_tensor_plan_init(fxc_ctx* ctx, fxc_pairplan* plan);
 void xc_tensor_plan_free(fxc_pairplan* plan);
 int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,

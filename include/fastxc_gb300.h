@@ -143,6 +143,27 @@ int fxc_xc_run_host(fxc_ctx *ctx, const fxc_pairplan *plan, const float *h_spec,
                     int32_t nchan, int64_t spec_pitch, const uint8_t *h_mask, float scale,
                     const fxc_xc_shape *shape, float *h_ncf, int method);
 
+/* Allocation-free variant of fxc_xc_run. No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc (a host framework that
+ * owns all device memory through its own pool, or a job whose device
+ * footprint is fixed at start-up). It allocates no device memory: its pair
+ * tiles, FFT tables and stacked spectra live in one file-scope 64 MiB device
+ * array that every GPU loading the library holds until exit. Takes the pair
+ * list on the host (h_src, h_rec as in fxc_pairplan_create) and the same
+ * device inputs/outputs as fxc_xc_run; FXC_XC_PLAIN method only.
+ * Limit: tiles + tables + npairs * round_up(nspec, 4) * 8 bytes must fit in
+ * 64 MiB (about 450 pairs at nspec 18523), else FXC_ERR_INVALID with the
+ * sizes in the message. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress), so make that first call before any
+ * stream capture. All calls share the array and it keeps the last call's
+ * contents (each call rewrites everything it reads, nothing needs
+ * clearing); calls whose work overlaps on the GPU race and must be
+ * serialised by the caller. */
+int fxc_xc_run_noalloc(fxc_ctx *ctx, const int32_t *h_src, const int32_t *h_rec, int64_t npairs,
+                       const float *d_spec, int64_t nwin, int32_t nchan, int64_t spec_pitch,
+                       const uint8_t *d_mask, float scale, const fxc_xc_shape *shape,
+                       float *d_ncf);
+
 #ifdef __cplusplus
 }
 #endif
