@@ -21,6 +21,7 @@ FXC_ERR_UNSUPPORTED = -3
 FXC_ERR_NOMEM = -4
 FXC_ERR_IO = -5
 FXC_ERR_NODEVICE = -6
+FXC_ERR_TIMEOUT = -7
 
 FXC_XC_PLAIN = 0
 FXC_XC_TENSOR = 1

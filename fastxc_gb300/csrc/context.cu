@@ -71,6 +71,18 @@ int ctx_enter(fxc_ctx* ctx) {
   return FXC_OK;
 }
 
+// Reads (and clears) the device error word after the stream is idle.
+int ctx_check_device_error(fxc_ctx* ctx) {
+  int h = 0;
+  FXC_CUDA_TRY(cudaMemcpy(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    FXC_CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(int)));
+    set_error("a kernel's bounded wait timed out (device error word %d); results of that launch are invalid", h);
+    return FXC_ERR_TIMEOUT;
+  }
+  return FXC_OK;
+}
+
 }  // namespace fxc
 
 using namespace fxc;
@@ -113,6 +125,15 @@ int fxc_ctx_create(int device, void* stream, fxc_ctx** out) {
   c->device = device;
   c->stream = (cudaStream_t)stream;
   c->num_sms = prop.multiProcessorCount;
+  cudaError_t e1 = cudaMalloc(&c->d_err, 256);
+  cudaError_t e2 = e1 == cudaSuccess ? cudaMemset(c->d_err, 0, 256) : e1;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    (void)cudaGetLastError();
+    if (c->d_err) cudaFree(c->d_err);
+    delete c;
+    set_error("allocation of the context error word failed: %s", cudaGetErrorString(e2));
+    return FXC_ERR_NOMEM;
+  }
   *out = c;
   return FXC_OK;
 }
@@ -123,6 +144,8 @@ int fxc_ctx_destroy(fxc_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   ctx->scratch.release();
   ctx->scratch2.release();
+  ctx->scratch3.release();
+  if (ctx->d_err) cudaFree(ctx->d_err);
   delete ctx;
   return FXC_OK;
 }
@@ -136,7 +159,7 @@ int fxc_ctx_set_stream(fxc_ctx* ctx, void* stream) {
 int fxc_ctx_synchronize(fxc_ctx* ctx) {
   FXC_TRY(ctx_enter(ctx));
   FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return FXC_OK;
+  return ctx_check_device_error(ctx);
 }
 
 }  // extern "C"

@@ -15,6 +15,7 @@ struct Scratch {
 
 void count_launch(int n = 1);
 int ctx_enter(fxc_ctx* ctx);
+int ctx_check_device_error(fxc_ctx* ctx);
 
 }  // namespace fxc
 
@@ -24,4 +25,6 @@ struct fxc_ctx {
   int num_sms = 148;
   fxc::Scratch scratch;   // per-pair stacked spectra between stack and finalize
   fxc::Scratch scratch2;  // host-call staging (device copies of host inputs)
+  fxc::Scratch scratch3;  // packed bf16 hi/lo operands of the tensor-core path
+  int* d_err = nullptr;   // device error word: set by kernels whose bounded waits time out
 };

@@ -242,8 +242,33 @@ __device__ __forceinline__ void dft_any(float2 (&x)[R]) {
 // so DIT(DIF(x)) with one of them inverse returns n*x. The point that holds
 // frequency k after a DIF is fft_digit_pos(k) (table fft_perm).
 
+// Stage twiddles w^k (k < n*tw_stride) come from a two-level table in shared
+// memory: w^k = coarse[k >> 8] * fine[k & 255], both entries of the global
+// table copied by fft_twiddles_to_smem (about 3 KB for the longest rows).
+constexpr int kTwFineShift = 8;
+constexpr int kTwFine = 1 << kTwFineShift;
+
+__host__ __device__ inline int fft_tw_smem_elems(const FftPlan& p) {
+  const int nt = p.n * p.tw_stride;
+  return kTwFine + (nt - 1) / kTwFine + 1;
+}
+
+// All T threads copy; the caller synchronises before the first stage.
+template <int T>
+__device__ __forceinline__ void fft_twiddles_to_smem(const FftPlan& p, float2* stw) {
+  const int nt = p.n * p.tw_stride;
+  for (int i = threadIdx.x; i < kTwFine; i += T)
+    stw[i] = i < nt ? __ldg(p.tw + i) : make_float2(1.f, 0.f);
+  const int nc = (nt - 1) / kTwFine + 1;
+  for (int h = threadIdx.x; h < nc; h += T) stw[kTwFine + h] = __ldg(p.tw + h * kTwFine);
+}
+
+__device__ __forceinline__ float2 tw_lookup(const float2* stw, int k) {
+  return cmul(stw[kTwFine + (k >> kTwFineShift)], stw[k & (kTwFine - 1)]);
+}
+
 template <int R, int T, bool DIT>
-__device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float2* __restrict__ tw,
+__device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float2* stw,
                                           int tw_step, bool conj_in, bool conj_out) {
   const int nb = n / R;
   const int B = L * R;
@@ -259,12 +284,12 @@ __device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float
     }
     if (DIT && j != 0) {
 #pragma unroll
-      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], __ldg(tw + t * j * tw_step));
+      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], tw_lookup(stw, t * j * tw_step));
     }
     dft_any<R>(x);
     if (!DIT && j != 0) {
 #pragma unroll
-      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], __ldg(tw + t * j * tw_step));
+      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], tw_lookup(stw, t * j * tw_step));
     }
 #pragma unroll
     for (int t = 0; t < R; ++t) buf[base + t * L] = conj_out ? conjf2(x[t]) : x[t];
@@ -273,31 +298,31 @@ __device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float
 }
 
 template <int T, bool DIT>
-__device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, int R, int L,
-                                              int tw_step, bool ci, bool co) {
+__device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, const float2* stw,
+                                              int R, int L, int tw_step, bool ci, bool co) {
   switch (R) {
-    case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 8: fft_stage_ip<8, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 3: fft_stage_ip<3, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 5: fft_stage_ip<5, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 7: fft_stage_ip<7, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 11: fft_stage_ip<11, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 13: fft_stage_ip<13, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 17: fft_stage_ip<17, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 19: fft_stage_ip<19, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 23: fft_stage_ip<23, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 29: fft_stage_ip<29, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
-    case 31: fft_stage_ip<31, T, DIT>(buf, p.n, L, p.tw, tw_step, ci, co); break;
+    case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 8: fft_stage_ip<8, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 3: fft_stage_ip<3, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 5: fft_stage_ip<5, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 7: fft_stage_ip<7, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 11: fft_stage_ip<11, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 13: fft_stage_ip<13, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 17: fft_stage_ip<17, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 19: fft_stage_ip<19, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 23: fft_stage_ip<23, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 29: fft_stage_ip<29, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 31: fft_stage_ip<31, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
     default: break;  // rejected by fft_make_plan
   }
 }
 
 // Natural-order input, digit-reversed output. All T threads must call it
-// after buf is written and the CTA synchronised; the result is visible to
-// the CTA on return.
+// after buf and the twiddle table stw (fft_twiddles_to_smem) are written and
+// the CTA synchronised; the result is visible to the CTA on return.
 template <int T>
-__device__ void fft_dif(float2* buf, const FftPlan& p, bool inverse) {
+__device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = p.n;
   int Rprod = 1;  // r_0 ... r_{s-1}
   for (int s = 0; s < p.nstages; ++s) {
@@ -305,7 +330,7 @@ __device__ void fft_dif(float2* buf, const FftPlan& p, bool inverse) {
     L /= R;
     // block length B = L*R = n / Rprod; twiddle w_B^{tj} = w_n^{t j Rprod}
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, false>(buf, p, R, L, tw_step, inverse && s == 0,
+    fft_run_stage<T, false>(buf, p, stw, R, L, tw_step, inverse && s == 0,
                             inverse && s == p.nstages - 1);
     Rprod *= R;
   }
@@ -313,14 +338,14 @@ __device__ void fft_dif(float2* buf, const FftPlan& p, bool inverse) {
 
 // Digit-reversed input (the layout fft_dif produces), natural-order output.
 template <int T>
-__device__ void fft_dit(float2* buf, const FftPlan& p, bool inverse) {
+__device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = 1;
   int Rprod = p.n;
   for (int s = p.nstages - 1; s >= 0; --s) {
     const int R = p.radix[s];
     Rprod /= R;
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, true>(buf, p, R, L, tw_step, inverse && s == p.nstages - 1,
+    fft_run_stage<T, true>(buf, p, stw, R, L, tw_step, inverse && s == p.nstages - 1,
                            inverse && s == 0);
     L *= R;
   }

@@ -13,10 +13,12 @@ __global__ void __launch_bounds__(T, 1)
               int64_t out_pitch, int inverse) {
   extern __shared__ float2 buf[];
   const int n = p.n;
+  float2* stw = buf + n;
+  fft_twiddles_to_smem<T>(p, stw);
   const float2* x = in + (int64_t)blockIdx.x * in_pitch;
   for (int i = threadIdx.x; i < n; i += T) buf[i] = x[i];
   __syncthreads();
-  fft_dif<T>(buf, p, inverse != 0);
+  fft_dif<T>(buf, p, stw, inverse != 0);
   float2* y = out + (int64_t)blockIdx.x * out_pitch;
   for (int i = threadIdx.x; i < n; i += T) y[i] = buf[__ldg(p.perm + i)];
 }
@@ -28,10 +30,12 @@ __global__ void __launch_bounds__(T, 1)
                    const float2* __restrict__ twn, int64_t in_pitch, int64_t out_pitch) {
   extern __shared__ float2 buf[];
   const int M = p.n;
+  float2* stw = buf + M;
+  fft_twiddles_to_smem<T>(p, stw);
   const float* x = in + (int64_t)blockIdx.x * in_pitch;
   for (int m = threadIdx.x; m < M; m += T) buf[m] = make_float2(x[2 * m], x[2 * m + 1]);
   __syncthreads();
-  fft_dif<T>(buf, p, false);
+  fft_dif<T>(buf, p, stw, false);
   float2* y = out + (int64_t)blockIdx.x * out_pitch;
   for (int k = threadIdx.x; k <= M; k += T) y[k] = r2c_post(buf, p.perm, M, k, twn);
 }
@@ -43,10 +47,12 @@ __global__ void __launch_bounds__(T, 1)
                   int64_t in_pitch, int64_t out_pitch) {
   extern __shared__ float2 buf[];
   const int n = p.n;
+  float2* stw = buf + n;
+  fft_twiddles_to_smem<T>(p, stw);
   const float* x = in + (int64_t)blockIdx.x * in_pitch;
   for (int i = threadIdx.x; i < n; i += T) buf[i] = make_float2(x[i], 0.f);
   __syncthreads();
-  fft_dif<T>(buf, p, false);
+  fft_dif<T>(buf, p, stw, false);
   float2* y = out + (int64_t)blockIdx.x * out_pitch;
   for (int k = threadIdx.x; k <= n / 2; k += T) y[k] = buf[__ldg(p.perm + k)];
 }
@@ -58,10 +64,12 @@ __global__ void __launch_bounds__(T, 1)
                    const float2* __restrict__ twn, int64_t in_pitch, int64_t out_pitch) {
   extern __shared__ float2 buf[];
   const int M = p.n;
+  float2* stw = buf + M;
+  fft_twiddles_to_smem<T>(p, stw);
   const float2* X = in + (int64_t)blockIdx.x * in_pitch;
   for (int k = threadIdx.x; k < M; k += T) buf[k] = c2r_pre(X, M, k, twn);
   __syncthreads();
-  fft_dif<T>(buf, p, true);
+  fft_dif<T>(buf, p, stw, true);
   float* y = out + (int64_t)blockIdx.x * out_pitch;
   for (int m = threadIdx.x; m < M; m += T) {
     float2 v = buf[__ldg(p.perm + m)];
@@ -103,7 +111,7 @@ int fxc_fft_c2c(fxc_ctx* ctx, const float* d_in, float* d_out, int n, int batch,
   FXC_TRY(fft_twiddles(n, &tw));
   FftPlan p;
   FXC_TRY(fft_make_plan(n, tw, 1, &p));
-  const size_t smem = sizeof(float2) * (size_t)n;
+  const size_t smem = sizeof(float2) * ((size_t)n + fft_tw_smem_elems(p));
   const float2* in = reinterpret_cast<const float2*>(d_in);
   float2* out = reinterpret_cast<float2*>(d_out);
   if (n <= kFftSmallNmax) {
@@ -133,7 +141,7 @@ int fxc_fft_r2c(fxc_ctx* ctx, const float* d_in, float* d_out, int n, int batch,
     FXC_CHECK_ARG(M <= kFftLargeNmax, "r2c length %d above the in-CTA limit", n);
     FftPlan p;
     FXC_TRY(fft_make_plan(M, twn, 2, &p));
-    const size_t smem = sizeof(float2) * (size_t)M;
+    const size_t smem = sizeof(float2) * ((size_t)M + fft_tw_smem_elems(p));
     if (M <= kFftSmallNmax) {
       k_fft_r2c_even<kFftSmallT, kFftSmallNmax><<<batch, kFftSmallT, smem, ctx->stream>>>(
           d_in, out, p, twn, in_pitch, out_pitch);
@@ -146,7 +154,7 @@ int fxc_fft_r2c(fxc_ctx* ctx, const float* d_in, float* d_out, int n, int batch,
     FXC_CHECK_ARG(n <= kFftLargeNmax, "r2c odd length %d above the in-CTA limit", n);
     FftPlan p;
     FXC_TRY(fft_make_plan(n, twn, 1, &p));
-    const size_t smem = sizeof(float2) * (size_t)n;
+    const size_t smem = sizeof(float2) * ((size_t)n + fft_tw_smem_elems(p));
     if (n <= kFftSmallNmax) {
       k_fft_r2c_odd<kFftSmallT, kFftSmallNmax><<<batch, kFftSmallT, smem, ctx->stream>>>(
           d_in, out, p, in_pitch, out_pitch);
@@ -174,7 +182,7 @@ int fxc_fft_c2r(fxc_ctx* ctx, const float* d_in, float* d_out, int n, int batch,
   FXC_TRY(fft_twiddles(n, &twn));
   FftPlan p;
   FXC_TRY(fft_make_plan(M, twn, 2, &p));
-  const size_t smem = sizeof(float2) * (size_t)M;
+  const size_t smem = sizeof(float2) * ((size_t)M + fft_tw_smem_elems(p));
   const float2* in = reinterpret_cast<const float2*>(d_in);
   if (M <= kFftSmallNmax) {
     k_fft_c2r_even<kFftSmallT, kFftSmallNmax><<<batch, kFftSmallT, smem, ctx->stream>>>(

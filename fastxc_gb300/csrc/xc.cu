@@ -99,34 +99,115 @@ int pairplan_build(const int32_t* src, const int32_t* rec, int64_t npairs, int32
 // ---------------------------------------------------------------------------
 // Plain FP32 stack kernel
 // ---------------------------------------------------------------------------
-// CTA = one 16x16 channel tile x kXcFreqChunk consecutive bins.
-// Thread (f = tid % 64, quadrant q = tid / 64): 8 src x 8 rec pairs for bin f.
+// CTA = one 16x16 channel tile x kXcFreqChunk (64) consecutive bins.
+// Windows stream through a ring of kXcSlots shared-memory window slots filled
+// with cp.async (8-byte copies: any spectrum pitch works; invalid channels
+// and bins past nspec are zero-filled by the copy itself). A slot is 32 rows
+// (16 src channels, then 16 rec channels) x 64 bins of float2 (16 KB).
+// Windows move in pairs: one barrier per pair, two pairs in flight.
+// Thread (col = tid % 64, quadrant q = tid / 64) accumulates 8 src x 8 rec
+// pairs of bin f0+col in registers: 512 FFMA per 32 shared loads per pair.
+// Window masks (when given) are staged as 32 bytes per slot, loaded one
+// iteration before they are stored so the load latency is hidden.
 
-__device__ __forceinline__ void xc_load8(float2 (&v)[8], const float2* __restrict__ spec,
-                                         int64_t row0, int64_t pitch, int f, int ch0, int nchan,
-                                         const uint8_t* __restrict__ mrow, bool fok) {
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int ch = ch0 + i;
-    bool ok = fok && ch < nchan;
-    if (mrow != nullptr && ok) ok = mrow[ch] != 0;
-    v[i] = ok ? __ldg(spec + (row0 + ch) * pitch + f) : make_float2(0.f, 0.f);
-  }
+constexpr int kXcSlots = 6;                                 // window slots (3 pairs)
+constexpr int kXcSlotElems = 2 * kXcTile * kXcFreqChunk;    // 2048 float2 = 16 KB
+
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+__device__ __forceinline__ void xc_cmac8x8(float (&re)[8][8], float (&im)[8][8],
+                                           const float2 (&a)[8], const float2 (&b)[8]) {
+  // conj(a) * b = (ar*br + ai*bi) + i (ar*bi - ai*br)
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      re[i][j] = fmaf(a[i].x, b[j].x, re[i][j]);
+      re[i][j] = fmaf(a[i].y, b[j].y, re[i][j]);
+      im[i][j] = fmaf(a[i].x, b[j].y, im[i][j]);
+      im[i][j] = fmaf(-a[i].y, b[j].x, im[i][j]);
+    }
+}
+
+template <bool MASK>
 __global__ void __launch_bounds__(256, 1)
     k_xc_stack_plain(const float2* __restrict__ spec, int64_t nwin, int nchan, int nspec,
                      int64_t spec_pitch, const uint8_t* __restrict__ mask,
                      const XcTile* __restrict__ tiles, const int32_t* __restrict__ maps,
                      float scale, float2* __restrict__ stack, int64_t stack_pitch) {
-  const XcTile tile = tiles[blockIdx.x];
-  const int f = blockIdx.y * kXcFreqChunk + (threadIdx.x % kXcFreqChunk);
-  const int q = threadIdx.x / kXcFreqChunk;
-  const int qa = q & 1, qb = q >> 1;
-  const int a0 = tile.a_base + qa * 8;
-  const int b0 = tile.b_base + qb * 8;
-  const bool fok = f < nspec;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* sm = reinterpret_cast<float2*>(smraw);
+  uint8_t* smask = smraw + sizeof(float2) * kXcSlots * kXcSlotElems;
 
+  const XcTile tile = tiles[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int col = tid & (kXcFreqChunk - 1);
+  const int f0 = blockIdx.y * kXcFreqChunk;
+  const bool colok = f0 + col < nspec;
+
+  // copy rows of this thread: r = (tid >> 6) + 4k, k < 8
+  const int r0 = tid >> 6;
+  int chs[8];
+  unsigned okbits = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int r = r0 + 4 * k;
+    const int ch = (r < kXcTile) ? tile.a_base + r : tile.b_base + (r - kXcTile);
+    chs[k] = ch;
+    if (colok && ch < nchan) okbits |= 1u << k;
+  }
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm) + (uint32_t)(col * sizeof(float2));
+
+  // Copy window w (zero-filled when w >= nwin) into its slot.
+  auto issue = [&](int64_t w) {
+    const int slot = (int)(w % kXcSlots);
+    const uint32_t dst = sbase + (uint32_t)(slot * kXcSlotElems * sizeof(float2));
+    const int64_t wrow = w * nchan;
+    const bool wok = w < nwin;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int r = r0 + 4 * k;
+      const bool ok = wok && ((okbits >> k) & 1u);
+      const float2* src = ok ? spec + (wrow + chs[k]) * spec_pitch + f0 + col : spec;
+      cp_async8(dst + (uint32_t)(r * kXcFreqChunk * sizeof(float2)), src, ok ? 8 : 0);
+    }
+  };
+
+  // mask bytes: thread tid < 32 owns row tid of every slot
+  const int mrow_ch = (tid < kXcTile) ? tile.a_base + tid : tile.b_base + (tid - kXcTile);
+  const bool mown = MASK && tid < 2 * kXcTile;
+  auto mask_at = [&](int64_t w) -> uint8_t {
+    return (w < nwin && mrow_ch < nchan) ? __ldg(mask + w * nchan + mrow_ch) : (uint8_t)0;
+  };
+
+  const int64_t npair = (nwin + 1) / 2;
+  // prologue: window pairs 0 and 1
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    issue(2 * p);
+    issue(2 * p + 1);
+    cp_async_commit();
+  }
+  uint8_t mp0 = 0, mp1 = 0;
+  if (mown) {
+    for (int w = 0; w < 4; ++w) smask[w * 2 * kXcTile + tid] = mask_at(w);
+    mp0 = mask_at(4);
+    mp1 = mask_at(5);
+  }
+
+  const int q = tid >> 6;
+  const int qa = q & 1, qb = q >> 1;
   float acc_re[8][8], acc_im[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
@@ -136,36 +217,49 @@ __global__ void __launch_bounds__(256, 1)
       acc_im[i][j] = 0.f;
     }
 
-  float2 ya[8], yb[8], na[8], nb[8];
-  if (nwin > 0) {
-    const uint8_t* m0 = mask ? mask : nullptr;
-    xc_load8(ya, spec, 0, spec_pitch, f, a0, nchan, m0, fok);
-    xc_load8(yb, spec, 0, spec_pitch, f, b0, nchan, m0, fok);
-  }
-  for (int64_t w = 0; w < nwin; ++w) {
-    if (w + 1 < nwin) {
-      const int64_t row = (w + 1) * nchan;
-      const uint8_t* mr = mask ? mask + row : nullptr;
-      xc_load8(na, spec, row, spec_pitch, f, a0, nchan, mr, fok);
-      xc_load8(nb, spec, row, spec_pitch, f, b0, nchan, mr, fok);
+  for (int64_t p = 0; p < npair; ++p) {
+    const int64_t w = 2 * p;
+    cp_async_wait<1>();  // pair p has landed (pair p+1 may be in flight)
+    __syncthreads();     // ... for every thread; pair p-1's slots are free
+    issue(w + 4);
+    issue(w + 5);
+    cp_async_commit();
+    if (mown) {
+      smask[(int)((w + 4) % kXcSlots) * 2 * kXcTile + tid] = mp0;
+      smask[(int)((w + 5) % kXcSlots) * 2 * kXcTile + tid] = mp1;
+      mp0 = mask_at(w + 6);
+      mp1 = mask_at(w + 7);
     }
-    // conj(a) * b = (ar*br + ai*bi) + i (ar*bi - ai*br)
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        acc_re[i][j] = fmaf(ya[i].x, yb[j].x, acc_re[i][j]);
-        acc_re[i][j] = fmaf(ya[i].y, yb[j].y, acc_re[i][j]);
-        acc_im[i][j] = fmaf(ya[i].x, yb[j].y, acc_im[i][j]);
-        acc_im[i][j] = fmaf(-ya[i].y, yb[j].x, acc_im[i][j]);
-      }
+    const int s0 = (int)(w % kXcSlots);
+    const int s1 = (int)((w + 1) % kXcSlots);
+    const float2* st0 = sm + s0 * kXcSlotElems + col;
+    const float2* st1 = sm + s1 * kXcSlotElems + col;
+    float2 ya0[8], yb0[8], ya1[8], yb1[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      ya[i] = na[i];
-      yb[i] = nb[i];
+      ya0[i] = st0[(qa * 8 + i) * kXcFreqChunk];
+      yb0[i] = st0[(kXcTile + qb * 8 + i) * kXcFreqChunk];
+      ya1[i] = st1[(qa * 8 + i) * kXcFreqChunk];
+      yb1[i] = st1[(kXcTile + qb * 8 + i) * kXcFreqChunk];
     }
+    if (MASK) {
+      const uint8_t* mk0 = smask + s0 * 2 * kXcTile;
+      const uint8_t* mk1 = smask + s1 * 2 * kXcTile;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (mk0[qa * 8 + i] == 0) ya0[i] = make_float2(0.f, 0.f);
+        if (mk0[kXcTile + qb * 8 + i] == 0) yb0[i] = make_float2(0.f, 0.f);
+        if (mk1[qa * 8 + i] == 0) ya1[i] = make_float2(0.f, 0.f);
+        if (mk1[kXcTile + qb * 8 + i] == 0) yb1[i] = make_float2(0.f, 0.f);
+      }
+    }
+    xc_cmac8x8(acc_re, acc_im, ya0, yb0);
+    xc_cmac8x8(acc_re, acc_im, ya1, yb1);
   }
-  if (!fok) return;
+  cp_async_wait<0>();
+
+  if (!colok) return;
+  const int f = f0 + col;
   const int32_t* map = maps + tile.map_offset;
 #pragma unroll
   for (int i = 0; i < 8; ++i)
@@ -192,10 +286,12 @@ __global__ void __launch_bounds__(T, 1)
   extern __shared__ float2 buf[];
   const int M = p.n;
   const int N = 2 * M;
+  float2* stw = buf + M;
+  fft_twiddles_to_smem<T>(p, stw);
   const float2* X = stack + (int64_t)blockIdx.x * stack_pitch;
   for (int k = threadIdx.x; k < M; k += T) buf[k] = c2r_pre(X, M, k, twn);
   __syncthreads();
-  fft_dif<T>(buf, p, true);
+  fft_dif<T>(buf, p, stw, true);
   float* out = ncf + (int64_t)blockIdx.x * cc_size;
   for (int j = threadIdx.x; j < cc_size; j += T) {
     int m = N - half_cc + j;
@@ -219,9 +315,18 @@ int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, 
   const int64_t nchunks = ceil_div(nspec, kXcFreqChunk);
   FXC_CHECK_ARG(nchunks <= 65535, "nspec %d too large for the grid", nspec);
   dim3 grid((unsigned)plan->ntiles, (unsigned)nchunks);
-  k_xc_stack_plain<<<grid, 256, 0, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch, mask,
-                                                  plan->d_tiles, plan->d_maps, scale, stack,
-                                                  stack_pitch);
+  const size_t smem = sizeof(float2) * kXcSlots * kXcSlotElems + kXcSlots * 2 * kXcTile;
+  if (mask) {
+    FXC_TRY(set_smem_limit(k_xc_stack_plain<true>, smem));
+    k_xc_stack_plain<true><<<grid, 256, smem, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch,
+                                                             mask, plan->d_tiles, plan->d_maps,
+                                                             scale, stack, stack_pitch);
+  } else {
+    FXC_TRY(set_smem_limit(k_xc_stack_plain<false>, smem));
+    k_xc_stack_plain<false><<<grid, 256, smem, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch,
+                                                              mask, plan->d_tiles, plan->d_maps,
+                                                              scale, stack, stack_pitch);
+  }
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;
@@ -242,7 +347,7 @@ int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_
   // 1/(width*dt) with width*dt in float, as InvNormalize2DKernel computes it
   const float wdt = (float)N * s->dt;
   const double inv_norm = 1.0 / (double)wdt;
-  const size_t smem = sizeof(float2) * (size_t)M;
+  const size_t smem = sizeof(float2) * ((size_t)M + fft_tw_smem_elems(p));
   if (M <= kFftSmallNmax) {
     k_xc_finalize<kFftSmallT, kFftSmallNmax><<<(unsigned)npairs, kFftSmallT, smem, ctx->stream>>>(
         stack, stack_pitch, p, twn, s->half_cc, s->cc_size, (float)inv_norm, inv_norm, ncf);
@@ -271,7 +376,7 @@ int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
   FXC_TRY(fft_make_plan_with(M, twn, 2, perm, &p));
   const float wdt = (float)N * s->dt;
   const double inv_norm = 1.0 / (double)wdt;
-  const size_t smem = sizeof(float2) * (size_t)M;
+  const size_t smem = sizeof(float2) * ((size_t)M + fft_tw_smem_elems(p));
   if (M <= kFftSmallNmax) {
     k_xc_finalize<kFftSmallT, kFftSmallNmax><<<(unsigned)npairs, kFftSmallT, smem, ctx->stream>>>(
         stack, stack_pitch, p, twn, s->half_cc, s->cc_size, (float)inv_norm, inv_norm, ncf);
@@ -444,7 +549,7 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
                      d_mask, scale, shape, d_ncf, method));
   FXC_CUDA_TRY(cudaMemcpyAsync(h_ncf, d_ncf, ncf_bytes, cudaMemcpyDeviceToHost, ctx->stream));
   FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return FXC_OK;
+  return ctx_check_device_error(ctx);
 }
 
 }  // extern "C"

@@ -1,27 +1,576 @@
-// BF16 hi/lo split tensor-core contraction S(f) = Y(f)^H Y(f) (placeholder
-// until the tcgen05 kernel lands: reports FXC_ERR_UNSUPPORTED).
+// BF16 hi/lo split tensor-core contraction S(f) = Y(f)^H Y(f) on tcgen05.
+//
+// Same result as the plain stack kernel (and as accumulateStepXc2DKernel,
+// native/xc/kernels/cuda.kernels.cu:16-36, summed over the windows):
+//   stack[p, f] = scale * sum_w conj(Y[w, src_p, f]) * Y[w, rec_p, f]
+// computed for all pairs of a 128 x N channel tile at once, per frequency,
+// as real GEMMs over the window axis:
+//   Re S = Yr_a . Yr_b + Yi_a . Yi_b        Im S = Yr_a . Yi_b - Yi_a . Yr_b
+// Every real operand x is split into bf16 hi = rn(x), lo = rn(x - hi) and
+// each product is hi.hi + hi.lo + lo.hi accumulated in FP32 in TMEM (the
+// dropped lo.lo term is ~2^-16 relative).
+//
+// Pipeline:
+//   1. k_xc_pack: complex64 [w][c][f] -> per frequency four bf16 planes
+//      (re-hi, re-lo, im-hi, im-lo), each stored exactly as the UMMA
+//      K-major, no-swizzle core-matrix image: for every K-block of 32
+//      windows, 4 chunks of 8 windows, each chunk [C_pad rows][8 bf16]
+//      (16 bytes per row). A row range of a chunk is one contiguous run, so
+//      the GEMM moves its tiles with plain cp.async.bulk copies.
+//   2. k_xc_tc_gemm: one CTA per (channel tile, frequency).
+//        warp 0      producer: bulk copies of the A (128 src rows) and B (N
+//                    rec rows) tiles of each K-block into a 2-stage ring,
+//                    completion counted on mbarriers (expect_tx bytes);
+//        warp 1      allocates 512 TMEM columns; lane 0 issues the 12
+//                    tcgen05.mma (M=128, N, K=16) per K step into two FP32
+//                    accumulators (Re at column 0, Im at column 256) and
+//                    frees each stage with tcgen05.commit;
+//        warps 2..5  epilogue: tcgen05.ld of the accumulators, scale,
+//                    conjugate reversed pairs, scatter to the pair rows.
+//      Only the upper triangle of channel tiles is computed (a pair is
+//      computed in the orientation (min, max) and conjugated if reversed).
+//      Every mbarrier wait is bounded by %globaltimer (2 s); a timeout sets
+//      the context's device error word, the CTA drains its copies and frees
+//      TMEM before it exits.
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "context.cuh"
 #include "xc.cuh"
 
 namespace fxc {
 
-struct XcTensorPlan {
-  int unused;
+constexpr int kTcKb = 32;             // windows per K-block
+constexpr int kTcKc = kTcKb / 8;      // 16-byte core-matrix chunks per K-block row
+constexpr int kTcM = 128;             // MMA M (src channel rows per tile)
+constexpr int kTcNmax = 256;          // MMA N limit (rec channel rows per tile)
+constexpr int kTcStages = 2;
+constexpr int kTcThreads = 192;       // 6 warps
+constexpr int kTcPlanes = 4;          // re-hi, re-lo, im-hi, im-lo
+constexpr uint32_t kTcAccImCol = 256; // TMEM column of the Im accumulator
+constexpr int kTcABytes = kTcPlanes * kTcM * kTcKb * 2;     // 32 KB per stage
+constexpr int kTcBBytesMax = kTcPlanes * kTcNmax * kTcKb * 2;  // 64 KB per stage
+constexpr int kTcStageBytes = kTcABytes + kTcBBytesMax;
+constexpr size_t kTcSmemBytes = (size_t)kTcStages * kTcStageBytes + 256;
+
+struct TcTile {
+  int32_t a0, am;  // first src row, valid src rows (<= 128)
+  int32_t b0, bn;  // first rec row, valid rec rows (<= n)
+  int32_t n;       // MMA N: bn rounded up to 16
+  int32_t map_offset;
 };
+
+struct XcTensorPlan {
+  int32_t nchan = 0;
+  int32_t cpad = 0;
+  int64_t ntiles = 0;
+  TcTile* d_tiles = nullptr;
+  int32_t* d_maps = nullptr;  // per tile [128][n]: p, -(p+2) for a reversed pair, -1 none
+};
+
+static int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 int xc_tensor_plan_init(fxc_ctx*, fxc_pairplan* plan) {
   plan->tensor = nullptr;
+  const int32_t C = plan->nchan;
+  XcTensorPlan* tp = new (std::nothrow) XcTensorPlan();
+  if (!tp) {
+    set_error("host allocation failed");
+    return FXC_ERR_NOMEM;
+  }
+  tp->nchan = C;
+  tp->cpad = (int32_t)round_up(C, 8);
+  // Tiles over the upper triangle: src block [a0, a0+128), rec range
+  // [a0, C) in chunks of <= 256. Duplicated pairs go to extra layers.
+  struct Geo {
+    int32_t a0, am, b0, bn;
+  };
+  std::vector<Geo> geos;
+  for (int32_t a0 = 0; a0 < C; a0 += kTcM) {
+    const int32_t am = std::min(kTcM, C - a0);
+    for (int32_t b0 = a0; b0 < C; b0 += kTcNmax) geos.push_back({a0, am, b0, std::min(kTcNmax, C - b0)});
+  }
+  auto geo_of = [&](int32_t lo, int32_t hi) -> int {
+    const int32_t ablk = lo / kTcM;
+    int idx = 0;
+    for (int32_t a0 = 0; a0 < ablk * kTcM; a0 += kTcM) idx += (int)((C - a0 + kTcNmax - 1) / kTcNmax);
+    return idx + (int)((hi - ablk * kTcM) / kTcNmax);
+  };
+  std::vector<TcTile> tiles;
+  std::vector<int32_t> maps;
+  std::vector<std::map<int, int>> layers(1);  // geo -> tile index
+  for (int64_t p = 0; p < plan->npairs; ++p) {
+    const int32_t s = plan->h_src[p], r = plan->h_rec[p];
+    const int32_t lo = std::min(s, r), hi = std::max(s, r);
+    const int g = geo_of(lo, hi);
+    const Geo& G = geos[g];
+    for (size_t layer = 0;; ++layer) {
+      if (layer == layers.size()) layers.emplace_back();
+      auto it = layers[layer].find(g);
+      int t;
+      if (it == layers[layer].end()) {
+        t = (int)tiles.size();
+        layers[layer][g] = t;
+        TcTile tt;
+        tt.a0 = G.a0;
+        tt.am = G.am;
+        tt.b0 = G.b0;
+        tt.bn = G.bn;
+        tt.n = (int32_t)round_up(G.bn, 16);
+        tt.map_offset = (int32_t)maps.size();
+        tiles.push_back(tt);
+        maps.insert(maps.end(), (size_t)kTcM * tt.n, -1);
+      } else {
+        t = it->second;
+      }
+      int32_t& cell = maps[(size_t)tiles[t].map_offset + (size_t)(lo - G.a0) * tiles[t].n + (hi - G.b0)];
+      if (cell == -1) {
+        cell = (s <= r) ? (int32_t)p : (int32_t)(-(p + 2));
+        break;
+      }
+    }
+  }
+  tp->ntiles = (int64_t)tiles.size();
+  if (!tiles.empty()) {
+    cudaError_t e1 = cudaMalloc(&tp->d_tiles, sizeof(TcTile) * tiles.size());
+    cudaError_t e2 = cudaMalloc(&tp->d_maps, sizeof(int32_t) * maps.size());
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      (void)cudaGetLastError();
+      if (tp->d_tiles) cudaFree(tp->d_tiles);
+      if (tp->d_maps) cudaFree(tp->d_maps);
+      delete tp;
+      set_error("cudaMalloc of tensor tile plan failed");
+      return FXC_ERR_NOMEM;
+    }
+    cudaMemcpy(tp->d_tiles, tiles.data(), sizeof(TcTile) * tiles.size(), cudaMemcpyHostToDevice);
+    cudaError_t e3 =
+        cudaMemcpy(tp->d_maps, maps.data(), sizeof(int32_t) * maps.size(), cudaMemcpyHostToDevice);
+    if (e3 != cudaSuccess) {
+      cudaFree(tp->d_tiles);
+      cudaFree(tp->d_maps);
+      delete tp;
+      set_error("upload of tensor tile plan failed: %s", cudaGetErrorString(e3));
+      return FXC_ERR_CUDA;
+    }
+  }
+  plan->tensor = tp;
   return FXC_OK;
 }
 
 void xc_tensor_plan_free(fxc_pairplan* plan) {
+  if (!plan->tensor) return;
+  if (plan->tensor->d_tiles) cudaFree(plan->tensor->d_tiles);
+  if (plan->tensor->d_maps) cudaFree(plan->tensor->d_maps);
   delete plan->tensor;
   plan->tensor = nullptr;
 }
 
-int xc_stack_tensor_launch(fxc_ctx*, const fxc_pairplan*, const float2*, int64_t, int, int,
-                           int64_t, const uint8_t*, float, float2*, int64_t) {
-  set_error("tensor-core contraction not built yet");
-  return FXC_ERR_UNSUPPORTED;
+// ---------------------------------------------------------------------------
+// Pack kernel
+// ---------------------------------------------------------------------------
+// CTA: 8 frequencies x 16 channels x one K-block of 32 windows.
+// Load [32 w][16 c][8 f] complex through shared memory, then every thread
+// writes 16-byte chunks (8 windows of one plane, one row): consecutive
+// threads write consecutive rows (256 contiguous bytes per 16 threads).
+
+constexpr int kPackF = 8;
+constexpr int kPackC = 16;
+
+__device__ __forceinline__ uint16_t bf16_bits_rn(float x) {
+  // round-to-nearest-even float -> bf16 (inputs are finite: the spectra are
+  // sanitised by the producing stage)
+  uint32_t u = __float_as_uint(x);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+__device__ __forceinline__ float bf16_bits_to_float(uint16_t b) {
+  return __uint_as_float((uint32_t)b << 16);
+}
+
+__global__ void __launch_bounds__(256)
+    k_xc_pack(const float2* __restrict__ spec, int64_t nwin, int nchan, int nspec,
+              int64_t spec_pitch, const uint8_t* __restrict__ mask, int nkb, int cpad,
+              uint4* __restrict__ packed) {
+  __shared__ float2 sm[kTcKb][kPackC][kPackF + 1];
+  const int f0 = blockIdx.x * kPackF;
+  const int c0 = blockIdx.y * kPackC;
+  const int kb = blockIdx.z;
+  const int tid = threadIdx.x;
+  // load: 32 w x 32 c rows of 8 complex; thread -> (row, f) with f fastest
+  for (int e = tid; e < kTcKb * kPackC * kPackF; e += 256) {
+    const int f = e % kPackF;
+    const int c = (e / kPackF) % kPackC;
+    const int wl = e / (kPackF * kPackC);
+    const int64_t w = (int64_t)kb * kTcKb + wl;
+    const int ch = c0 + c;
+    float2 v = make_float2(0.f, 0.f);
+    if (w < nwin && ch < nchan && f0 + f < nspec) {
+      bool ok = true;
+      if (mask) ok = mask[w * nchan + ch] != 0;
+      if (ok) v = __ldg(spec + (w * nchan + ch) * spec_pitch + f0 + f);
+    }
+    sm[wl][c][f] = v;
+  }
+  __syncthreads();
+  // write: item = (f, kc, row); thread computes the 4 planes of 8 windows
+  for (int it = tid; it < kPackF * kTcKc * kPackC; it += 256) {
+    const int row = it % kPackC;
+    const int kc = (it / kPackC) % kTcKc;
+    const int f = it / (kPackC * kTcKc);
+    if (f0 + f >= nspec || c0 + row >= cpad) continue;
+    uint32_t w_rh[4], w_rl[4], w_ih[4], w_il[4];
+#pragma unroll
+    for (int e2 = 0; e2 < 4; ++e2) {
+      uint32_t rh = 0, rl = 0, ih = 0, il = 0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float2 v = sm[kc * 8 + e2 * 2 + h][row][f];
+        const uint16_t a = bf16_bits_rn(v.x);
+        const uint16_t b = bf16_bits_rn(v.x - bf16_bits_to_float(a));
+        const uint16_t c = bf16_bits_rn(v.y);
+        const uint16_t d = bf16_bits_rn(v.y - bf16_bits_to_float(c));
+        rh |= (uint32_t)a << (16 * h);
+        rl |= (uint32_t)b << (16 * h);
+        ih |= (uint32_t)c << (16 * h);
+        il |= (uint32_t)d << (16 * h);
+      }
+      w_rh[e2] = rh;
+      w_rl[e2] = rl;
+      w_ih[e2] = ih;
+      w_il[e2] = il;
+    }
+    const int64_t fo = f0 + f;
+    // chunk index of (f, plane, kb, kc) -> rows [0, cpad)
+    const int64_t base = (((fo * kTcPlanes) * nkb + kb) * kTcKc + kc) * cpad + c0 + row;
+    const int64_t plane_stride = (int64_t)nkb * kTcKc * cpad;
+    packed[base + 0 * plane_stride] = make_uint4(w_rh[0], w_rh[1], w_rh[2], w_rh[3]);
+    packed[base + 1 * plane_stride] = make_uint4(w_rl[0], w_rl[1], w_rl[2], w_rl[3]);
+    packed[base + 2 * plane_stride] = make_uint4(w_ih[0], w_ih[1], w_ih[2], w_ih[3]);
+    packed[base + 3 * plane_stride] = make_uint4(w_il[0], w_il[1], w_il[2], w_il[3]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 GEMM
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false after ~2 s without completion.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try(bar, parity)) return true;
+    if ((i & 255u) == 0 && globaltimer() - t0 > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// tcgen05 shared-memory descriptor, K-major, no swizzle:
+// start>>4 [0,14), LBO>>4 [16,30) (K-direction core-matrix stride),
+// SBO>>4 [32,46) (M/N-direction 8-row stride), version 1 at [46,48).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A bf16 (7-9 = 1),
+// B bf16 (10-12 = 1), negate A (13), K-major A/B (15,16 = 0), N>>3 at 17,
+// M>>4 at 24.
+__host__ __device__ constexpr uint32_t umma_idesc(int m, int n, bool neg_a) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((neg_a ? 1u : 0u) << 13) |
+         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_xc_tc_gemm(const uint4* __restrict__ packed, int nkb, int cpad,
+                 const TcTile* __restrict__ tiles, const int32_t* __restrict__ maps, int nspec,
+                 float scale, float2* __restrict__ stack, int64_t stack_pitch,
+                 int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* stage_base = smem;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)kTcStages * kTcStageBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
+  const uint32_t bar_full0 = smem_u32(bars + 0);
+  const uint32_t bar_empty0 = smem_u32(bars + 2);
+  const uint32_t bar_acc = smem_u32(bars + 4);
+
+  const TcTile tile = tiles[blockIdx.x];
+  const int f = blockIdx.y;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int n = tile.n;
+  const uint32_t b_plane_bytes = (uint32_t)n * kTcKb * 2;  // n rows x 64 B
+  const uint32_t a_plane_bytes = (uint32_t)kTcM * kTcKb * 2;
+
+  // Zero the padding rows once (bulk copies never write them).
+  if (tile.am < kTcM || tile.bn < n) {
+    for (int s = 0; s < kTcStages; ++s) {
+      unsigned char* st = stage_base + (size_t)s * kTcStageBytes;
+      for (int pl = 0; pl < kTcPlanes; ++pl)
+        for (int kc = 0; kc < kTcKc; ++kc) {
+          uint4* a = reinterpret_cast<uint4*>(st + pl * a_plane_bytes + kc * kTcM * 16);
+          for (int r = tile.am + threadIdx.x; r < kTcM; r += kTcThreads) a[r] = make_uint4(0, 0, 0, 0);
+          uint4* b = reinterpret_cast<uint4*>(st + kTcABytes + pl * b_plane_bytes + kc * n * 16);
+          for (int r = tile.bn + threadIdx.x; r < n; r += kTcThreads) b[r] = make_uint4(0, 0, 0, 0);
+        }
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; ++s) {
+      mbar_init(bar_full0 + 8 * s, 1);
+      mbar_init(bar_empty0 + 8 * s, 1);
+    }
+    mbar_init(bar_acc, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // make the generic-proxy zero fill visible to the tensor core (async proxy)
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  bool failed = false;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const int64_t plane_stride = (int64_t)nkb * kTcKc * cpad;  // in 16-byte chunks
+      const uint32_t tx = (uint32_t)kTcPlanes * kTcKc * (uint32_t)(tile.am + tile.bn) * 16u;
+      int issued = 0;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kTcStages;
+        const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
+        if (!mbar_wait(bar_empty0 + 8 * s, ph ^ 1u)) {
+          failed = true;
+          break;
+        }
+        const uint32_t full = bar_full0 + 8 * s;
+        mbar_expect_tx(full, tx);
+        const uint32_t st = smem_u32(stage_base + (size_t)s * kTcStageBytes);
+        for (int pl = 0; pl < kTcPlanes; ++pl) {
+          const int64_t pbase = (((int64_t)f * kTcPlanes + pl) * nkb + kb) * kTcKc * cpad;
+          for (int kc = 0; kc < kTcKc; ++kc) {
+            const uint4* srcA = packed + pbase + (int64_t)kc * cpad + tile.a0;
+            const uint4* srcB = packed + pbase + (int64_t)kc * cpad + tile.b0;
+            bulk_g2s(st + pl * a_plane_bytes + kc * kTcM * 16, srcA, (uint32_t)tile.am * 16u, full);
+            bulk_g2s(st + kTcABytes + pl * b_plane_bytes + kc * n * 16, srcB, (uint32_t)tile.bn * 16u,
+                     full);
+          }
+        }
+        ++issued;
+      }
+      (void)plane_stride;
+      if (failed) {
+        atomicExch(err, 1);
+        // drain the copies already issued before leaving
+        for (int kb = 0; kb < issued; ++kb) (void)mbar_wait(bar_full0 + 8 * (kb % kTcStages),
+                                                            (uint32_t)(kb / kTcStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t id_pos = umma_idesc(kTcM, n, false);
+      const uint32_t id_neg = umma_idesc(kTcM, n, true);
+      const uint32_t acc_re = tmem, acc_im = tmem + kTcAccImCol;
+      const uint32_t a_lbo = kTcM * 16, b_lbo = (uint32_t)n * 16, sbo = 128;
+      bool first = true;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kTcStages;
+        const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
+        if (!mbar_wait(bar_full0 + 8 * s, ph)) {
+          failed = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem_u32(stage_base + (size_t)s * kTcStageBytes);
+        const uint32_t sa = st, sb = st + kTcABytes;
+#pragma unroll
+        for (int ks = 0; ks < kTcKc / 2; ++ks) {
+          const uint32_t koff_a = ks * 2 * a_lbo, koff_b = ks * 2 * b_lbo;
+          uint64_t A[4], B[4];
+#pragma unroll
+          for (int pl = 0; pl < 4; ++pl) {
+            A[pl] = umma_desc(sa + pl * a_plane_bytes + koff_a, a_lbo, sbo);
+            B[pl] = umma_desc(sb + pl * b_plane_bytes + koff_b, b_lbo, sbo);
+          }
+          const uint32_t acc = first ? 0u : 1u;
+          // Re += re.re + im.im (hi.hi, hi.lo, lo.hi)
+          umma_bf16(acc_re, A[0], B[0], id_pos, acc);
+          umma_bf16(acc_re, A[0], B[1], id_pos, 1);
+          umma_bf16(acc_re, A[1], B[0], id_pos, 1);
+          umma_bf16(acc_re, A[2], B[2], id_pos, 1);
+          umma_bf16(acc_re, A[2], B[3], id_pos, 1);
+          umma_bf16(acc_re, A[3], B[2], id_pos, 1);
+          // Im += re.im - im.re
+          umma_bf16(acc_im, A[0], B[2], id_pos, acc);
+          umma_bf16(acc_im, A[0], B[3], id_pos, 1);
+          umma_bf16(acc_im, A[1], B[2], id_pos, 1);
+          umma_bf16(acc_im, A[2], B[0], id_neg, 1);
+          umma_bf16(acc_im, A[2], B[1], id_neg, 1);
+          umma_bf16(acc_im, A[3], B[0], id_neg, 1);
+          first = false;
+        }
+        umma_commit(bar_empty0 + 8 * s);  // stage free once these MMAs are done
+      }
+      if (failed) atomicExch(err, 1);
+      umma_commit(bar_acc);  // accumulators complete (or abandoned)
+    }
+  } else {
+    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    const int q = warp & 3;
+    const int row = q * 32 + lane;  // src row within the tile
+    const bool ok = mbar_wait(bar_acc, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+      atomicExch(err, 1);
+      failed = true;
+    } else {
+      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+      const int32_t* map = maps + tile.map_offset + (int64_t)row * n;
+      for (int c0 = 0; c0 < n; c0 += 16) {
+        float re[16], im[16];
+        tmem_ld16(lane_base + (uint32_t)c0, re);
+        tmem_ld16(lane_base + kTcAccImCol + (uint32_t)c0, im);
+        tmem_ld_wait();
+        if (row < tile.am) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int b = c0 + j;
+            if (b < tile.bn) {
+              const int32_t v = __ldg(map + b);
+              if (v != -1) {
+                const bool rev = v < -1;
+                const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
+                const float im_s = rev ? -im[j] : im[j];
+                stack[p * stack_pitch + f] = make_float2(re[j] * scale, im_s * scale);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+  (void)nspec;
+}
+
+int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
+                           int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
+                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch) {
+  const XcTensorPlan* tp = plan->tensor;
+  FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
+  if (tp->ntiles == 0) return FXC_OK;
+  FXC_CHECK_ARG(nspec <= 65535, "nspec %d above the tensor grid limit", nspec);
+  const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
+  if (nkb == 0) {
+    // no windows: every stacked bin is zero
+    FXC_CUDA_TRY(cudaMemset2DAsync(stack, sizeof(float2) * (size_t)stack_pitch, 0,
+                                   sizeof(float2) * (size_t)nspec, (size_t)plan->npairs,
+                                   ctx->stream));
+    return FXC_OK;
+  }
+  const int cpad = tp->cpad;
+  const size_t packed_chunks = (size_t)nspec * kTcPlanes * nkb * kTcKc * (size_t)cpad;
+  FXC_TRY(ctx->scratch3.reserve(packed_chunks * 16));
+  uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
+  dim3 pg((unsigned)((nspec + kPackF - 1) / kPackF), (unsigned)((cpad + kPackC - 1) / kPackC),
+          (unsigned)nkb);
+  k_xc_pack<<<pg, 256, 0, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch, mask, nkb, cpad,
+                                         packed);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  FXC_CUDA_TRY(cudaFuncSetAttribute(k_xc_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kTcSmemBytes));
+  dim3 gg((unsigned)tp->ntiles, (unsigned)nspec);
+  k_xc_tc_gemm<<<gg, kTcThreads, kTcSmemBytes, ctx->stream>>>(
+      packed, nkb, cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, ctx->d_err);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
 }
 
 }  // namespace fxc

@@ -41,6 +41,7 @@ extern "C" {
 #define FXC_ERR_NOMEM (-4)       /* device or host allocation failed */
 #define FXC_ERR_IO (-5)          /* file format or I/O error */
 #define FXC_ERR_NODEVICE (-6)    /* no CUDA device / driver */
+#define FXC_ERR_TIMEOUT (-7)     /* a kernel's bounded device-side wait gave up */
 
 #define FXC_XC_PLAIN 0  /* FP32 CUDA-core per-pair product, register blocked */
 #define FXC_XC_TENSOR 1 /* BF16 hi/lo split tcgen05 contraction S(f)=Y^H Y */
