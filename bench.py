@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="auto", choices=["auto", "plain", "tensor"])
     ap.add_argument("--days", type=int, default=NDAYS)
+    ap.add_argument("--nspec", type=int, default=NSPEC, help="smaller values only for profiling runs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -212,6 +213,7 @@ def main():
     from fastxc_gb300.core import Context, PairPlan, xc_shape
     from fastxc_gb300.synthetic import cross_station_pairs, spectra_device, station_array
 
+    nspec = args.nspec
     nwin = NSTEP * args.days
     arr = station_array(NSTA, seed=0)
     nchan = arr.nchan
@@ -220,17 +222,17 @@ def main():
     stream = torch.cuda.current_stream(dev)
     ctx = Context(local, stream.cuda_stream)
     plan = PairPlan(ctx, src, rec, nchan)
-    shape = xc_shape(NSPEC, NSTEP, DT, CC_LEN)
-    spec, mask = spectra_device(torch, nwin, arr, NSPEC, DT, seed=rank, gap_frac=GAP_FRAC, device=dev)
+    shape = xc_shape(nspec, NSTEP, DT, CC_LEN)
+    spec, mask = spectra_device(torch, nwin, arr, nspec, DT, seed=rank, gap_frac=GAP_FRAC, device=dev)
     scale = 1.0 / nwin  # mean over days of per-day stacks with 1/nstep each
-    pitch_stack = (NSPEC + 3) // 4 * 4
+    pitch_stack = (nspec + 3) // 4 * 4
     d_stack = torch.empty((npairs, pitch_stack), dtype=torch.complex64, device=dev)
     d_ncf = torch.empty((npairs, shape.cc_size), dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
 
     methods = {"plain": FXC_XC_PLAIN}
     try:
-        ctx.xc_stack(plan, spec, nwin, nchan, NSPEC, NSPEC, None, scale, d_stack, pitch_stack, FXC_XC_TENSOR)
+        ctx.xc_stack(plan, spec, nwin, nchan, nspec, nspec, None, scale, d_stack, pitch_stack, FXC_XC_TENSOR)
         torch.cuda.synchronize()
         methods["tensor"] = FXC_XC_TENSOR
     except FxcError:
@@ -242,15 +244,27 @@ def main():
         if head not in methods:
             raise SystemExit(f"method {head} not available")
 
+    packed_bytes = Context.xc_packed_bytes(nchan, nwin, nspec)
+    d_packed = torch.empty((max(packed_bytes, 16) // 16, 4), dtype=torch.int32, device=dev) if "tensor" in methods else None
+
     def step(method, ev=None):
+        # events: 0 start, 1 after pack (tensor only), 2 after stack, 3 after finalize
         if ev is not None:
             ev[0].record(stream)
-        ctx.xc_stack(plan, spec, nwin, nchan, NSPEC, NSPEC, None, scale, d_stack, pitch_stack, method)
-        if ev is not None:
-            ev[1].record(stream)
-        ctx.xc_finalize(d_stack, npairs, pitch_stack, shape, d_ncf)
+        if method == FXC_XC_TENSOR:
+            ctx.xc_pack(spec, nwin, nchan, nspec, nspec, None, d_packed)
+            if ev is not None:
+                ev[1].record(stream)
+            ctx.xc_stack_packed(plan, d_packed, nwin, nspec, scale, d_stack, pitch_stack)
+        else:
+            if ev is not None:
+                ev[1].record(stream)
+            ctx.xc_stack(plan, spec, nwin, nchan, nspec, nspec, None, scale, d_stack, pitch_stack, method)
         if ev is not None:
             ev[2].record(stream)
+        ctx.xc_finalize(d_stack, npairs, pitch_stack, shape, d_ncf)
+        if ev is not None:
+            ev[3].record(stream)
 
     def barrier():
         if world > 1:
@@ -258,12 +272,13 @@ def main():
 
     results = {}
     sampler = ClockSampler(local)
+    clocks = None
     for name in (["plain", "tensor"] if "tensor" in methods else ["plain"]):
         m = methods[name]
         for _ in range(args.warmup):
             step(m)
         torch.cuda.synchronize()
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
         barrier()
         torch.cuda.synchronize()
         if name == head:
@@ -285,11 +300,12 @@ def main():
             t = torch.tensor([total_ms], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             total_ms = float(t.item())
-        stack_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
-        fin_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+        pack_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+        kern_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+        fin_ms = statistics.mean(e[2].elapsed_time(e[3]) for e in evs)
         ncf_snapshot = d_ncf[:16].float().cpu().numpy().copy()
-        results[name] = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps, "stack_ms": stack_ms,
-                         "finalize_ms": fin_ms, "launches": launches, "ncf16": ncf_snapshot}
+        results[name] = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps, "pack_ms": pack_ms,
+                         "stack_ms": kern_ms, "finalize_ms": fin_ms, "launches": launches, "ncf16": ncf_snapshot}
 
     # parity sample: 16 pairs over all windows against the FP64 oracle
     from oracle import xc_oracle as xo
@@ -298,7 +314,7 @@ def main():
     chans = np.unique(np.concatenate([src[sel], rec[sel]]))
     remap = {c: i for i, c in enumerate(chans)}
     host_spec = spec[:, torch.tensor(chans, device=dev), :].cpu().numpy()
-    oshape = xo.finalize_shape(NSPEC, NSTEP, DT, CC_LEN)
+    oshape = xo.finalize_shape(nspec, NSTEP, DT, CC_LEN)
     ref = xo.xc_run(host_spec, np.array([remap[c] for c in src[sel]]), np.array([remap[c] for c in rec[sel]]),
                     scale, oshape)
     rel = {}
@@ -313,30 +329,41 @@ def main():
     hr = results[head]
     value = pw * world / (hr["total_ms"] / args.steps / 1e3)
 
-    # roofline of the dominant kernel (the stack kernel)
-    import json as _json
-
+    # roofline of the dominant kernel: the tcgen05 GEMM (tensor) or the plain
+    # stack kernel, each timed with CUDA events on the launching stream
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
-        peaks = _json.loads(pk.read_text())
-    useful_flop = 8.0 * NSPEC * pw  # complex MAC per pair-window-bin
+        peaks = json.loads(pk.read_text())
+    useful_flop = 8.0 * nspec * pw  # one complex MAC (8 flop) per pair-window-bin
     if head == "tensor":
-        issued = None
-        bound, unit = "tensor", "TFLOP/s"
-        achieved = useful_flop / (hr["stack_ms"] / 1e3) / 1e12
-        peak = peaks.get("bf16_tflops", 1900.0)
-        peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
+        # issued MMA flops: per (tile, bin, 32-window block) 24 MMAs of 128 x n x 16
+        nkb = (nwin + 31) // 32
+        sum_n = 0
+        for a0 in range(0, nchan, 128):
+            for b0 in range(a0, nchan, 256):
+                sum_n += (min(256, nchan - b0) + 15) // 16 * 16
+        issued = float(nspec) * nkb * 24 * 2 * 128 * 16 * sum_n
+        kms = hr["stack_ms"]
+        achieved = issued / (kms / 1e3) / 1e12
+        peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        peak_src = ("measured sustained bf16 (cuBLAS, MEASURED_PEAKS.json)" if "bf16_tflops_sustained" in peaks
+                    else "fallback 1.7 PFLOP/s sustained")
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                    "traffic": None, "peak_source": peak_src, "kernel": "k_xc_tc_gemm",
+                    "algorithmic": "issued MMA flops = nspec x ceil(nwin/32) x 24 x (2 x 128 x 16 x n) summed over tiles "
+                                   "(3 bf16 hi/lo products, Re and Im, upper-triangle tiles)",
+                    "useful_tflops": useful_flop / (kms / 1e3) / 1e12, "kernel_ms": kms,
+                    "pack_ms": hr["pack_ms"], "finalize_ms": hr["finalize_ms"]}
     else:
-        bound, unit = "fp32", "TFLOP/s"
-        achieved = useful_flop / (hr["stack_ms"] / 1e3) / 1e12
+        kms = hr["stack_ms"]
+        achieved = useful_flop / (kms / 1e3) / 1e12
         sm_max = peaks.get("sm_max_mhz", 2070.0)
-        peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # FP32 FMA lanes x 2 flop x max SM clock
-        peak_src = "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)"
-    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
-                "traffic": None, "peak_source": peak_src, "kernel": "k_xc_stack_plain" if head == "plain" else "xc tensor",
-                "algorithmic": "8 flop x nspec x pair-windows (useful complex MAC flops)",
-                "finalize_ms": hr["finalize_ms"], "stack_ms": hr["stack_ms"]}
+        peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                    "traffic": None, "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)",
+                    "kernel": "k_xc_stack_plain", "algorithmic": "8 flop x nspec x pair-windows",
+                    "kernel_ms": kms, "finalize_ms": hr["finalize_ms"]}
 
     line = {
         "metric": "pair-windows/s",
@@ -353,12 +380,13 @@ def main():
         "data": "synthetic (seeded whitened-like spectra, coherent 0.1-2 Hz source, 5% gap windows)",
         "method": head,
         "config": {"workload": f"xc linear stack: {NSTA} sta x {NCOMP} comp x {args.days} days, delta {DT}s, "
-                               f"win 3600s -> {nwin} windows, nspec {NSPEC}, {npairs} pairs, lag {CC_LEN}s",
-                   "pairs": npairs, "windows": nwin, "nspec": NSPEC, "cc_size": shape.cc_size,
+                               f"win 3600s -> {nwin} windows, nspec {nspec}, {npairs} pairs, lag {CC_LEN}s",
+                   "pairs": npairs, "windows": nwin, "nspec": nspec, "cc_size": shape.cc_size,
                    "l2": "inputs (20.5 GB) larger than L2, no flush", "parallelism": f"replicas x{world}"},
         "rel_l2_vs_fp64": rel,
         "per_method": {k: {"pair_windows_per_s": pw / (v["ms_per_step"] / 1e3), "ms_per_step": v["ms_per_step"],
-                           "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"]} for k, v in results.items()},
+                           "pack_ms": v["pack_ms"], "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"]}
+                       for k, v in results.items()},
         "roofline": roofline,
         "gpu_launches": hr["launches"],
         "clocks": clocks,
@@ -371,16 +399,17 @@ def main():
         host_spec = torch.empty(spec.shape, dtype=torch.complex64, pin_memory=True)
         host_spec.copy_(spec)
         host_ncf = torch.empty((npairs, shape.cc_size), dtype=torch.float32, pin_memory=True)
-        del d_stack
+        del d_stack, d_packed
+        torch.cuda.empty_cache()
         hs = host_spec.numpy()
         hn = host_ncf.numpy()
         m = methods[head]
-        ctx.xc_run_host(plan, hs, nwin, nchan, NSPEC, None, scale, shape, hn, m)
+        ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
         barrier()
         t0 = time.perf_counter()
         e2e_steps = max(1, min(args.steps, 5))
         for _ in range(e2e_steps):
-            ctx.xc_run_host(plan, hs, nwin, nchan, NSPEC, None, scale, shape, hn, m)
+            ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
         el = (time.perf_counter() - t0) / e2e_steps
         if world > 1:
             t = torch.tensor([el], device=dev)

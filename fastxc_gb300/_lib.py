@@ -76,6 +76,9 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_pairplan_npairs": (_i64, [_vp]),
     "fxc_pairplan_ntiles": (_i64, [_vp]),
     "fxc_xc_stack": (_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, _vp, _f32, _vp, _i64, _int]),
+    "fxc_xc_packed_bytes": (_int, [_i32, _i64, _i32, C.POINTER(_i64)]),
+    "fxc_xc_pack": (_int, [_vp, _vp, _i64, _i32, _i32, _i64, _vp, _vp]),
+    "fxc_xc_stack_packed": (_int, [_vp, _vp, _vp, _i64, _i32, _f32, _vp, _i64]),
     "fxc_xc_finalize": (_int, [_vp, _vp, _i64, _i64, C.POINTER(XcShape), _vp]),
     "fxc_xc_run": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
     "fxc_xc_run_host": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),

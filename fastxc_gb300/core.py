@@ -90,6 +90,20 @@ class Context:
         lib().fxc_xc_stack(self.handle, plan.handle, _ptr(d_spec), nwin, nchan, nspec, spec_pitch,
                            _ptr(d_mask), float(scale), _ptr(d_stack), stack_pitch, method)
 
+    @staticmethod
+    def xc_packed_bytes(nchan, nwin, nspec) -> int:
+        out = C.c_int64()
+        lib().fxc_xc_packed_bytes(nchan, nwin, nspec, C.byref(out))
+        return int(out.value)
+
+    def xc_pack(self, d_spec, nwin, nchan, nspec, spec_pitch, d_mask, d_packed):
+        lib().fxc_xc_pack(self.handle, _ptr(d_spec), nwin, nchan, nspec, spec_pitch, _ptr(d_mask),
+                          _ptr(d_packed))
+
+    def xc_stack_packed(self, plan: "PairPlan", d_packed, nwin, nspec, scale, d_stack, stack_pitch):
+        lib().fxc_xc_stack_packed(self.handle, plan.handle, _ptr(d_packed), nwin, nspec, float(scale),
+                                  _ptr(d_stack), stack_pitch)
+
     def xc_finalize(self, d_stack, npairs, stack_pitch, shape: XcShape, d_ncf):
         lib().fxc_xc_finalize(self.handle, _ptr(d_stack), npairs, stack_pitch, C.byref(shape),
                               _ptr(d_ncf))

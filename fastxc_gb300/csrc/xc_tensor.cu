@@ -25,8 +25,9 @@
 //                    tcgen05.mma (M=128, N, K=16) per K step into two FP32
 //                    accumulators (Re at column 0, Im at column 256) and
 //                    frees each stage with tcgen05.commit;
-//        warps 2..5  epilogue: tcgen05.ld of the accumulators, scale,
-//                    conjugate reversed pairs, scatter to the pair rows.
+//        warps 2..9  epilogue: tcgen05.ld of the accumulators, scale,
+//                    conjugate reversed pairs, scatter to the pair rows
+//                    (two warps per TMEM lane quarter, alternate chunks).
 //      Only the upper triangle of channel tiles is computed (a pair is
 //      computed in the orientation (min, max) and conjugated if reversed).
 //      Every mbarrier wait is bounded by %globaltimer (2 s); a timeout sets
@@ -37,6 +38,7 @@
 #include <vector>
 
 #include "context.cuh"
+#include "fft_launch.cuh"
 #include "xc.cuh"
 
 namespace fxc {
@@ -46,7 +48,7 @@ constexpr int kTcKc = kTcKb / 8;      // 16-byte core-matrix chunks per K-block 
 constexpr int kTcM = 128;             // MMA M (src channel rows per tile)
 constexpr int kTcNmax = 256;          // MMA N limit (rec channel rows per tile)
 constexpr int kTcStages = 2;
-constexpr int kTcThreads = 192;       // 6 warps
+constexpr int kTcThreads = 320;       // 10 warps: producer, MMA, 8 epilogue
 constexpr int kTcPlanes = 4;          // re-hi, re-lo, im-hi, im-lo
 constexpr uint32_t kTcAccImCol = 256; // TMEM column of the Im accumulator
 constexpr int kTcABytes = kTcPlanes * kTcM * kTcKb * 2;     // 32 KB per stage
@@ -169,13 +171,15 @@ void xc_tensor_plan_free(fxc_pairplan* plan) {
 // ---------------------------------------------------------------------------
 // Pack kernel
 // ---------------------------------------------------------------------------
-// CTA: 8 frequencies x 16 channels x one K-block of 32 windows.
-// Load [32 w][16 c][8 f] complex through shared memory, then every thread
-// writes 16-byte chunks (8 windows of one plane, one row): consecutive
-// threads write consecutive rows (256 contiguous bytes per 16 threads).
+// CTA: 16 frequencies x 16 channels x one K-block of 32 windows.
+// Thread (c = tid / 16, f = tid % 16) loads its 32 windows with all loads in
+// flight at once (each 16-thread group reads one 128-byte run), then every
+// thread writes 16-byte chunks (8 windows of one plane, one row):
+// consecutive threads write consecutive rows (256 contiguous bytes).
 
-constexpr int kPackF = 8;
+constexpr int kPackF = 16;
 constexpr int kPackC = 16;
+constexpr size_t kPackSmem = sizeof(float2) * kTcKb * kPackC * (kPackF + 1);
 
 __device__ __forceinline__ uint16_t bf16_bits_rn(float x) {
   // round-to-nearest-even float -> bf16 (inputs are finite: the spectra are
@@ -193,25 +197,27 @@ __global__ void __launch_bounds__(256)
     k_xc_pack(const float2* __restrict__ spec, int64_t nwin, int nchan, int nspec,
               int64_t spec_pitch, const uint8_t* __restrict__ mask, int nkb, int cpad,
               uint4* __restrict__ packed) {
-  __shared__ float2 sm[kTcKb][kPackC][kPackF + 1];
+  extern __shared__ float2 psm[];  // [kTcKb][kPackC][kPackF + 1]
   const int f0 = blockIdx.x * kPackF;
   const int c0 = blockIdx.y * kPackC;
   const int kb = blockIdx.z;
   const int tid = threadIdx.x;
-  // load: 32 w x 32 c rows of 8 complex; thread -> (row, f) with f fastest
-  for (int e = tid; e < kTcKb * kPackC * kPackF; e += 256) {
-    const int f = e % kPackF;
-    const int c = (e / kPackF) % kPackC;
-    const int wl = e / (kPackF * kPackC);
-    const int64_t w = (int64_t)kb * kTcKb + wl;
+  {
+    const int f = tid % kPackF;
+    const int c = tid / kPackF;
     const int ch = c0 + c;
-    float2 v = make_float2(0.f, 0.f);
-    if (w < nwin && ch < nchan && f0 + f < nspec) {
-      bool ok = true;
-      if (mask) ok = mask[w * nchan + ch] != 0;
-      if (ok) v = __ldg(spec + (w * nchan + ch) * spec_pitch + f0 + f);
+    const bool okcf = ch < nchan && f0 + f < nspec;
+    const int64_t w0 = (int64_t)kb * kTcKb;
+    float2 v[kTcKb];
+#pragma unroll
+    for (int k = 0; k < kTcKb; ++k) {
+      const int64_t w = w0 + k;
+      bool ok = okcf && w < nwin;
+      if (ok && mask) ok = __ldg(mask + w * nchan + ch) != 0;
+      v[k] = ok ? __ldg(spec + (w * nchan + ch) * spec_pitch + f0 + f) : make_float2(0.f, 0.f);
     }
-    sm[wl][c][f] = v;
+#pragma unroll
+    for (int k = 0; k < kTcKb; ++k) psm[(k * kPackC + c) * (kPackF + 1) + f] = v[k];
   }
   __syncthreads();
   // write: item = (f, kc, row); thread computes the 4 planes of 8 windows
@@ -226,7 +232,7 @@ __global__ void __launch_bounds__(256)
       uint32_t rh = 0, rl = 0, ih = 0, il = 0;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const float2 v = sm[kc * 8 + e2 * 2 + h][row][f];
+        const float2 v = psm[((kc * 8 + e2 * 2 + h) * kPackC + row) * (kPackF + 1) + f];
         const uint16_t a = bf16_bits_rn(v.x);
         const uint16_t b = bf16_bits_rn(v.x - bf16_bits_to_float(a));
         const uint16_t c = bf16_bits_rn(v.y);
@@ -495,8 +501,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       umma_commit(bar_acc);  // accumulators complete (or abandoned)
     }
   } else {
-    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    // epilogue warps 2..9: TMEM lane quarter = warp % 4; the two warps of a
+    // quarter take alternate 16-column chunks. The pair-map words of the next
+    // chunk are fetched (16-byte loads) while the current chunk is stored.
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row = q * 32 + lane;  // src row within the tile
     const bool ok = mbar_wait(bar_acc, 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -505,27 +514,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       failed = true;
     } else {
       const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-      const int32_t* map = maps + tile.map_offset + (int64_t)row * n;
-      for (int c0 = 0; c0 < n; c0 += 16) {
+      const int4* map4 = reinterpret_cast<const int4*>(maps + tile.map_offset + (int64_t)row * n);
+      const bool row_ok = row < tile.am;
+      int4 mcur[4], mnxt[4];
+      int c0 = 16 * half;
+      if (row_ok && c0 < n) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) mcur[k] = __ldg(map4 + c0 / 4 + k);
+      }
+      for (; c0 < n; c0 += 32) {
+        const int c1 = c0 + 32;
+        if (row_ok && c1 < n) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) mnxt[k] = __ldg(map4 + c1 / 4 + k);
+        }
         float re[16], im[16];
         tmem_ld16(lane_base + (uint32_t)c0, re);
         tmem_ld16(lane_base + kTcAccImCol + (uint32_t)c0, im);
         tmem_ld_wait();
-        if (row < tile.am) {
+        if (row_ok) {
+          const int32_t* mv = reinterpret_cast<const int32_t*>(mcur);
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int b = c0 + j;
-            if (b < tile.bn) {
-              const int32_t v = __ldg(map + b);
-              if (v != -1) {
-                const bool rev = v < -1;
-                const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
-                const float im_s = rev ? -im[j] : im[j];
-                stack[p * stack_pitch + f] = make_float2(re[j] * scale, im_s * scale);
-              }
+            const int32_t v = mv[j];  // padding columns (b >= bn) hold -1
+            if (v != -1) {
+              const bool rev = v < -1;
+              const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
+              const float im_s = rev ? -im[j] : im[j];
+              stack[p * stack_pitch + f] = make_float2(re[j] * scale, im_s * scale);
             }
           }
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) mcur[k] = mnxt[k];
       }
     }
   }
@@ -538,12 +559,32 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   (void)nspec;
 }
 
-int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
-                           int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
-                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch) {
+static int64_t packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
+  const int64_t nkb = (nwin + kTcKb - 1) / kTcKb;
+  return (int64_t)nspec * kTcPlanes * nkb * kTcKc * round_up(nchan, 8);
+}
+
+int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, int nspec,
+                   int64_t spec_pitch, const uint8_t* mask, uint4* packed) {
+  const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
+  if (nkb == 0 || nspec == 0) return FXC_OK;
+  const int cpad = (int)round_up(nchan, 8);
+  FXC_CHECK_ARG((cpad + kPackC - 1) / kPackC <= 65535 && nkb <= 65535, "pack grid too large");
+  dim3 pg((unsigned)((nspec + kPackF - 1) / kPackF), (unsigned)((cpad + kPackC - 1) / kPackC),
+          (unsigned)nkb);
+  FXC_TRY(set_smem_limit(k_xc_pack, kPackSmem));
+  k_xc_pack<<<pg, 256, kPackSmem, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch, mask, nkb,
+                                                 cpad, packed);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
+                   int nspec, float scale, float2* stack, int64_t stack_pitch) {
   const XcTensorPlan* tp = plan->tensor;
   FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
-  if (tp->ntiles == 0) return FXC_OK;
+  if (tp->ntiles == 0 || nspec == 0) return FXC_OK;
   FXC_CHECK_ARG(nspec <= 65535, "nspec %d above the tensor grid limit", nspec);
   const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
   if (nkb == 0) {
@@ -553,24 +594,62 @@ int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2*
                                    ctx->stream));
     return FXC_OK;
   }
-  const int cpad = tp->cpad;
-  const size_t packed_chunks = (size_t)nspec * kTcPlanes * nkb * kTcKc * (size_t)cpad;
-  FXC_TRY(ctx->scratch3.reserve(packed_chunks * 16));
-  uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
-  dim3 pg((unsigned)((nspec + kPackF - 1) / kPackF), (unsigned)((cpad + kPackC - 1) / kPackC),
-          (unsigned)nkb);
-  k_xc_pack<<<pg, 256, 0, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch, mask, nkb, cpad,
-                                         packed);
-  count_launch();
-  FXC_LAUNCH_CHECK();
-  FXC_CUDA_TRY(cudaFuncSetAttribute(k_xc_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kTcSmemBytes));
+  FXC_TRY(set_smem_limit(k_xc_tc_gemm, kTcSmemBytes));
   dim3 gg((unsigned)tp->ntiles, (unsigned)nspec);
   k_xc_tc_gemm<<<gg, kTcThreads, kTcSmemBytes, ctx->stream>>>(
-      packed, nkb, cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, ctx->d_err);
+      packed, nkb, tp->cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, ctx->d_err);
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;
 }
 
+int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
+                           int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
+                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch) {
+  const XcTensorPlan* tp = plan->tensor;
+  FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
+  if (tp->ntiles == 0) return FXC_OK;
+  const int64_t chunks = packed_chunks(nchan, nwin, nspec);
+  if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
+  uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
+  FXC_TRY(xc_pack_launch(ctx, spec, nwin, nchan, nspec, spec_pitch, mask, packed));
+  return xc_gemm_launch(ctx, plan, packed, nwin, nspec, scale, stack, stack_pitch);
+}
+
 }  // namespace fxc
+
+using namespace fxc;
+
+extern "C" {
+
+int fxc_xc_packed_bytes(int32_t nchan, int64_t nwin, int32_t nspec, int64_t* out_bytes) {
+  clear_error();
+  FXC_CHECK_ARG(out_bytes != nullptr, "out_bytes is null");
+  FXC_CHECK_ARG(nchan > 0 && nwin >= 0 && nspec >= 0, "invalid shape");
+  *out_bytes = packed_chunks(nchan, nwin, nspec) * 16;
+  return FXC_OK;
+}
+
+int fxc_xc_pack(fxc_ctx* ctx, const float* d_spec, int64_t nwin, int32_t nchan, int32_t nspec,
+                int64_t spec_pitch, const uint8_t* d_mask, void* d_packed) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(nchan > 0 && nwin >= 0 && nspec >= 0 && spec_pitch >= nspec, "invalid shape");
+  FXC_CHECK_ARG(nwin == 0 || nspec == 0 || (d_spec && d_packed), "null pointer");
+  FXC_CHECK_ARG(((uintptr_t)d_packed & 15) == 0, "d_packed must be 16-byte aligned");
+  return xc_pack_launch(ctx, reinterpret_cast<const float2*>(d_spec), nwin, nchan, nspec,
+                        spec_pitch, d_mask, reinterpret_cast<uint4*>(d_packed));
+}
+
+int fxc_xc_stack_packed(fxc_ctx* ctx, const fxc_pairplan* plan, const void* d_packed, int64_t nwin,
+                        int32_t nspec, float scale, float* d_stack, int64_t stack_pitch) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(plan != nullptr, "null pair plan");
+  FXC_CHECK_ARG(nwin >= 0 && nspec >= 1 && stack_pitch >= nspec, "invalid shape");
+  FXC_CHECK_ARG(plan->npairs == 0 || (d_packed && d_stack), "null pointer");
+  return xc_gemm_launch(ctx, plan, reinterpret_cast<const uint4*>(d_packed), nwin, nspec, scale,
+                        reinterpret_cast<float2*>(d_stack), stack_pitch);
+}
+
+}  // extern "C"

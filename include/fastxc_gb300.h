@@ -125,6 +125,19 @@ int fxc_xc_stack(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, in
                  int32_t nchan, int32_t nspec, int64_t spec_pitch, const uint8_t *d_mask,
                  float scale, float *d_stack, int64_t stack_pitch, int method);
 
+/* Tensor-core operand form of the spectra: per bin, bf16 hi/lo planes of
+ * the real and imaginary parts laid out as UMMA core-matrix tiles. Packing
+ * once and keeping the result resident lets many pair plans (requests)
+ * correlate the same spectra without repacking. fxc_xc_stack with
+ * FXC_XC_TENSOR is fxc_xc_pack + fxc_xc_stack_packed through context
+ * scratch. Same stacked-spectrum contract as accumulateStepXc2DKernel
+ * (native/xc/kernels/cuda.kernels.cu:16-36). */
+int fxc_xc_packed_bytes(int32_t nchan, int64_t nwin, int32_t nspec, int64_t *out_bytes);
+int fxc_xc_pack(fxc_ctx *ctx, const float *d_spec, int64_t nwin, int32_t nchan, int32_t nspec,
+                int64_t spec_pitch, const uint8_t *d_mask, void *d_packed);
+int fxc_xc_stack_packed(fxc_ctx *ctx, const fxc_pairplan *plan, const void *d_packed, int64_t nwin,
+                        int32_t nspec, float scale, float *d_stack, int64_t stack_pitch);
+
 /* ncf[p, j] = C2R(stack[p] * (-1)^f)[nfft/2 - half_cc + j] / (nfft * dt),
  * j < cc_size. d_ncf is [npairs][cc_size] float. Replaces
  * finalize_xc_batch (native/xc/worker/executor.cu:6-55). */

@@ -113,6 +113,32 @@ def test_stack_matches_oracle_with_mask_and_ragged_tiles(ctx, torch_cuda, method
     assert np.all(d_stack.cpu().numpy()[:, nspec:] == 0)
 
 
+def test_packed_resident_path_equals_tensor_stack(ctx, torch_cuda):
+    """fxc_xc_pack + fxc_xc_stack_packed (spectra kept in packed form) gives
+    bit-identical stacks to fxc_xc_stack(FXC_XC_TENSOR), for two pair plans
+    on the same packed spectra."""
+    torch = torch_cuda
+    from fastxc_gb300.core import Context, PairPlan
+
+    rng = np.random.default_rng(21)
+    nwin, nchan, nspec = 45, 20, 257
+    spec = make_spec(rng, nwin, nchan, nspec)
+    d_spec = torch.from_numpy(spec).cuda()
+    nbytes = Context.xc_packed_bytes(nchan, nwin, nspec)
+    d_packed = torch.zeros((nbytes // 16, 4), dtype=torch.int32, device="cuda")
+    ctx.xc_pack(d_spec, nwin, nchan, nspec, nspec, None, d_packed)
+    for src, rec in (station_pairs(6), station_pairs(5, auto=True)):
+        plan = PairPlan(ctx, src, rec, nchan)
+        a = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+        b = torch.zeros_like(a)
+        ctx.xc_stack_packed(plan, d_packed, nwin, nspec, 0.5, a, nspec)
+        ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, b, nspec, 1)
+        ctx.synchronize()
+        assert torch.equal(a, b)
+        ref = xo.xc_stack(spec, src, rec, 0.5)
+        assert rel_l2(a.cpu().numpy(), ref) < 2e-5
+
+
 def test_zero_windows_contribute_zero(ctx, torch_cuda):
     """A gap window (all-zero spectrum) changes nothing but the divisor stays nstep."""
     rng = np.random.default_rng(11)
