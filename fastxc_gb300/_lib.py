@@ -137,3 +137,41 @@ def lib() -> _Lib:
     if _LIB is None:
         _LIB = _Lib(Path(os.environ.get("FXC_LIB", LIB_PATH)))
     return _LIB
+
+
+class S2sPlan(C.Structure):
+    """fxc_s2s_plan (include/fastxc_gb300.h)."""
+
+    _fields_ = [
+        ("delta", C.c_float),
+        ("npts", C.c_int32),
+        ("segment_pts", C.c_int32),
+        ("shift_pts", C.c_int32),
+        ("nstep", C.c_int32),
+        ("output_nfft", C.c_int32),
+        ("nspec", C.c_int32),
+        ("filter_padding", C.c_int32),
+        ("filter_nfft", C.c_int32),
+        ("freq_low", C.c_float),
+        ("freq_high", C.c_float),
+        ("f_idx1", C.c_int32),
+        ("f_idx2", C.c_int32),
+        ("f_idx3", C.c_int32),
+        ("f_idx4", C.c_int32),
+        ("taper_pts", C.c_int32),
+        ("runabs_win", C.c_int32),
+        ("whiten_win", C.c_int32),
+        ("whiten", C.c_int32),
+        ("normalize", C.c_int32),
+        ("phase_only", C.c_int32),
+        ("nfilters", C.c_int32),
+        ("band_freq_low", C.c_float * 100),
+    ]
+
+
+_SIGNATURES.update({
+    "fxc_s2s_plan_init": (_int, [_f32, _f32, _f32, _f32, _f32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32,
+                                 C.POINTER(S2sPlan)]),
+    "fxc_s2s_filter_response": (_int, [C.POINTER(S2sPlan), _vp, _vp, _i32, _vp]),
+    "fxc_s2s_run": (_int, [_vp, C.POINTER(S2sPlan), _vp, _i64, _i64, _i32, _i32, _vp, _i32, _vp, _vp, _i64]),
+})

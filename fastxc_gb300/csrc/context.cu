@@ -145,6 +145,7 @@ int fxc_ctx_destroy(fxc_ctx* ctx) {
   ctx->scratch.release();
   ctx->scratch2.release();
   ctx->scratch3.release();
+  ctx->scratch4.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   delete ctx;
   return FXC_OK;

@@ -26,5 +26,6 @@ struct fxc_ctx {
   fxc::Scratch scratch;   // per-pair stacked spectra between stack and finalize
   fxc::Scratch scratch2;  // host-call staging (device copies of host inputs)
   fxc::Scratch scratch3;  // packed bf16 hi/lo operands of the tensor-core path
+  fxc::Scratch scratch4;  // sac2spec intermediate rows (time rows, weights, spectra)
   int* d_err = nullptr;   // device error word: set by kernels whose bounded waits time out
 };

@@ -1,0 +1,824 @@
+// sac2spec hot path: SAC windows -> preprocessed, normalised, whitened
+// output spectra (the stepack payload [step][row][nspec] complex64).
+//
+// Reference: ComputeWorkerBatch (native/sac2spec/worker/compute.cu:8-272)
+// and the kernels it launches (native/sac2spec/kernels/*.cu,
+// native/sac2spec/core/{preprocess,normalization,spectrum}.cu); about 30
+// launches and 5 cuFFT executions per batch there.
+//
+// GB300 design: one CTA (1024 threads) per (window, channel) row keeps the
+// whole row and its transform in shared memory. A real transform of length
+// 2M runs as a length-M complex FFT: forward DIF (natural in, digit-reversed
+// out), a pointwise pass over the bin pairs (k, M-k) that does the real
+// post-processing, the per-bin work (x dt, sanitize, |H|^2, whitening
+// divide, band taper) and the inverse pre-processing in place, then an
+// inverse DIT (digit-reversed in, natural out) -- no permutation pass and
+// no HBM round trip between the forward and the inverse transform.
+// Coupling across the num_ch components of a station (running-absolute-mean
+// weights, whitening weights) goes through small HBM buffers between
+// kernels:
+//   k_s2s_front     load window, NaN->0, FP64 demean/detrend sums, Hann
+//                   taper, prefilter (R2C, x dt, sanitize, x |H|^2, C2R,
+//                   x 1/(N dt)), then one-bit or the smoothed |x| weight
+//   k_s2s_mfband    (RUN-ABS-MF) per band: R2C, x |H_band|^2, C2R, weight
+//   k_s2s_mfsum     (RUN-ABS-MF) sum of the normalised bands
+//   k_s2s_whiten_a  [RAM divide] R2C(seg), x dt, sanitize, smoothed |X|
+//   k_s2s_whiten_b  divide by the station weight, band taper, sanitize,
+//                   C2R, then either the output transform or the time row
+//   k_s2s_output    [RAM divide] zero-pad, R2C(output_nfft), x dt,
+//                   sanitize, optional phase-only
+// Boxcar smoothing keeps the reference's window and divisor; the running
+// sums are FP32 with Kahan compensation (FP64 is kept for the detrend sums).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.cuh"
+#include "fft.cuh"
+#include "fft_launch.cuh"
+
+namespace fxc {
+
+constexpr int kS2sT = 1024;
+constexpr float kMaxVal = 20.0f;  // MAXVAL, native/sac2spec/include/config.h:13
+constexpr double kMinValD = 1e-30;  // MINVAL as a double literal (div2DKernel compares this)
+constexpr float kMinValF = 1e-30f;  // MINVAL passed as a float (clampmin2DKernel)
+
+struct S2sDev {
+  float delta;
+  int seg, shift, filter_nfft, out_nfft, nspec;
+  int taper;
+  int f_idx1, f_idx2, f_idx3, f_idx4;
+  int phase_only;
+  int num_ch;
+  int nrows;  // rows per step
+};
+
+// ---------------------------------------------------------------------------
+// block helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double block_sum_f64(double v, double* sred) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sred[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = (l < (int)(blockDim.x >> 5)) ? sred[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (l == 0) sred[0] = t;
+  }
+  __syncthreads();
+  t = sred[0];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ bool finite2(float2 v) { return isfinite(v.x) && isfinite(v.y); }
+__device__ __forceinline__ float2 sanitize2(float2 v) {
+  return finite2(v) ? v : make_float2(0.f, 0.f);
+}
+
+// Centred boxcar of width win over src[0, n) (reference smoothRowsRollingKernel:
+// window [c - win/2, c - win/2 + win - 1] clipped to the row, divided by win).
+// Each thread owns a contiguous run of outputs and slides a Kahan-compensated
+// FP32 sum across it. abs_src takes |src|.
+template <bool ABS, typename Store>
+__device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, Store store) {
+  const int per = (n + kS2sT - 1) / kS2sT;
+  const int c0 = threadIdx.x * per;
+  if (c0 >= n) return;
+  const int c1 = min(n, c0 + per);
+  const double inv = 1.0 / (double)win;
+  const int half = win / 2;
+  float s = 0.f, comp = 0.f;
+  auto kadd = [&](float v) {
+    const float y = v - comp;
+    const float t = s + y;
+    comp = (t - s) - y;
+    s = t;
+  };
+  int lo = max(0, c0 - half), hi = min(n - 1, c0 - half + win - 1);
+  for (int j = lo; j <= hi; ++j) kadd(ABS ? fabsf(src[j]) : src[j]);
+  for (int c = c0; c < c1; ++c) {
+    store(c, (float)((double)s * inv));
+    const int out = c - half;      // leaves the window
+    const int in = c - half + win;  // enters the window
+    if (out >= 0 && out < n) kadd(-(ABS ? fabsf(src[out]) : src[out]));
+    if (in >= 0 && in < n) kadd(ABS ? fabsf(src[in]) : src[in]);
+  }
+}
+
+// RAM divide of one sample (runabsNormalizeSharedWeight): the station weight
+// is the float sum of the component weights, clamped to MINVAL; x / w, NaN
+// -> 0, clip to +-MAXVAL.
+__device__ __forceinline__ float ram_divide(float x, const float* __restrict__ w, int64_t row0,
+                                            int64_t pitch, int num_ch, int i) {
+  float s = 0.f;
+  for (int c = 0; c < num_ch; ++c) s += w[(row0 + c) * pitch + i];
+  if (!isfinite(s) || s < kMinValF) s = kMinValF;
+  float y = ((double)s < kMinValD) ? 0.f : x / s;
+  if (!isfinite(y)) y = 0.f;
+  return fminf(fmaxf(y, -kMaxVal), kMaxVal);
+}
+
+// Pointwise pass of a real round trip: Z is the DIF output of the length-M
+// complex FFT of a real row of length 2M. For every bin pair (k, M-k) the
+// thread forms the real-spectrum bins X[k], X[M-k] (X[M] for k = 0), maps
+// them through f(k, X) and writes back the pre-processed inverse input Z'
+// at the same digit-reversed points, ready for fft_dit(inverse).
+template <typename F>
+__device__ __forceinline__ void real_roundtrip_pointwise(float2* buf, const FftPlan& p,
+                                                         const float2* __restrict__ twn, F f) {
+  const int M = p.n;
+  for (int k = threadIdx.x; k <= M / 2; k += kS2sT) {
+    const int k2 = M - k;  // == M for k == 0
+    const int pk = __ldg(p.perm + k);
+    const int pk2 = (k == 0) ? pk : __ldg(p.perm + k2);
+    const float2 zk = buf[pk];
+    const float2 zk2 = buf[pk2];
+    // forward post-processing (r2c_post with Z[M] == Z[0])
+    auto post = [&](float2 za, float2 zb, int kk) {
+      const float2 zc = conjf2(zb);
+      const float2 xe = make_float2(0.5f * (za.x + zc.x), 0.5f * (za.y + zc.y));
+      const float2 d = make_float2(0.5f * (za.x - zc.x), 0.5f * (za.y - zc.y));
+      const float2 w = (kk == M) ? make_float2(-1.f, 0.f) : __ldg(twn + kk);
+      return cadd(xe, cmul(w, mul_mi(d)));
+    };
+    float2 Xk = post(zk, zk2, k);
+    float2 Xk2 = (k == 0) ? post(zk, zk, M) : post(zk2, zk, k2);
+    Xk = f(k, Xk);
+    Xk2 = f(k2, Xk2);
+    if (k == 0) {
+      // Z'[0] from Y[0], Y[M] (imaginary parts of DC / Nyquist ignored)
+      buf[pk] = c2r_pre_vals(make_float2(Xk.x, 0.f), make_float2(Xk2.x, 0.f), 0, twn);
+    } else if (k == k2) {
+      buf[pk] = c2r_pre_vals(Xk, Xk, k, twn);
+    } else {
+      buf[pk] = c2r_pre_vals(Xk, Xk2, k, twn);
+      buf[pk2] = c2r_pre_vals(Xk2, Xk, k2, twn);
+    }
+  }
+}
+
+// InvNormalize2DKernel weight: 1 / (width * dt) with width*dt in float.
+__host__ __device__ inline double inv_norm(int n, float dt) { return 1.0 / (double)((float)n * dt); }
+
+// ---------------------------------------------------------------------------
+// k_s2s_front: window load, preprocess, prefilter, one-bit / RAM weight
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kS2sT, 1)
+    k_s2s_front(const float* __restrict__ series, int64_t series_pitch, int64_t series_len,
+                const int* __restrict__ steps, S2sDev d, FftPlan pf, const float2* __restrict__ twf,
+                const float* __restrict__ resp, int mode, int raw_win, float* __restrict__ xout,
+                float* __restrict__ wout) {
+  // mode: 0 = write x only, 1 = one-bit, 2 = x and smoothed |x| weight
+  extern __shared__ float2 sbuf[];
+  __shared__ double sred[32];
+  const int Mf = pf.n;
+  float2* stw = sbuf + Mf;
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int r = blockIdx.x;
+  const int sidx = r / d.nrows, row = r % d.nrows;
+  const int64_t start = (int64_t)steps[sidx] * d.shift;
+  const float* src = series + (int64_t)row * series_pitch + start;
+  const int seg = d.seg;
+  fft_twiddles_to_smem<kS2sT>(pf, stw);
+  // load + NaN/Inf -> 0 (isnan2DKernel); samples past the series are zero
+  double s1 = 0.0;
+  for (int i = threadIdx.x; i < 2 * Mf; i += kS2sT) {
+    float v = 0.f;
+    if (i < seg && start + i < series_len) {
+      v = src[i];
+      if (!isfinite(v)) v = 0.f;
+    }
+    xs[i] = v;
+    if (i < seg) s1 += (double)v;
+  }
+  // demean (rdc2DKernel): x -= sum/width in double
+  const double mean = block_sum_f64(s1, sred) / (double)seg;
+  double s2 = 0.0, si = 0.0;
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    const float v = (float)((double)xs[i] - mean);
+    xs[i] = v;
+    s2 += (double)v;
+    si += (double)v * (double)i;
+  }
+  // detrend (rtr2DKernel): closed-form least squares in double
+  const double y2 = block_sum_f64(s2, sred);
+  const double y1 = block_sum_f64(si, sred);
+  const double a12 = 0.5 * seg * (seg - 1);
+  const double a11 = a12 * (2 * seg - 1) / 3.0;
+  const double a22 = seg;
+  const double det = a11 * a22 - a12 * a12;
+  const double ca = (a22 * y1 - a12 * y2) / det;
+  const double cb = (a11 * y2 - a12 * y1) / det;
+  const int tap = d.taper;
+  const double pi = 3.14159265358979323846;
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    float v = (float)((double)xs[i] - (ca * i + cb));
+    // timetaper2DKernel (float factor computed in double)
+    float fac = 1.0f;
+    if (i < tap)
+      fac = (float)(0.5 * (1.0 - cos(pi * i / tap)));
+    else if (i >= seg - tap)
+      fac = (float)(0.5 * (1.0 - cos(pi * (seg - i) / tap)));
+    xs[i] = v * fac;
+  }
+  __syncthreads();
+  // prefilter: R2C(filter_nfft), x dt, sanitize, x |H|^2, C2R
+  fft_dif<kS2sT>(sbuf, pf, stw, false);
+  const float dt = d.delta;
+  real_roundtrip_pointwise(sbuf, pf, twf, [&](int k, float2 X) {
+    X = sanitize2(make_float2(X.x * dt, X.y * dt));
+    const float h = __ldg(resp + k);
+    return make_float2(X.x * h, X.y * h);
+  });
+  __syncthreads();
+  fft_dit<kS2sT>(sbuf, pf, stw, true);
+  const double inrm = inv_norm(2 * Mf, dt);
+  float* xo = xout + (int64_t)r * seg;
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    float v = (float)((double)xs[i] * inrm);
+    if (mode == 1) v = (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f);
+    xs[i] = v;
+    xo[i] = v;
+  }
+  if (mode == 2) {
+    __syncthreads();
+    float* wo = wout + (int64_t)r * seg;
+    boxcar_rows<true>(xs, seg, raw_win, [&](int c, float v) { wo[c] = v; });
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RUN-ABS-MF: per band filter + weight, then the sum of normalised bands
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kS2sT, 1)
+    k_s2s_mfband(const float* __restrict__ xin, S2sDev d, FftPlan pf, const float2* __restrict__ twf,
+                 const float* __restrict__ resp, int raw_win, float* __restrict__ xb,
+                 float* __restrict__ wb) {
+  extern __shared__ float2 sbuf[];
+  const int Mf = pf.n;
+  float2* stw = sbuf + Mf;
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int r = blockIdx.x;
+  const int seg = d.seg;
+  fft_twiddles_to_smem<kS2sT>(pf, stw);
+  const float* xi = xin + (int64_t)r * seg;
+  for (int i = threadIdx.x; i < 2 * Mf; i += kS2sT) xs[i] = (i < seg) ? xi[i] : 0.f;
+  __syncthreads();
+  fft_dif<kS2sT>(sbuf, pf, stw, false);
+  const float dt = d.delta;
+  real_roundtrip_pointwise(sbuf, pf, twf, [&](int k, float2 X) {
+    X = sanitize2(make_float2(X.x * dt, X.y * dt));
+    const float h = __ldg(resp + k);
+    return make_float2(X.x * h, X.y * h);
+  });
+  __syncthreads();
+  fft_dit<kS2sT>(sbuf, pf, stw, true);
+  const double inrm = inv_norm(2 * Mf, dt);
+  float* xo = xb + (int64_t)r * seg;
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    const float v = (float)((double)xs[i] * inrm);
+    xs[i] = v;
+    xo[i] = v;
+  }
+  __syncthreads();
+  float* wo = wb + (int64_t)r * seg;
+  boxcar_rows<true>(xs, seg, raw_win, [&](int c, float v) { wo[c] = v; });
+}
+
+__global__ void k_s2s_mfsum(const float* __restrict__ xb, const float* __restrict__ wb, int nbands,
+                            int64_t band_stride, S2sDev d, float* __restrict__ xout) {
+  const int r = blockIdx.y;
+  const int row = r % d.nrows;
+  const int64_t row0 = (int64_t)(r - row) + (row / d.num_ch) * d.num_ch;  // first row of the station
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.seg; i += gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int b = 0; b < nbands; ++b) {
+      const float* xbb = xb + b * band_stride;
+      const float* wbb = wb + b * band_stride;
+      acc += ram_divide(xbb[(int64_t)r * d.seg + i], wbb, row0, d.seg, d.num_ch, i);
+    }
+    xout[(int64_t)r * d.seg + i] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Whitening phase A: [RAM divide] R2C(seg), x dt, sanitize, smoothed |X|
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kS2sT, 1)
+    k_s2s_whiten_a(const float* __restrict__ xin, const float* __restrict__ win_w, S2sDev d,
+                   FftPlan ps, const float2* __restrict__ tws, int ww, float2* __restrict__ Xout,
+                   float* __restrict__ Aout, int64_t fpitch) {
+  extern __shared__ float2 sbuf[];
+  const int Ms = ps.n;
+  float2* stw = sbuf + Ms;
+  float* amp = reinterpret_cast<float*>(stw + fft_tw_smem_elems(ps));
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int r = blockIdx.x;
+  const int row = r % d.nrows;
+  const int64_t row0 = (int64_t)(r - row) + (row / d.num_ch) * d.num_ch;
+  const int seg = d.seg;
+  fft_twiddles_to_smem<kS2sT>(ps, stw);
+  const float* xi = xin + (int64_t)r * seg;
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    float v = xi[i];
+    if (win_w) v = ram_divide(v, win_w, row0, seg, d.num_ch, i);
+    xs[i] = v;
+  }
+  __syncthreads();
+  fft_dif<kS2sT>(sbuf, ps, stw, false);
+  const int fw = Ms + 1;
+  const float dt = d.delta;
+  float2* Xo = Xout + (int64_t)r * fpitch;
+  for (int k = threadIdx.x; k < fw; k += kS2sT) {
+    float2 X = r2c_post(sbuf, ps.perm, Ms, k, tws);
+    X = sanitize2(make_float2(X.x * dt, X.y * dt));
+    Xo[k] = X;
+    amp[k] = hypotf(X.x, X.y);
+  }
+  __syncthreads();
+  float* Ao = Aout + (int64_t)r * fpitch;
+  boxcar_rows<false>(amp, fw, ww, [&](int c, float v) { Ao[c] = v; });
+}
+
+// ---------------------------------------------------------------------------
+// Whitening phase B (+ output transform, or back to the time row)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float spec_taper_factor(int col, int width, const S2sDev& d) {
+  // specTaper2DKernel, np = 1 (factor in double)
+  const int i1 = d.f_idx1, i2 = d.f_idx2, i3 = d.f_idx3;
+  const int i4 = d.f_idx4 < width ? d.f_idx4 : width;
+  const double pi = 3.14159265358979323846;
+  if (col < i1) return 0.f;
+  if (col >= i1 && col < i2) {
+    const double dom = pi / (double)(i2 - i1);
+    return (float)((1.0 - cos(dom * (col - i1))) / 2.0);
+  }
+  if (col >= i3 && col < i4) {
+    const double dom = pi / (double)(i4 - i3);
+    return (float)((1.0 + cos(dom * (col - i3))) / 2.0);
+  }
+  if (col >= i4 && col < width) return 0.f;
+  return 1.f;
+}
+
+__device__ __forceinline__ void output_transform(float2* sbuf, float* xs, int nvalid,
+                                                 const FftPlan& po, const float2* twp,
+                                                 float2* stw, const S2sDev& d,
+                                                 float2* __restrict__ out) {
+  // zero-pad to output_nfft, R2C x dt, sanitize, optional phase-only
+  const int Mo = po.n;
+  for (int i = nvalid + threadIdx.x; i < 2 * Mo; i += kS2sT) xs[i] = 0.f;
+  __syncthreads();
+  fft_twiddles_to_smem<kS2sT>(po, stw);
+  __syncthreads();
+  fft_dif<kS2sT>(sbuf, po, stw, false);
+  const float dt = d.delta;
+  for (int k = threadIdx.x; k < d.nspec; k += kS2sT) {
+    float2 X = r2c_post(sbuf, po.perm, Mo, k, twp);
+    X = sanitize2(make_float2(X.x * dt, X.y * dt));
+    if (d.phase_only) {
+      // spectralOnebit2DKernel (hypotf, amp <= MINVAL -> 0), then sanitize
+      const float a = hypotf(X.x, X.y);
+      if (!isfinite(a) || a <= kMinValF)
+        X = make_float2(0.f, 0.f);
+      else {
+        const float ia = 1.0f / a;
+        X = sanitize2(make_float2(X.x * ia, X.y * ia));
+      }
+    }
+    out[k] = X;
+  }
+}
+
+__global__ void __launch_bounds__(kS2sT, 1)
+    k_s2s_whiten_b(const float2* __restrict__ Xin, const float* __restrict__ Ain, int64_t fpitch,
+                   S2sDev d, FftPlan ps, const float2* __restrict__ tws, FftPlan po,
+                   const float2* __restrict__ two, int to_time, int time_mode, int raw_win,
+                   float* __restrict__ xout, float* __restrict__ wout, float2* __restrict__ out,
+                   int64_t out_pitch) {
+  extern __shared__ float2 sbuf[];
+  const int Mbuf = max(ps.n, po.n);
+  float2* stw = sbuf + Mbuf;
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int r = blockIdx.x;
+  const int row = r % d.nrows;
+  const int64_t row0 = (int64_t)(r - row) + (row / d.num_ch) * d.num_ch;
+  const int Ms = ps.n;
+  const int fw = Ms + 1;
+  fft_twiddles_to_smem<kS2sT>(ps, stw);
+  const float2* Xr = Xin + (int64_t)r * fpitch;
+  // whitened, tapered, sanitised bins written as the C2R pre-processed input
+  // at the digit-reversed points of the length-Ms transform
+  auto wbin = [&](int k) -> float2 {
+    float s = 0.f;
+    for (int c = 0; c < d.num_ch; ++c) s += Ain[(row0 + c) * fpitch + k];
+    if (!isfinite(s) || s < kMinValF) s = kMinValF;  // clampmin2DKernel
+    float2 X = Xr[k];
+    if ((double)s < kMinValD) X = make_float2(0.f, 0.f);  // cdiv2DKernel
+    else X = make_float2(X.x / s, X.y / s);
+    const float f = spec_taper_factor(k, fw, d);
+    X = make_float2((float)((double)X.x * f), (float)((double)X.y * f));
+    return sanitize2(X);
+  };
+  for (int k = threadIdx.x; k < Ms; k += kS2sT) {
+    float2 a = wbin(k);
+    float2 b = wbin(Ms - k);
+    if (k == 0) {
+      a.y = 0.f;
+      b.y = 0.f;
+    }
+    sbuf[__ldg(ps.perm + k)] = c2r_pre_vals(a, b, k, tws);
+  }
+  __syncthreads();
+  fft_dit<kS2sT>(sbuf, ps, stw, true);
+  const int seg = d.seg;
+  const double inrm = inv_norm(seg, d.delta);
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    float v = (float)((double)xs[i] * inrm);
+    if (to_time && time_mode == 1) v = (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f);
+    xs[i] = v;
+  }
+  __syncthreads();
+  if (to_time) {
+    float* xo = xout + (int64_t)r * seg;
+    for (int i = threadIdx.x; i < seg; i += kS2sT) xo[i] = xs[i];
+    if (time_mode == 2) {
+      float* wo = wout + (int64_t)r * seg;
+      boxcar_rows<true>(xs, seg, raw_win, [&](int c, float v) { wo[c] = v; });
+    }
+    return;
+  }
+  output_transform(sbuf, xs, seg, po, two, stw, d, out + (int64_t)r * out_pitch);
+}
+
+__global__ void __launch_bounds__(kS2sT, 1)
+    k_s2s_output(const float* __restrict__ xin, const float* __restrict__ win_w, S2sDev d,
+                 FftPlan po, const float2* __restrict__ two, float2* __restrict__ out,
+                 int64_t out_pitch) {
+  extern __shared__ float2 sbuf[];
+  const int Mo = po.n;
+  float2* stw = sbuf + Mo;
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int r = blockIdx.x;
+  const int row = r % d.nrows;
+  const int64_t row0 = (int64_t)(r - row) + (row / d.num_ch) * d.num_ch;
+  const int seg = d.seg;
+  const float* xi = xin + (int64_t)r * seg;
+  for (int i = threadIdx.x; i < seg; i += kS2sT) {
+    float v = xi[i];
+    if (win_w) v = ram_divide(v, win_w, row0, seg, d.num_ch, i);
+    xs[i] = v;
+  }
+  output_transform(sbuf, xs, seg, po, two, stw, d, out + (int64_t)r * out_pitch);
+}
+
+// ---------------------------------------------------------------------------
+// host
+// ---------------------------------------------------------------------------
+
+static int make_real_plan(int n, FftPlan* p, const float2** tw) {
+  FXC_CHECK_ARG(n % 2 == 0 && n / 2 <= kFftLargeNmax, "real transform length %d not supported "
+                "(must be even and at most %d)", n, 2 * kFftLargeNmax);
+  FXC_TRY(fft_twiddles(n, tw));
+  return fft_make_plan(n / 2, *tw, 2, p);
+}
+
+}  // namespace fxc
+
+using namespace fxc;
+
+static int64_t llround_d(double x) { return (int64_t)llround(x); }
+
+static bool smooth2357(int v) {
+  if (v < 1) return false;
+  const int ps[4] = {2, 3, 5, 7};
+  for (int p : ps)
+    while (v > 1 && v % p == 0) v /= p;
+  return v == 1;
+}
+static int next_smooth(int n) {
+  if (n < 1) n = 1;
+  while (!smooth2357(n)) ++n;
+  return n;
+}
+static int next_even_smooth(int n) {
+  int l = next_smooth(n);
+  while (l % 2 != 0) l = next_smooth(l + 1);
+  return l;
+}
+static int prev_smooth(int maxlen) {
+  if (maxlen <= 1) return 0;
+  for (int l = maxlen - 1; l > 0; --l)
+    if (smooth2357(l)) return l;
+  return 0;
+}
+
+// estimateSinglePassImpulseLength (native/sac2spec/core/filter_response.c:11-72)
+static int impulse_len(const double* b, const double* a, int max_samples) {
+  const double a0 = a[0];
+  if (fabs(a0) < 1e-30) return max_samples;
+  std::vector<double> resp((size_t)max_samples);
+  double xh[5] = {0}, yh[5] = {0}, total = 0.0;
+  for (int n = 0; n < max_samples; ++n) {
+    for (int j = 4; j > 0; --j) {
+      xh[j] = xh[j - 1];
+      yh[j] = yh[j - 1];
+    }
+    xh[0] = (n == 0) ? 1.0 : 0.0;
+    double y = 0.0;
+    for (int j = 0; j < 5; ++j) y += b[j] * xh[j];
+    for (int j = 1; j < 5; ++j) y -= a[j] * yh[j];
+    y /= a0;
+    yh[0] = y;
+    resp[n] = y;
+    total += y * y;
+  }
+  if (total <= 0.0) return 1;
+  double tail = 0.0;
+  for (int n = max_samples - 1; n >= 0; --n) {
+    tail += resp[n] * resp[n];
+    if (tail > total * 1.0e-6) return n + 1;
+  }
+  return 1;
+}
+
+extern "C" {
+
+int fxc_s2s_plan_init(float sac_len, float win_len, float shift_len, float xcorr_lag, float delta,
+                      const double* h_b, const double* h_a, const float* h_freq_low,
+                      const float* h_freq_high, int32_t nfilters, int32_t whiten, int32_t normalize,
+                      int32_t phase_only, fxc_s2s_plan* out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "out is null");
+  FXC_CHECK_ARG(delta > 0.0f && sac_len > 0.0f && win_len > 0.0f, "invalid lengths");
+  FXC_CHECK_ARG(nfilters >= 1 && h_b && h_a && h_freq_low && h_freq_high, "need >= 1 filter");
+  FXC_CHECK_ARG(nfilters <= FXC_S2S_MAX_BANDS, "at most %d filters", FXC_S2S_MAX_BANDS);
+  FXC_CHECK_ARG(whiten >= 0 && whiten <= 3 && normalize >= 0 && normalize <= 3,
+                "whiten %d / normalize %d out of range", whiten, normalize);
+  fxc_s2s_plan p;
+  memset(&p, 0, sizeof(p));
+  p.delta = delta;
+  const double ts = (double)sac_len / (double)delta;
+  FXC_CHECK_ARG(std::isfinite(ts) && ts >= 1.0 && ts <= 2147483647.0, "invalid sac_len");
+  p.npts = (int32_t)llround_d(ts);
+  // segment_length_from_seconds (native/sac2spec/fft_length.c:90-108)
+  int req = 0;
+  {
+    const double s = (double)win_len / (double)delta;
+    req = (!std::isfinite(s) || s > 2147483647.0) ? 2147483647 : (int)llround_d(s);
+  }
+  int seg = next_smooth(req);
+  if (seg > p.npts) seg = prev_smooth(p.npts);
+  FXC_CHECK_ARG(seg > 0, "no 2-3-5-7-smooth segment length below %d", p.npts);
+  p.segment_pts = seg;
+  int shift = (int)llround_d((double)shift_len / (double)delta);
+  if (shift < 1) shift = seg;
+  p.shift_pts = shift;
+  p.nstep = (seg <= p.npts) ? std::max((p.npts - seg) / shift + 1, 1) : 1;
+  const int max_out = seg * 2;
+  int keep = (int)llround_d((double)xcorr_lag / (double)delta);
+  if (keep > seg) keep = seg;
+  p.output_nfft = std::min(next_even_smooth(seg + keep), max_out);
+  p.nspec = p.output_nfft / 2 + 1;
+  const float seg_df = 1.0f / ((float)seg * delta);
+  p.freq_low = h_freq_low[0];
+  p.freq_high = h_freq_high[0];
+  FXC_CHECK_ARG(p.freq_low > 0.0f && p.freq_high > p.freq_low, "invalid broad band");
+  p.f_idx1 = (int32_t)(p.freq_low * 0.667f / seg_df);
+  p.f_idx2 = (int32_t)(p.freq_low / seg_df);
+  p.f_idx3 = (int32_t)(p.freq_high / seg_df);
+  p.f_idx4 = (int32_t)(p.freq_high * 1.333f / seg_df);
+  int maxi = 1;
+  for (int i = 0; i < nfilters; ++i) maxi = std::max(maxi, impulse_len(h_b + 5 * i, h_a + 5 * i, seg));
+  int pad = std::min(std::max(2 * maxi, 1), seg);
+  p.filter_padding = pad;
+  p.filter_nfft = std::min(next_even_smooth(seg + pad), max_out);
+  p.taper_pts = (int32_t)(2.0f * (1.0f / p.freq_low) / delta);
+  {
+    const float fl = p.freq_low * 0.667f;
+    int w = 2 * (int)(1.0 / (double)(fl * delta)) + 1;
+    p.runabs_win = w < 1 ? 1 : w;
+  }
+  {
+    int w = (int)(0.02 * (double)seg * (double)delta);
+    p.whiten_win = w < 1 ? 1 : w;
+  }
+  p.whiten = whiten;
+  p.normalize = normalize;
+  p.phase_only = phase_only;
+  p.nfilters = nfilters;
+  for (int i = 0; i < nfilters; ++i) p.band_freq_low[i] = h_freq_low[i];
+  *out = p;
+  return FXC_OK;
+}
+
+int fxc_s2s_filter_response(const fxc_s2s_plan* plan, const double* h_b, const double* h_a,
+                            int32_t nfilters, float* h_out) {
+  clear_error();
+  FXC_CHECK_ARG(plan && h_b && h_a && h_out && nfilters >= 1, "null argument");
+  const int nfft = plan->filter_nfft;
+  const int half = nfft / 2;
+  const double pi = 3.14159265358979323846;
+  for (int f = 0; f < nfilters; ++f) {
+    const double* b = h_b + 5 * f;
+    const double* a = h_a + 5 * f;
+    float* o = h_out + (size_t)f * (half + 1);
+    // calFilterPowerResp (native/sac2spec/core/filter_response.c:186-233)
+    for (int i = 0; i < half + 1; ++i) {
+      const double nf = (double)i / (double)half;
+      double Bx = 0, By = 0, Ax = 0, Ay = 0;
+      for (int j = 0; j < 5; ++j) {
+        const double ang = -1.0 * pi * nf * (double)j;
+        const double c = cos(ang), s = sin(ang);
+        Bx += b[j] * c;
+        By += b[j] * s;
+        Ax += a[j] * c;
+        Ay += a[j] * s;
+      }
+      const double num = Bx * Bx + By * By, den = Ax * Ax + Ay * Ay;
+      double rp = (den <= 2.2250738585072014e-308) ? 0.0 : (num / den);
+      if (!std::isfinite(rp)) rp = 0.0;
+      else if (rp > 3.402823466e38) rp = 3.402823466e38;
+      o[i] = (float)rp;
+    }
+  }
+  return FXC_OK;
+}
+
+int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, int64_t series_pitch,
+                int64_t series_len, int32_t nrows, int32_t num_ch, const int32_t* h_steps,
+                int32_t nsteps, const float* d_responses, float* d_out, int64_t out_pitch) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(plan && d_series && h_steps && d_responses && d_out, "null argument");
+  FXC_CHECK_ARG(nrows > 0 && num_ch > 0 && nrows % num_ch == 0, "nrows %d must be a multiple of "
+                "num_ch %d", nrows, num_ch);
+  FXC_CHECK_ARG(nsteps > 0, "no steps");
+  FXC_CHECK_ARG(out_pitch >= plan->nspec, "out_pitch < nspec");
+  const int seg = plan->segment_pts;
+  const bool wh_before = plan->whiten == 1 || plan->whiten == 3;
+  const bool wh_after = plan->whiten == 2 || plan->whiten == 3;
+  if (wh_before || wh_after)
+    FXC_CHECK_ARG(seg % 2 == 0 && seg / 2 <= kFftLargeNmax,
+                  "whitening needs an even segment length <= %d (got %d)", 2 * kFftLargeNmax, seg);
+  for (int i = 0; i < nsteps; ++i)
+    FXC_CHECK_ARG(h_steps[i] >= 0 && h_steps[i] < plan->nstep, "step %d out of range", h_steps[i]);
+  const int64_t nr = (int64_t)nsteps * nrows;
+  FXC_CHECK_ARG(nr <= 0x7fffffff, "too many rows");
+
+  FftPlan pf, ps, po;
+  const float2 *twf = nullptr, *tws = nullptr, *two = nullptr;
+  FXC_TRY(make_real_plan(plan->filter_nfft, &pf, &twf));
+  FXC_TRY(make_real_plan(plan->output_nfft, &po, &two));
+  if (wh_before || wh_after) FXC_TRY(make_real_plan(seg, &ps, &tws));
+
+  S2sDev d;
+  d.delta = plan->delta;
+  d.seg = seg;
+  d.shift = plan->shift_pts;
+  d.filter_nfft = plan->filter_nfft;
+  d.out_nfft = plan->output_nfft;
+  d.nspec = plan->nspec;
+  d.taper = plan->taper_pts;
+  d.f_idx1 = plan->f_idx1;
+  d.f_idx2 = plan->f_idx2;
+  d.f_idx3 = plan->f_idx3;
+  d.f_idx4 = plan->f_idx4;
+  d.phase_only = plan->phase_only;
+  d.num_ch = num_ch;
+  d.nrows = nrows;
+
+  const int nbands = plan->normalize == 1 ? plan->nfilters - 1 : 0;
+  const int64_t fpitch = (int64_t)(seg / 2 + 1 + 3) / 4 * 4;
+  const size_t xbytes = sizeof(float) * (size_t)nr * seg;
+  const size_t a256 = 256;
+  auto al = [&](size_t x) { return (x + a256 - 1) / a256 * a256; };
+  size_t off = 0;
+  const size_t o_steps = off;
+  off = al(off + sizeof(int) * nsteps);
+  const size_t o_x = off;
+  off = al(off + xbytes);
+  const size_t o_w = off;
+  off = al(off + xbytes);
+  const size_t o_X = off;
+  off = al(off + ((wh_before || wh_after) ? sizeof(float2) * (size_t)nr * fpitch : 0));
+  const size_t o_A = off;
+  off = al(off + ((wh_before || wh_after) ? sizeof(float) * (size_t)nr * fpitch : 0));
+  const size_t o_xb = off;
+  off = al(off + (size_t)nbands * xbytes);
+  const size_t o_wb = off;
+  off = al(off + (size_t)nbands * xbytes);
+  FXC_TRY(ctx->scratch4.reserve(off));
+  char* base = reinterpret_cast<char*>(ctx->scratch4.ptr);
+  int* d_steps = reinterpret_cast<int*>(base + o_steps);
+  float* x = reinterpret_cast<float*>(base + o_x);
+  float* w = reinterpret_cast<float*>(base + o_w);
+  float2* X = reinterpret_cast<float2*>(base + o_X);
+  float* A = reinterpret_cast<float*>(base + o_A);
+  float* xb = reinterpret_cast<float*>(base + o_xb);
+  float* wb = reinterpret_cast<float*>(base + o_wb);
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_steps, h_steps, sizeof(int) * nsteps, cudaMemcpyHostToDevice,
+                               ctx->stream));
+  const size_t rpitch = (size_t)plan->filter_nfft / 2 + 1;
+  const float* resp0 = d_responses;
+
+  const size_t smf = sizeof(float2) * ((size_t)pf.n + fft_tw_smem_elems(pf));
+  const size_t smo = sizeof(float2) * ((size_t)po.n + fft_tw_smem_elems(po));
+  const int Mbuf = (wh_before || wh_after) ? std::max(ps.n, po.n) : po.n;
+  const size_t smb = sizeof(float2) * ((size_t)Mbuf + std::max(fft_tw_smem_elems(po),
+                                       (wh_before || wh_after) ? fft_tw_smem_elems(ps) : 0));
+  const size_t sma = (wh_before || wh_after)
+                         ? sizeof(float2) * ((size_t)ps.n + fft_tw_smem_elems(ps)) +
+                               sizeof(float) * (size_t)(ps.n + 1)
+                         : 0;
+  FXC_CHECK_ARG(smf <= 227 * 1024 && smo <= 227 * 1024 && smb <= 227 * 1024 && sma <= 227 * 1024,
+                "row transform too long for one CTA's shared memory");
+
+  // front: preprocess + prefilter (+ one-bit / RAM weight unless whitening comes first)
+  int mode = 0;
+  if (!wh_before) {
+    if (plan->normalize == 2) mode = 1;
+    if (plan->normalize == 3) mode = 2;
+  }
+  FXC_TRY(set_smem_limit(k_s2s_front, smf));
+  k_s2s_front<<<(unsigned)nr, kS2sT, smf, ctx->stream>>>(d_series, series_pitch, series_len,
+                                                         d_steps, d, pf, twf, resp0, mode,
+                                                         plan->runabs_win, x, w);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  const float* wgt = (mode == 2) ? w : nullptr;
+
+  if (wh_before) {
+    FXC_TRY(set_smem_limit(k_s2s_whiten_a, sma));
+    k_s2s_whiten_a<<<(unsigned)nr, kS2sT, sma, ctx->stream>>>(x, nullptr, d, ps, tws,
+                                                              plan->whiten_win, X, A, fpitch);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    int tmode = 0;
+    if (plan->normalize == 2) tmode = 1;
+    if (plan->normalize == 3) tmode = 2;
+    FXC_TRY(set_smem_limit(k_s2s_whiten_b, smb));
+    k_s2s_whiten_b<<<(unsigned)nr, kS2sT, smb, ctx->stream>>>(X, A, fpitch, d, ps, tws, po, two, 1,
+                                                              tmode, plan->runabs_win, x, w,
+                                                              nullptr, 0);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    wgt = (tmode == 2) ? w : nullptr;
+  }
+
+  if (plan->normalize == 1 && nbands > 0) {
+    // RUN-ABS-MF: filter each band from the broad-band row, weight, sum
+    FXC_TRY(set_smem_limit(k_s2s_mfband, smf));
+    for (int b = 0; b < nbands; ++b) {
+      const float fl = plan->band_freq_low[b + 1];
+      int win = 2 * (int)(1.0 / (double)(fl * plan->delta)) + 1;
+      if (win < 1) win = 1;
+      k_s2s_mfband<<<(unsigned)nr, kS2sT, smf, ctx->stream>>>(
+          x, d, pf, twf, resp0 + (size_t)(b + 1) * rpitch, win, xb + (size_t)b * nr * seg,
+          wb + (size_t)b * nr * seg);
+      count_launch();
+      FXC_LAUNCH_CHECK();
+    }
+    dim3 g((unsigned)((seg + 255) / 256), (unsigned)nr);
+    k_s2s_mfsum<<<g, 256, 0, ctx->stream>>>(xb, wb, nbands, (int64_t)nr * seg, d, x);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    wgt = nullptr;
+  }
+
+  float2* out = reinterpret_cast<float2*>(d_out);
+  if (wh_after) {
+    FXC_TRY(set_smem_limit(k_s2s_whiten_a, sma));
+    k_s2s_whiten_a<<<(unsigned)nr, kS2sT, sma, ctx->stream>>>(x, wgt, d, ps, tws, plan->whiten_win,
+                                                              X, A, fpitch);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    FXC_TRY(set_smem_limit(k_s2s_whiten_b, smb));
+    k_s2s_whiten_b<<<(unsigned)nr, kS2sT, smb, ctx->stream>>>(X, A, fpitch, d, ps, tws, po, two, 0,
+                                                              0, 0, nullptr, nullptr, out,
+                                                              out_pitch);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+  } else {
+    FXC_TRY(set_smem_limit(k_s2s_output, smo));
+    k_s2s_output<<<(unsigned)nr, kS2sT, smo, ctx->stream>>>(x, wgt, d, po, two, out, out_pitch);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+  }
+  return FXC_OK;
+}
+
+}  // extern "C"

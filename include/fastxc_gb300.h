@@ -87,6 +87,65 @@ int fxc_fft_c2r(fxc_ctx *ctx, const float *d_in, float *d_out, int n, int batch,
 /* 1 if the length is supported by the fused in-CTA transforms. */
 int fxc_fft_supported(int n, int real_transform);
 
+/* ---- sac2spec: windows -> normalised, whitened output spectra ----------- */
+
+#define FXC_S2S_MAX_BANDS 100 /* MAXBAND, native/sac2spec/include/config.h:8 */
+
+/* Whitening codes (-W a/...) and normalisation codes (-N) of the sac2spec
+ * command line (native/sac2spec/include/config.h:16-27). */
+#define FXC_WHITEN_NONE 0
+#define FXC_WHITEN_BEFORE 1
+#define FXC_WHITEN_AFTER 2
+#define FXC_WHITEN_BOTH 3
+#define FXC_NORM_NONE 0
+#define FXC_NORM_RUNABS_MF 1
+#define FXC_NORM_ONEBIT 2
+#define FXC_NORM_RUNABS 3
+
+typedef struct fxc_s2s_plan {
+  float delta;
+  int32_t npts;          /* llround(sac_len / delta) */
+  int32_t segment_pts;   /* segment_length_from_seconds (fft_length.c:90-108) */
+  int32_t shift_pts;
+  int32_t nstep;         /* (npts - seg) / shift + 1 */
+  int32_t output_nfft;   /* next even 2357-smooth >= seg + lag samples, <= 2 seg */
+  int32_t nspec;         /* output_nfft / 2 + 1 */
+  int32_t filter_padding;
+  int32_t filter_nfft;
+  float freq_low, freq_high; /* broad band (first filter) */
+  int32_t f_idx1, f_idx2, f_idx3, f_idx4; /* whitening band taper bins */
+  int32_t taper_pts;     /* (int)(2 / f_low / delta) */
+  int32_t runabs_win;    /* 2 * int(1 / (0.667 f_low * delta)) + 1 */
+  int32_t whiten_win;    /* int(0.02 * seg * delta) */
+  int32_t whiten, normalize, phase_only;
+  int32_t nfilters;
+  float band_freq_low[FXC_S2S_MAX_BANDS];
+} fxc_s2s_plan;
+
+/* Segment / FFT / band planning of sac2spec (native/sac2spec/cuda.main.cu:
+ * 203-296, fft_length.c:39-108, core/filter_response.c:74-104). Filters are
+ * the filter.txt entries (first = broad band): b and a are [nfilters][5]. */
+int fxc_s2s_plan_init(float sac_len, float win_len, float shift_len, float xcorr_lag, float delta,
+                      const double *h_b, const double *h_a, const float *h_freq_low,
+                      const float *h_freq_high, int32_t nfilters, int32_t whiten,
+                      int32_t normalize, int32_t phase_only, fxc_s2s_plan *out);
+/* Zero-phase power responses |B/A|^2 on filter_nfft/2+1 bins, float
+ * (calFilterPowerResp, core/filter_response.c:186-233); h_out is
+ * [nfilters][filter_nfft/2+1]. */
+int fxc_s2s_filter_response(const fxc_s2s_plan *plan, const double *h_b, const double *h_a,
+                            int32_t nfilters, float *h_out);
+/* ComputeWorkerBatch (native/sac2spec/worker/compute.cu:8-272) for nsteps
+ * windows (h_steps: window indices < nstep) of nrows channel series.
+ * d_series is [nrows][series_pitch] float with series_len valid samples
+ * (shorter series are zero-padded as read_sac_buffer does); rows are grouped
+ * by station, num_ch consecutive rows per station. d_responses is the
+ * device copy of fxc_s2s_filter_response's output. d_out receives
+ * [nsteps][nrows][out_pitch] complex spectra (nspec bins used). */
+int fxc_s2s_run(fxc_ctx *ctx, const fxc_s2s_plan *plan, const float *d_series,
+                int64_t series_pitch, int64_t series_len, int32_t nrows, int32_t num_ch,
+                const int32_t *h_steps, int32_t nsteps, const float *d_responses, float *d_out,
+                int64_t out_pitch);
+
 /* ---- xc_fast: correlation + within-window linear stack ------------------ */
 
 typedef struct fxc_xc_shape {
