@@ -175,3 +175,10 @@ _SIGNATURES.update({
     "fxc_s2s_filter_response": (_int, [C.POINTER(S2sPlan), _vp, _vp, _i32, _vp]),
     "fxc_s2s_run": (_int, [_vp, C.POINTER(S2sPlan), _vp, _i64, _i64, _i32, _i32, _vp, _i32, _vp, _vp, _i64]),
 })
+
+_SIGNATURES.update({
+    "fxc_linear_stack": (_int, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
+    "fxc_stack_prestack": (_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "fxc_pws_run": (_int, [_vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _f32, _vp]),
+    "fxc_tfpws_run": (_int, [_vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _f32, _i32, _f32, _f32, _f32, _f32, _vp]),
+})

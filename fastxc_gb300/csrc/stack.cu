@@ -1,0 +1,532 @@
+// Stacking stages: cross-timestamp linear stack, substack prestacking,
+// phase-weighted stack (ncf_pws) and S-transform time-frequency PWS
+// (ncf_tfpws).
+//
+// Reference behaviour reproduced here:
+//   _linear_stack_group        fastxc/operators/stacking/linear_stack.py:228-247
+//   prepare_sourcepack_host_item (PWS prestack = group means)
+//                              native/pws/io/sourcepack_io.cu:385-478
+//   TF-PWS prestack (group sums) native/tfpws/io/sourcepack_io.cu:440-490
+//   compute_pws_host_batch + hilbertTransformKernel, cudaNormalizeComplex,
+//   cudaWeightedMeanBatch, cudaMultiplyBatch
+//                              native/pws/worker/gpu.cu:87-282, kernels/cuda.pws.cu
+//   compute_tfpws_from_prestack + gaussianModulateSub, calculateWeightSub,
+//   applyWeight, sumOverTimeAxisKernel, blendBandLimitedSpectrum, extractReal
+//                              native/tfpws/core/tfpws_compute.cu:19-366,
+//                              kernels/cuda.stransform.cu
+//
+// GB300 design: every row transform (N = 2001 = 3*23*29 lags for +-100 s at
+// 10 Hz) stays in shared memory. PWS runs one CTA per pair that streams its
+// groups (forward FFT, analytic mask in the digit-reversed layout, inverse
+// DIT back to natural order, unit phasor, weighted sum) without writing any
+// group row back. TF-PWS runs one CTA per (pair, frequency): the group
+// voices of that frequency are produced and reduced into the weight in
+// shared memory; the Gaussian window is evaluated in FP64. The weight power
+// (1 in the reference) is a parameter.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "context.cuh"
+#include "fft.cuh"
+#include "fft_launch.cuh"
+
+namespace fxc {
+
+constexpr int kStT = 64;        // threads per row transform CTA
+constexpr int kStNmax = 8192;   // longest stacked trace (complex FFT in shared memory)
+
+// ---------------------------------------------------------------------------
+// linear stack and prestack
+// ---------------------------------------------------------------------------
+
+// out[p, t] = float(sum_k double(tr[off_p + k, t]) / count_p)
+__global__ void k_linear_stack(const float* __restrict__ traces, const int64_t* __restrict__ offs,
+                               const int32_t* __restrict__ counts, int n, float* __restrict__ out) {
+  const int p = blockIdx.y;
+  const int64_t off = offs[p];
+  const int cnt = counts[p];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int k = 0; k < cnt; ++k) acc += (double)traces[(off + k) * n + t];
+    out[(int64_t)p * n + t] = cnt > 0 ? (float)(acc / (double)cnt) : 0.f;
+  }
+}
+
+// Group rows of `substack` consecutive traces (B < 2 -> 1): mode 0 mean
+// (PWS), mode 1 sum (TF-PWS). weight[g] = count_g / count_p. linear: mode 0
+// sum_g mean_g * weight_g, mode 1 sum_g sum_g / count_p.
+__global__ void k_prestack(const float* __restrict__ traces, const int64_t* __restrict__ toffs,
+                           const int32_t* __restrict__ tcounts, const int64_t* __restrict__ goffs,
+                           int n, int substack, int mode, float* __restrict__ groups,
+                           float* __restrict__ weights, float* __restrict__ linear) {
+  const int p = blockIdx.y;
+  const int64_t toff = toffs[p];
+  const int cnt = tcounts[p];
+  const int64_t goff = goffs[p];
+  const int b = substack >= 2 ? substack : 1;
+  const int ng = (cnt + b - 1) / b;
+  const float inv_total = 1.0f / (float)cnt;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    float lin = 0.f;
+    for (int g = 0; g < ng; ++g) {
+      const int k0 = g * b, k1 = min(cnt, k0 + b);
+      float s = 0.f;
+      for (int k = k0; k < k1; ++k) s += traces[(toff + k) * n + t];
+      const int gc = k1 - k0;
+      float v, wgt;
+      if (mode == 0) {
+        // group mean, weight count/num_segments, linear += mean * weight
+        v = s * (1.0f / (float)gc);
+        wgt = (float)gc / (float)cnt;
+        lin += v * wgt;
+      } else {
+        // group sum, weight count * (1/num_segments), linear += sum / num_segments
+        v = s;
+        wgt = (float)gc * inv_total;
+        lin += s * inv_total;
+      }
+      groups[(goff + g) * n + t] = v;
+      if (t == 0) weights[goff + g] = wgt;
+    }
+    linear[(int64_t)p * n + t] = lin;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared pieces of the row transforms
+// ---------------------------------------------------------------------------
+
+// Analytic-signal mask of hilbertTransformKernel: bin 0 and bins >= (N+1)/2
+// -> 0, the others x 2. buf holds the DIF output (digit-reversed points).
+__device__ __forceinline__ void analytic_mask(float2* buf, const FftPlan& p) {
+  const int n = p.n;
+  const int half = (n + 1) / 2;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int pos = __ldg(p.perm + k);
+    float2 v = buf[pos];
+    if (k == 0 || k >= half)
+      v = make_float2(0.f, 0.f);
+    else
+      v = make_float2(v.x * 2.0f, v.y * 2.0f);
+    buf[pos] = v;
+  }
+}
+
+__device__ __forceinline__ float weight_pow(float mag2, float power) {
+  // |W|^power from |W|^2 (applyWeight: powf(rw*rw + iw*iw, 0.5*order))
+  return power == 1.0f ? sqrtf(mag2) : powf(mag2, 0.5f * power);
+}
+
+// ---------------------------------------------------------------------------
+// PWS: one CTA per pair
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kStT)
+    k_pws(const float* __restrict__ groups, const float* __restrict__ weights,
+          const int64_t* __restrict__ goffs, const int32_t* __restrict__ gcounts,
+          const float* __restrict__ linear, FftPlan p, float power, float* __restrict__ out) {
+  extern __shared__ float2 sm[];
+  const int n = p.n;
+  float2* buf = sm;
+  float2* acc = sm + n;
+  float2* stw = sm + 2 * n;
+  const int pair = blockIdx.x;
+  const int64_t goff = goffs[pair];
+  const int ng = gcounts[pair];
+  fft_twiddles_to_smem<kStT>(p, stw);
+  for (int t = threadIdx.x; t < n; t += kStT) acc[t] = make_float2(0.f, 0.f);
+  const float invn = 1.0f / (float)n;
+  for (int g = 0; g < ng; ++g) {
+    const float* x = groups + (goff + g) * n;
+    const float wg = weights[goff + g];
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
+    __syncthreads();
+    fft_dif<kStT>(buf, p, stw, false);  // R2C into an N-point row (odd N: full spectrum)
+    analytic_mask(buf, p);
+    __syncthreads();
+    fft_dit<kStT>(buf, p, stw, true);   // C2C inverse, unnormalised, natural order
+    for (int t = threadIdx.x; t < n; t += kStT) {
+      // cudaNormalizeComplex: z / nfft, modulus floored at 1e-7
+      const float2 z = buf[t];
+      const float re = z.x * invn, im = z.y * invn;
+      float mod = sqrtf(re * re + im * im);
+      mod = (mod > 1e-7f) ? mod : 1e-7f;
+      // cudaWeightedMeanBatch
+      acc[t].x += (re / mod) * wg;
+      acc[t].y += (im / mod) * wg;
+    }
+  }
+  __syncthreads();
+  const float* lin = linear + (int64_t)pair * n;
+  float* o = out + (int64_t)pair * n;
+  for (int t = threadIdx.x; t < n; t += kStT) {
+    const float2 a = acc[t];
+    o[t] = lin[t] * weight_pow(a.x * a.x + a.y * a.y, power);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TF-PWS
+// ---------------------------------------------------------------------------
+
+// Analytic spectrum (natural order) of every row: groups of all pairs, then
+// the linear stack of every pair.
+__global__ void __launch_bounds__(kStT)
+    k_analytic_spectrum(const float* __restrict__ rows, FftPlan p, float2* __restrict__ out) {
+  extern __shared__ float2 sm[];
+  const int n = p.n;
+  float2* buf = sm;
+  float2* stw = sm + n;
+  fft_twiddles_to_smem<kStT>(p, stw);
+  const float* x = rows + (int64_t)blockIdx.x * n;
+  for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
+  __syncthreads();
+  fft_dif<kStT>(buf, p, stw, false);
+  analytic_mask(buf, p);
+  __syncthreads();
+  float2* o = out + (int64_t)blockIdx.x * n;
+  for (int k = threadIdx.x; k < n; k += kStT) o[k] = buf[__ldg(p.perm + k)];
+}
+
+struct TfBand {
+  int limited;
+  float df, fmin, fmax, taper;
+};
+
+// gaussianModulateSub factor (FP64): f = 0 -> 1; c = 0 -> 0; c < (N+1)/2 ->
+// exp(-2 pi^2 c^2 scale / f^2); otherwise the mirror c' = N - c under the
+// same rules.
+__device__ __forceinline__ float gauss_factor(int c, int f, int n, double scale) {
+  if (f == 0) return 1.0f;
+  if (c == 0) return 0.0f;
+  const int half = (n + 1) / 2;
+  int cc = c;
+  if (c >= half) {
+    cc = n - c;
+    if (!(cc < half && cc != 0)) return 0.0f;
+  }
+  const double pi = 3.14159265358979323846;
+  return (float)exp(-2.0 * pi * pi * (double)cc * (double)cc * scale / ((double)f * (double)f));
+}
+
+// One CTA per (frequency f, pair): voices of every group and of the linear
+// stack at f, the time-frequency weight, the weighted stack voice summed
+// over time -> bin f of the output spectrum (band blend applied).
+__global__ void __launch_bounds__(kStT)
+    k_tfpws_freq(const float2* __restrict__ Xg, const float2* __restrict__ Xl,
+                 const float* __restrict__ weights, const int64_t* __restrict__ goffs,
+                 const int32_t* __restrict__ gcounts, FftPlan p, int f0, TfBand band, float power,
+                 float2* __restrict__ spec_out) {
+  extern __shared__ float2 sm[];
+  __shared__ float sred[kStT / 32];
+  __shared__ float sredi[kStT / 32];
+  const int n = p.n;
+  float2* buf = sm;
+  float2* W = sm + n;
+  float* gs = reinterpret_cast<float*>(sm + 2 * n);
+  float2* stw = reinterpret_cast<float2*>(gs + ((n + 1) & ~1));
+  const int f = f0 + blockIdx.x;
+  const int pair = blockIdx.y;
+  const int nfreq = n / 2 + 1;
+  if (f >= nfreq) return;
+  float alpha = 1.0f;
+  if (band.limited) {
+    const float freq = (float)f * band.df;
+    if (!(freq >= band.fmin && freq <= band.fmax)) return;  // bin keeps the linear spectrum
+    const float bw = band.fmax - band.fmin;
+    const float tp = fminf(band.taper, 0.5f * bw);
+    const float pi = 3.14159265358979323846f;
+    if (tp <= 0.0f) {
+      alpha = 1.0f;
+    } else if (freq < band.fmin + tp) {
+      alpha = 0.5f - 0.5f * cosf(pi * ((freq - band.fmin) / tp));
+    } else if (freq > band.fmax - tp) {
+      alpha = 0.5f - 0.5f * cosf(pi * ((band.fmax - freq) / tp));
+    }
+  }
+  fft_twiddles_to_smem<kStT>(p, stw);
+  for (int c = threadIdx.x; c < n; c += kStT) {
+    gs[c] = gauss_factor(c, f, n, 0.1);
+    W[c] = make_float2(0.f, 0.f);
+  }
+  const int64_t goff = goffs[pair];
+  const int ng = gcounts[pair];
+  const float nf = (float)n;
+  for (int g = 0; g < ng; ++g) {
+    const float2* X = Xg + (goff + g) * n;
+    const float wg = weights[goff + g];
+    __syncthreads();
+    for (int c = threadIdx.x; c < n; c += kStT) {
+      int k = f + c;
+      if (k >= n) k -= n;
+      const float2 v = X[k];
+      const float gf = gs[c];
+      buf[__ldg(p.perm + c)] = make_float2(v.x * gf, v.y * gf);
+    }
+    __syncthreads();
+    fft_dit<kStT>(buf, p, stw, true);  // voice of group g (unnormalised C2C inverse)
+    for (int t = threadIdx.x; t < n; t += kStT) {
+      // calculateWeightSub
+      const float x = buf[t].x, y = buf[t].y;
+      float fa = sqrtf(x * x + y * y);
+      if (fa <= 1e-7f) fa = 1.0f;
+      W[t].x += wg * x / (fa * nf);
+      W[t].y += wg * y / (fa * nf);
+    }
+  }
+  __syncthreads();
+  const float2* XL = Xl + (int64_t)pair * n;
+  for (int c = threadIdx.x; c < n; c += kStT) {
+    int k = f + c;
+    if (k >= n) k -= n;
+    const float2 v = XL[k];
+    const float gf = gs[c];
+    buf[__ldg(p.perm + c)] = make_float2(v.x * gf, v.y * gf);
+  }
+  __syncthreads();
+  fft_dit<kStT>(buf, p, stw, true);  // stack voice
+  // applyWeight + sumOverTimeAxisKernel
+  float sr = 0.f, si = 0.f;
+  for (int t = threadIdx.x; t < n; t += kStT) {
+    const float mag = weight_pow(W[t].x * W[t].x + W[t].y * W[t].y, power);
+    sr += buf[t].x * mag;
+    si += buf[t].y * mag;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sred[threadIdx.x >> 5] = sr;
+    sredi[threadIdx.x >> 5] = si;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float tr = 0.f, ti = 0.f;
+    for (int w = 0; w < kStT / 32; ++w) {
+      tr += sred[w];
+      ti += sredi[w];
+    }
+    float2 val = make_float2(tr, ti);
+    if (band.limited) {
+      // blendBandLimitedSpectrum
+      const float2 lin = XL[f];
+      val = make_float2(lin.x * (1.0f - alpha) + val.x * alpha, lin.y * (1.0f - alpha) + val.y * alpha);
+    }
+    spec_out[(int64_t)pair * n + f] = val;
+  }
+}
+
+// Final C2C inverse of the output spectrum, real part / N (extractReal).
+__global__ void __launch_bounds__(kStT)
+    k_tfpws_final(const float2* __restrict__ spec, FftPlan p, float* __restrict__ out) {
+  extern __shared__ float2 sm[];
+  const int n = p.n;
+  float2* buf = sm;
+  float2* stw = sm + n;
+  fft_twiddles_to_smem<kStT>(p, stw);
+  const float2* S = spec + (int64_t)blockIdx.x * n;
+  for (int k = threadIdx.x; k < n; k += kStT) buf[__ldg(p.perm + k)] = S[k];
+  __syncthreads();
+  fft_dit<kStT>(buf, p, stw, true);
+  float* o = out + (int64_t)blockIdx.x * n;
+  for (int t = threadIdx.x; t < n; t += kStT) o[t] = buf[t].x / (float)n;
+}
+
+// output spectrum initialisation: band-limited -> the linear analytic
+// spectrum everywhere (bins outside the band keep it), else zeros.
+__global__ void k_tfpws_init(const float2* __restrict__ Xl, int64_t total, int limited,
+                             float2* __restrict__ spec) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x)
+    spec[i] = limited ? Xl[i] : make_float2(0.f, 0.f);
+}
+
+static int stack_plan(int n, FftPlan* p) {
+  FXC_CHECK_ARG(n >= 2 && n <= kStNmax, "trace length %d outside [2, %d]", n, kStNmax);
+  const float2* tw = nullptr;
+  FXC_TRY(fft_twiddles(n, &tw));
+  return fft_make_plan(n, tw, 1, p);
+}
+
+struct PairGroups {
+  std::vector<int64_t> offs;
+  std::vector<int32_t> counts;
+};
+
+}  // namespace fxc
+
+using namespace fxc;
+
+extern "C" {
+
+int fxc_linear_stack(fxc_ctx* ctx, const float* d_traces, const int64_t* h_offsets,
+                     const int32_t* h_counts, int32_t npairs, int32_t nsamples, float* d_out) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0 && nsamples > 0, "invalid shape");
+  if (npairs == 0) return FXC_OK;
+  FXC_CHECK_ARG(d_traces && h_offsets && h_counts && d_out, "null pointer");
+  FXC_CHECK_ARG(npairs <= 65535, "at most 65535 pairs per call");
+  const size_t ob = sizeof(int64_t) * npairs, cb = sizeof(int32_t) * npairs;
+  FXC_TRY(ctx->scratch2.reserve(ob + cb + 256));
+  int64_t* d_off = reinterpret_cast<int64_t*>(ctx->scratch2.ptr);
+  int32_t* d_cnt = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(ctx->scratch2.ptr) + ((ob + 255) & ~size_t(255)));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_off, h_offsets, ob, cudaMemcpyHostToDevice, ctx->stream));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_cnt, h_counts, cb, cudaMemcpyHostToDevice, ctx->stream));
+  dim3 g((unsigned)((nsamples + 255) / 256), (unsigned)npairs);
+  k_linear_stack<<<g, 256, 0, ctx->stream>>>(d_traces, d_off, d_cnt, nsamples, d_out);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+int fxc_stack_prestack(fxc_ctx* ctx, const float* d_traces, const int64_t* h_trace_offsets,
+                       const int32_t* h_trace_counts, int32_t npairs, int32_t nsamples,
+                       int32_t substack, int32_t mode, float* d_groups, float* d_weights,
+                       float* d_linear, int64_t* h_group_offsets, int32_t* h_group_counts) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0 && nsamples > 0 && (mode == 0 || mode == 1), "invalid arguments");
+  if (npairs == 0) return FXC_OK;
+  FXC_CHECK_ARG(npairs <= 65535, "at most 65535 pairs per call");
+  FXC_CHECK_ARG(d_traces && h_trace_offsets && h_trace_counts && d_groups && d_weights && d_linear &&
+                    h_group_offsets && h_group_counts, "null pointer");
+  const int b = substack >= 2 ? substack : 1;
+  int64_t goff = 0;
+  for (int p = 0; p < npairs; ++p) {
+    FXC_CHECK_ARG(h_trace_counts[p] >= 1, "pair %d has no traces", p);
+    h_group_offsets[p] = goff;
+    h_group_counts[p] = (h_trace_counts[p] + b - 1) / b;
+    goff += h_group_counts[p];
+  }
+  const size_t n8 = sizeof(int64_t) * npairs, n4 = sizeof(int32_t) * npairs;
+  const size_t o2 = (n8 + 255) & ~size_t(255), o3 = o2 + ((n4 + 255) & ~size_t(255));
+  FXC_TRY(ctx->scratch2.reserve(o3 + n8 + 256));
+  char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
+  int64_t* d_toff = reinterpret_cast<int64_t*>(base);
+  int32_t* d_tcnt = reinterpret_cast<int32_t*>(base + o2);
+  int64_t* d_goff = reinterpret_cast<int64_t*>(base + o3);
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_toff, h_trace_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_tcnt, h_trace_counts, n4, cudaMemcpyHostToDevice, ctx->stream));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_goff, h_group_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
+  dim3 g((unsigned)((nsamples + 255) / 256), (unsigned)npairs);
+  k_prestack<<<g, 256, 0, ctx->stream>>>(d_traces, d_toff, d_tcnt, d_goff, nsamples, substack, mode,
+                                         d_groups, d_weights, d_linear);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  // the host arrays outlive the call; keep the copies ordered before return
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
+}
+
+int fxc_pws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
+                const int64_t* h_group_offsets, const int32_t* h_group_counts, int32_t npairs,
+                const float* d_linear, int32_t nsamples, float power, float* d_out) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0, "invalid npairs");
+  if (npairs == 0) return FXC_OK;
+  FXC_CHECK_ARG(d_groups && d_weights && h_group_offsets && h_group_counts && d_linear && d_out,
+                "null pointer");
+  FftPlan p;
+  FXC_TRY(stack_plan(nsamples, &p));
+  const size_t n8 = sizeof(int64_t) * npairs, n4 = sizeof(int32_t) * npairs;
+  const size_t o2 = (n8 + 255) & ~size_t(255);
+  FXC_TRY(ctx->scratch2.reserve(o2 + n4 + 256));
+  char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
+  int64_t* d_goff = reinterpret_cast<int64_t*>(base);
+  int32_t* d_gcnt = reinterpret_cast<int32_t*>(base + o2);
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_goff, h_group_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_gcnt, h_group_counts, n4, cudaMemcpyHostToDevice, ctx->stream));
+  const size_t smem = sizeof(float2) * (2 * (size_t)nsamples + fft_tw_smem_elems(p));
+  FXC_TRY(set_smem_limit(k_pws, smem));
+  k_pws<<<(unsigned)npairs, kStT, smem, ctx->stream>>>(d_groups, d_weights, d_goff, d_gcnt, d_linear,
+                                                        p, power, d_out);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
+}
+
+int fxc_tfpws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
+                  const int64_t* h_group_offsets, const int32_t* h_group_counts, int32_t npairs,
+                  const float* d_linear, int32_t nsamples, float delta, int32_t band_limited,
+                  float fmin, float fmax, float taper_hz, float power, float* d_out) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0, "invalid npairs");
+  if (npairs == 0) return FXC_OK;
+  FXC_CHECK_ARG(d_groups && d_weights && h_group_offsets && h_group_counts && d_linear && d_out,
+                "null pointer");
+  FXC_CHECK_ARG(npairs <= 65535, "at most 65535 pairs per call");
+  FftPlan p;
+  FXC_TRY(stack_plan(nsamples, &p));
+  const int n = nsamples;
+  int64_t total_groups = 0;
+  for (int i = 0; i < npairs; ++i) total_groups = std::max<int64_t>(total_groups, h_group_offsets[i] + h_group_counts[i]);
+  TfBand band{0, 0.f, 0.f, 0.f, 0.f};
+  if (band_limited) {
+    // compute_tfpws_from_prestack (tfpws_compute.cu:112-153)
+    FXC_CHECK_ARG(delta > 0.0f, "band limit needs delta > 0");
+    const double df_hz = 1.0 / ((double)n * (double)delta);
+    const double nyq = 0.5 / (double)delta;
+    FXC_CHECK_ARG((double)fmin < nyq, "band lower bound %g above Nyquist %g", fmin, nyq);
+    double fm = fmax;
+    if (fm > nyq) fm = nyq;
+    double tp = taper_hz;
+    if (tp < 0.0) tp = 0.05 * (fm - (double)fmin);
+    band = TfBand{1, (float)df_hz, fmin, (float)fm, (float)tp};
+  }
+  const size_t n8 = sizeof(int64_t) * npairs, n4 = sizeof(int32_t) * npairs;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t o_gcnt = al(n8);
+  const size_t o_xg = o_gcnt + al(n4);
+  const size_t o_xl = o_xg + al(sizeof(float2) * (size_t)total_groups * n);
+  const size_t o_sp = o_xl + al(sizeof(float2) * (size_t)npairs * n);
+  const size_t total = o_sp + al(sizeof(float2) * (size_t)npairs * n);
+  FXC_TRY(ctx->scratch4.reserve(total));
+  char* base = reinterpret_cast<char*>(ctx->scratch4.ptr);
+  int64_t* d_goff = reinterpret_cast<int64_t*>(base);
+  int32_t* d_gcnt = reinterpret_cast<int32_t*>(base + o_gcnt);
+  float2* Xg = reinterpret_cast<float2*>(base + o_xg);
+  float2* Xl = reinterpret_cast<float2*>(base + o_xl);
+  float2* spec = reinterpret_cast<float2*>(base + o_sp);
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_goff, h_group_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_gcnt, h_group_counts, n4, cudaMemcpyHostToDevice, ctx->stream));
+  const size_t sm1 = sizeof(float2) * ((size_t)n + fft_tw_smem_elems(p));
+  FXC_TRY(set_smem_limit(k_analytic_spectrum, sm1));
+  FXC_CHECK_ARG(total_groups <= 0x7fffffff, "too many groups");
+  if (total_groups > 0) {
+    k_analytic_spectrum<<<(unsigned)total_groups, kStT, sm1, ctx->stream>>>(d_groups, p, Xg);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+  }
+  k_analytic_spectrum<<<(unsigned)npairs, kStT, sm1, ctx->stream>>>(d_linear, p, Xl);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  k_tfpws_init<<<1024, 256, 0, ctx->stream>>>(Xl, (int64_t)npairs * n, band_limited, spec);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  const int nfreq = n / 2 + 1;
+  const size_t sm2 = sizeof(float2) * (2 * (size_t)n + fft_tw_smem_elems(p)) + sizeof(float) * (size_t)((n + 1) & ~1);
+  FXC_TRY(set_smem_limit(k_tfpws_freq, sm2));
+  for (int f0 = 0; f0 < nfreq; f0 += 65535) {
+    dim3 g((unsigned)std::min(65535, nfreq - f0), (unsigned)npairs);
+    k_tfpws_freq<<<g, kStT, sm2, ctx->stream>>>(Xg, Xl, d_weights, d_goff, d_gcnt, p, f0, band, power,
+                                                spec);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+  }
+  FXC_TRY(set_smem_limit(k_tfpws_final, sm1));
+  k_tfpws_final<<<(unsigned)npairs, kStT, sm1, ctx->stream>>>(spec, p, d_out);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
+}
+
+}  // extern "C"

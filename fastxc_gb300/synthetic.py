@@ -108,3 +108,27 @@ def spectra_device(torch, nwin: int, arr: StationArray, nspec: int, dt: float, s
         y = (n + 0.7 * gains * c * phase) * taper[None, :]
         out[w] = y * mask_d[w][:, None]
     return out, mask
+
+
+def ricker(t: np.ndarray, f0: float) -> np.ndarray:
+    a = (np.pi * f0 * t) ** 2
+    return (1 - 2 * a) * np.exp(-a)
+
+
+def ncf_traces(npairs: int, ntraces: int, nsamples: int = 2001, delta: float = 0.1, seed: int = 0,
+               snr=(0.05, 0.5)) -> np.ndarray:
+    """Stacking-configuration input: per pair `ntraces` NCF windows of
+    `nsamples` lags holding a Ricker arrival (seeded f0 in 0.1-0.5 Hz) at a
+    pair-specific lag plus Gaussian noise at an SNR drawn from `snr`.
+    Returns float32 [npairs][ntraces][nsamples]."""
+    rng = np.random.default_rng(seed)
+    t = (np.arange(nsamples) - nsamples // 2) * delta
+    out = np.empty((npairs, ntraces, nsamples), np.float32)
+    for p in range(npairs):
+        f0 = rng.uniform(0.1, 0.5)
+        lag = rng.uniform(-0.6, 0.6) * t[-1]
+        sig = ricker(t - lag, f0) + 0.6 * ricker(t + lag, f0)
+        s = rng.uniform(*snr, size=ntraces)
+        noise = rng.standard_normal((ntraces, nsamples))
+        out[p] = (s[:, None] * sig[None, :] + noise).astype(np.float32)
+    return out

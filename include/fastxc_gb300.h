@@ -216,6 +216,47 @@ int fxc_xc_run_host(fxc_ctx *ctx, const fxc_pairplan *plan, const float *h_spec,
                     int32_t nchan, int64_t spec_pitch, const uint8_t *h_mask, float scale,
                     const fxc_xc_shape *shape, float *h_ncf, int method);
 
+/* ---- stacking: linear stack, PWS, TF-PWS -------------------------------- */
+
+/* Cross-timestamp linear stack (_linear_stack_group,
+ * fastxc/operators/stacking/linear_stack.py:228-247): out[p] = float(sum of
+ * double(trace) / count) over traces [h_offsets[p], h_offsets[p]+h_counts[p])
+ * of d_traces ([*][nsamples]). */
+int fxc_linear_stack(fxc_ctx *ctx, const float *d_traces, const int64_t *h_offsets,
+                     const int32_t *h_counts, int32_t npairs, int32_t nsamples, float *d_out);
+
+/* Substack prestacking of each pair's traces into groups of `substack`
+ * (< 2 -> 1): mode 0 group means with weight count/num_segments and
+ * linear = sum(mean*weight) (prepare_sourcepack_host_item,
+ * native/pws/io/sourcepack_io.cu:385-478); mode 1 group sums with weight
+ * count/num_segments and linear = sum(sum)/num_segments (native/tfpws/io/
+ * sourcepack_io.cu:440-490). Writes h_group_offsets/h_group_counts
+ * ([npairs]) on the host, d_groups [total_groups][nsamples], d_weights
+ * [total_groups], d_linear [npairs][nsamples]. Synchronous. */
+int fxc_stack_prestack(fxc_ctx *ctx, const float *d_traces, const int64_t *h_trace_offsets,
+                       const int32_t *h_trace_counts, int32_t npairs, int32_t nsamples,
+                       int32_t substack, int32_t mode, float *d_groups, float *d_weights,
+                       float *d_linear, int64_t *h_group_offsets, int32_t *h_group_counts);
+
+/* Phase-weighted stack (compute_pws_host_batch, native/pws/worker/gpu.cu:
+ * 87-282): analytic signal of every group, unit phasors (modulus floor
+ * 1e-7), weighted mean, out = linear * |mean|^power (power 1 in the
+ * reference). Synchronous. */
+int fxc_pws_run(fxc_ctx *ctx, const float *d_groups, const float *d_weights,
+                const int64_t *h_group_offsets, const int32_t *h_group_counts, int32_t npairs,
+                const float *d_linear, int32_t nsamples, float power, float *d_out);
+
+/* S-transform time-frequency PWS (compute_tfpws_from_prestack,
+ * native/tfpws/core/tfpws_compute.cu:19-366): for every frequency of the
+ * nsamples/2+1 bins the Gaussian voices (scale 0.1) of the groups and of
+ * the linear stack, the phase weight, the weighted voice summed over time;
+ * optional -F band blend (taper_hz < 0 -> 5% of the band); final inverse,
+ * real part / N. Synchronous. */
+int fxc_tfpws_run(fxc_ctx *ctx, const float *d_groups, const float *d_weights,
+                  const int64_t *h_group_offsets, const int32_t *h_group_counts, int32_t npairs,
+                  const float *d_linear, int32_t nsamples, float delta, int32_t band_limited,
+                  float fmin, float fmax, float taper_hz, float power, float *d_out);
+
 /* Allocation-free variant of fxc_xc_run. No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc (a host framework that
  * owns all device memory through its own pool, or a job whose device

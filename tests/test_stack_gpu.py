@@ -1,0 +1,91 @@
+"""Stacking parity: linear stack (bit-exact with the reference's Python),
+PWS and TF-PWS against the FP64 oracle on seeded Ricker-plus-noise NCFs.
+
+Tolerances (relative L2 per pair): linear stack exact; PWS 1e-5; TF-PWS
+1e-5 (FP32 voices and weights against FP64; the Gaussian window is FP64 on
+both sides).
+"""
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from fastxc_gb300.synthetic import ncf_traces
+from oracle import stack_oracle as sto
+
+pytestmark = pytest.mark.gpu
+G = Path(__file__).resolve().parent / "golden"
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b, axis=-1) / np.maximum(np.linalg.norm(b, axis=-1), 1e-30)
+
+
+def test_linear_stack_matches_reference_golden(ctx, torch_cuda):
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    d = np.load(G / "linear_stack_golden.npz")
+    tr = torch.from_numpy(d["traces"]).cuda()
+    out = torch.empty((1, tr.shape[1]), dtype=torch.float32, device="cuda")
+    stack.linear_stack(ctx, tr, [0], [tr.shape[0]], tr.shape[1], out)
+    ctx.synchronize()
+    assert np.array_equal(out.cpu().numpy()[0], d["stacked"])
+
+
+def _prestacked(ctx, torch, tr, substack, mode):
+    from fastxc_gb300 import stack
+
+    npairs, nt, n = tr.shape
+    d_tr = torch.from_numpy(tr.reshape(-1, n)).cuda()
+    offs = np.arange(npairs) * nt
+    return stack.prestack(ctx, torch, d_tr, offs, [nt] * npairs, n, substack, mode)
+
+
+@pytest.mark.parametrize("substack,power", [(1, 1.0), (3, 1.0), (1, 2.0)])
+def test_pws_matches_oracle(ctx, torch_cuda, substack, power):
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    tr = ncf_traces(5, 17, 2001, seed=3)
+    g, w, lin, goff, gcnt = _prestacked(ctx, torch, tr, substack, stack.MODE_PWS)
+    out = torch.empty((5, 2001), dtype=torch.float32, device="cuda")
+    stack.pws(ctx, g, w, goff, gcnt, lin, 2001, out, power)
+    got = out.cpu().numpy()
+    ref = np.stack([sto.pws(tr[p], substack, power) for p in range(5)])
+    err = rel(got, ref)
+    print("pws rel err", err)
+    assert err.max() < 1e-5
+
+
+def test_prestack_matches_oracle(ctx, torch_cuda):
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    tr = ncf_traces(3, 10, 1001, seed=4)
+    for mode, fn in ((stack.MODE_PWS, sto.pws_prestack), (stack.MODE_TFPWS, sto.tfpws_prestack)):
+        g, w, lin, goff, gcnt = _prestacked(ctx, torch, tr, 4, mode)
+        assert list(gcnt) == [3, 3, 3] and list(goff) == [0, 3, 6]
+        for p in range(3):
+            rg, rw, rl = fn(tr[p], 4)
+            assert np.allclose(g.cpu().numpy()[3 * p: 3 * p + 3], rg, rtol=1e-6, atol=1e-6)
+            assert np.allclose(w.cpu().numpy()[3 * p: 3 * p + 3], rw, rtol=1e-7)
+            assert np.allclose(lin.cpu().numpy()[p], rl, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("band,power", [(None, 1.0), ((0.05, 2.0), 1.0), (None, 2.0)])
+def test_tfpws_matches_oracle(ctx, torch_cuda, band, power):
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    n = 1001
+    tr = ncf_traces(2, 9, n, seed=5)
+    g, w, lin, goff, gcnt = _prestacked(ctx, torch, tr, 3, stack.MODE_TFPWS)
+    out = torch.empty((2, n), dtype=torch.float32, device="cuda")
+    stack.tfpws(ctx, g, w, goff, gcnt, lin, n, out, 0.1, band=band, power=power)
+    got = out.cpu().numpy()
+    ref = np.stack([sto.tfpws(tr[p], 3, power, band=band, delta=0.1) for p in range(2)])
+    err = rel(got, ref)
+    print("tfpws rel err", err)
+    assert err.max() < 1e-5
