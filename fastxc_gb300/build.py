@@ -44,8 +44,33 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA 13 toolkit is required to build fastxc_gb300")
 
 
+APPS = PKG / "apps"
+BINDIR = PKG / "bin"
+
+
 def _sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
+
+
+def _build_apps(nvcc: str, force: bool) -> list[Path]:
+    """Drop-in executables (C++ host code linked against the library)."""
+    BINDIR.mkdir(exist_ok=True)
+    out = []
+    hdr = _headers_digest()
+    for src in sorted(APPS.glob("*.cpp")):
+        exe = BINDIR / src.stem
+        stamp = BUILD / f"app_{src.stem}.stamp"
+        key = hashlib.sha256((src.read_bytes().decode("utf-8", "replace") + hdr + LIB.name).encode()).hexdigest()[:16]
+        if force or not exe.exists() or not stamp.exists() or stamp.read_text() != key or \
+                exe.stat().st_mtime < LIB.stat().st_mtime:
+            cmd = [nvcc, "-O2", "-std=c++17", "-I" + str(INCLUDE), "-I" + str(CSRC), str(src), "-o", str(exe),
+                   "-L" + str(LIBDIR), "-lfastxc_gb300", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN/../lib"]
+            proc = subprocess.run(cmd, capture_output=True, text=True)
+            if proc.returncode != 0:
+                raise RuntimeError(f"app build failed for {src.name}:\n{' '.join(cmd)}\n{proc.stderr}")
+            stamp.write_text(key)
+        out.append(exe)
+    return out
 
 
 def _headers_digest() -> str:
@@ -100,6 +125,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
     for o in BUILD.glob("*.o"):
         if o.name not in keep:
             o.unlink()
+    _build_apps(nvcc, force)
     return LIB
 
 

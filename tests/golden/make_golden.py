@@ -15,7 +15,10 @@ copied):  python tests/golden/make_golden.py
                         station layouts;
   linear_stack_golden.npz  _linear_stack_group of
                         fastxc/operators/stacking/linear_stack.py on seeded
-                        records.
+                        records;
+  formats_golden.json   a stepack batch written by fastxc_gb300.formats as
+                        parsed by the reference's fastxc/tools/extract_stepack.py,
+                        and a SAC header encoded by fastxc/io/sac_binary.py.
 """
 
 from __future__ import annotations
@@ -57,6 +60,7 @@ PLAN_CASES = [
 def load_module(path: Path, name: str):
     spec = importlib.util.spec_from_file_location(name, path)
     mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod  # dataclasses look their module up while the class body runs
     spec.loader.exec_module(mod)
     return mod
 
@@ -206,7 +210,70 @@ def main() -> None:
                 fh.write(blob)
         _, stacked = ls._linear_stack_group(records)
     np.savez_compressed(HERE / "linear_stack_golden.npz", traces=traces, stacked=np.asarray(stacked, np.float32))
+
+    # file formats: a stepack written by fastxc_gb300.formats, read back by the
+    # reference's own stepack reader (fastxc/tools/extract_stepack.py); a SAC
+    # header written by the reference's encoder (fastxc/io/sac_binary.py)
+    sys.path.insert(0, str(HERE.parents[1]))
+    from fastxc_gb300 import formats
+
+    es = load_module(REF_ROOT / "fastxc" / "tools" / "extract_stepack.py", "ref_extract_stepack")
+    chans, spec = formats_case()
+    with tempfile.TemporaryDirectory() as td:
+        formats.write_stepack(td, 2, 5, chans, spec, 0.1, 0.05, group_count=2, start_group=4)
+        frags = es.discover_stepack_fragments(td)
+        out = {"fragments": [], "entries": []}
+        for fr in frags:
+            out["fragments"].append({k: (str(getattr(fr, k)) if k in ("tsv_path", "pack_path") else getattr(fr, k))
+                                     for k in ("timestamp", "nslc_start", "nslc_count", "batch_nslc_count", "nspec",
+                                               "nstep", "dt", "df", "payload_offset", "pitch_step_bytes",
+                                               "nslc_step_bytes")})
+            for e in es.read_fragment_nslc_entries(fr):
+                sp = es.read_entry_spectra(e)
+                out["entries"].append({"file_index": e.file_index, "nsl_id": e.nsl_id, "stla": e.stla, "stlo": e.stlo,
+                                       "key": e.key, "sum_re": float(np.real(sp).astype(np.float64).sum()),
+                                       "sum_im": float(np.imag(sp).astype(np.float64).sum()), "shape": list(sp.shape)})
+        hdr = es.read_stepack_header(Path(td) / "w002.b000005.stepack")
+        out["header"] = {k: getattr(hdr, k) for k in ("version", "header_size", "nslc_entry_size", "layout", "batch_seq",
+                                                      "start_group", "group_count", "worker_id", "nstep", "nslc_count",
+                                                      "nspec", "payload_offset", "payload_bytes", "pitch_step_bytes",
+                                                      "first_timestamp")}
+    for fr in out["fragments"]:
+        fr.pop("tsv_path", None)
+        fr.pop("pack_path", None)
+    sac = importlib.import_module("fastxc.io.sac_binary")
+    hd = sac.SacHeader.empty()
+    for k, v in SAC_PIN_FLOATS.items():
+        hd.set_float(k, v)
+    for k, v in SAC_PIN_INTS.items():
+        hd.set_int(k, v)
+    for k, v in SAC_PIN_TEXT.items():
+        hd.set_text(k, v)
+    raw = sac.encode_sac_record(hd, np.zeros(SAC_PIN_INTS["npts"], dtype=np.float32))
+    out["sac_header_hex"] = raw[:632].hex()
+    (HERE / "formats_golden.json").write_text(json.dumps(out, indent=1))
     print("goldens written to", HERE)
+
+
+SAC_PIN_FLOATS = {"delta": 0.1, "b": -100.0, "e": 100.0, "o": 0.0, "stla": 31.5, "stlo": 101.25, "evla": 30.5,
+                  "evlo": 100.75, "user0": 7.0, "user1": 12.0, "user2": 70012.0, "dist": 55.5, "az": 10.0,
+                  "baz": 190.0, "gcarc": 0.5}
+SAC_PIN_INTS = {"nzyear": 2020, "nzjday": 123, "nzhour": 4, "nzmin": 5, "nzsec": 0, "nzmsec": 0, "npts": 2001,
+                "iftype": 1, "leven": 1, "unused27": 1}
+SAC_PIN_TEXT = {"kstnm": "ST12", "kevnm": "XX.ST07", "kcmpnm": "BHE-BHN", "knetwk": "XX-XX"}
+
+
+def formats_case():
+    """Seeded channels + spectra of the stepack pin (two timestamps in one batch)."""
+    rng = np.random.default_rng(11)
+    chans = []
+    for t, ts in enumerate(("2020.123.0000", "2020.123.0100")):
+        for s, g in enumerate((3, 9)):
+            for c in "EN":
+                chans.append(dict(timestamp=ts, nsl_id=g, network="XX", station=f"ST{g:02d}", location="00",
+                                  component=f"BH{c}", stla=30.0 + s + t, stlo=100.5 - s))
+    spec = (rng.standard_normal((3, len(chans), 17)) + 1j * rng.standard_normal((3, len(chans), 17))).astype(np.complex64)
+    return chans, spec
 
 
 if __name__ == "__main__":
