@@ -190,6 +190,22 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_traffic(kernel: str, workload: str):
+    """DRAM bytes (read + write) of one launch of `kernel` on `workload`, from
+    the ncu summaries committed under profiles/ (their 'machine-readable'
+    lines); None when no capture of that workload exists."""
+    for p in sorted((ROOT / "profiles").glob("*.md")):
+        for ln in p.read_text().splitlines():
+            if ln.startswith("machine-readable:"):
+                try:
+                    d = json.loads(ln.split(":", 1)[1])
+                except ValueError:
+                    continue
+                if d.get("kernel") == kernel and d.get("workload") == workload:
+                    return int(d["traffic_bytes_per_launch"])
+    return None
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -225,6 +241,7 @@ def main():
     shape = xc_shape(nspec, NSTEP, DT, CC_LEN)
     spec, mask = spectra_device(torch, nwin, arr, nspec, DT, seed=rank, gap_frac=GAP_FRAC, device=dev)
     scale = 1.0 / nwin  # mean over days of per-day stacks with 1/nstep each
+    spec_bytes = nwin * nchan * nspec * 8
     pitch_stack = (nspec + 3) // 4 * 4
     d_stack = torch.empty((npairs, pitch_stack), dtype=torch.complex64, device=dev)
     d_ncf = torch.empty((npairs, shape.cc_size), dtype=torch.float32, device=dev)
@@ -332,6 +349,7 @@ def main():
     # roofline of the dominant kernel: the tcgen05 GEMM (tensor) or the plain
     # stack kernel, each timed with CUDA events on the launching stream
     peaks = {}
+    wkey = f"{nchan}ch_{nwin}win_nspec{nspec}"
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
         peaks = json.loads(pk.read_text())
@@ -350,7 +368,7 @@ def main():
         peak_src = ("measured sustained bf16 (cuBLAS, MEASURED_PEAKS.json)" if "bf16_tflops_sustained" in peaks
                     else "fallback 1.7 PFLOP/s sustained")
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": None, "peak_source": peak_src, "kernel": "k_xc_tc_gemm",
+                    "traffic": profile_traffic("k_xc_tc_gemm", wkey), "peak_source": peak_src, "kernel": "k_xc_tc_gemm",
                     "algorithmic": "issued MMA flops = nspec x ceil(nwin/32) x 24 x (2 x 128 x 16 x n) summed over tiles "
                                    "(3 bf16 hi/lo products, Re and Im, upper-triangle tiles)",
                     "useful_tflops": useful_flop / (kms / 1e3) / 1e12, "kernel_ms": kms,
@@ -361,7 +379,7 @@ def main():
         sm_max = peaks.get("sm_max_mhz", 2070.0)
         peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
         roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": None, "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)",
+                    "traffic": profile_traffic("k_xc_stack_plain", wkey), "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)",
                     "kernel": "k_xc_stack_plain", "algorithmic": "8 flop x nspec x pair-windows",
                     "kernel_ms": kms, "finalize_ms": hr["finalize_ms"]}
 
@@ -382,7 +400,7 @@ def main():
         "config": {"workload": f"xc linear stack: {NSTA} sta x {NCOMP} comp x {args.days} days, delta {DT}s, "
                                f"win 3600s -> {nwin} windows, nspec {nspec}, {npairs} pairs, lag {CC_LEN}s",
                    "pairs": npairs, "windows": nwin, "nspec": nspec, "cc_size": shape.cc_size,
-                   "l2": "inputs (20.5 GB) larger than L2, no flush", "parallelism": f"replicas x{world}"},
+                   "l2": f"inputs ({spec_bytes / 1e9:.1f} GB) larger than L2 (129 MB), no flush", "parallelism": f"replicas x{world}"},
         "rel_l2_vs_fp64": rel,
         "per_method": {k: {"pair_windows_per_s": pw / (v["ms_per_step"] / 1e3), "ms_per_step": v["ms_per_step"],
                            "pack_ms": v["pack_ms"], "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"]}

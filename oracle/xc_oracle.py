@@ -5,11 +5,13 @@ TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).
 
 Pinning: the integer functions (``finalize_shape``, ``build_jobs``,
 ``build_tasks_for_job``, path-table lookups) follow the reference C/C++ line by
-line and are checked bit-exactly. The reference ships no golden NCF vectors
-and its correlation runs only on a GPU through cuFFT, so the float path is
-pinned against the reference's own kernel source compiled for the CPU
-(``oracle/refkernels``) where available; otherwise it is "parity unpinned"
-beyond this restatement.
+line and are checked bit-exactly against the reference's own scheduler and
+path-table code compiled for the CPU (``oracle/build_ref.py``). The
+reference ships no golden NCF vectors and its correlation runs only on a GPU
+through cuFFT, so the float path (accumulateStepXc2DKernel,
+native/xc/kernels/cuda.kernels.cu:16-36, and finalize_xc_batch,
+native/xc/worker/executor.cu:6-55) is "parity unpinned" beyond this FP64
+restatement.
 """
 
 from __future__ import annotations
