@@ -66,6 +66,11 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_ctx_destroy": (_int, [_vp]),
     "fxc_ctx_set_stream": (_int, [_vp, _vp]),
     "fxc_ctx_synchronize": (_int, [_vp]),
+    "fxc_device_alloc": (_int, [_vp, C.c_size_t, C.POINTER(_vp)]),
+    "fxc_device_free": (_int, [_vp, _vp]),
+    "fxc_host_alloc": (_int, [C.c_size_t, C.POINTER(_vp)]),
+    "fxc_host_free": (_int, [_vp]),
+    "fxc_memcpy": (_int, [_vp, _vp, _vp, C.c_size_t, C.c_int]),
     "fxc_fft_c2c": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64, _int]),
     "fxc_fft_r2c": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64]),
     "fxc_fft_c2r": (_int, [_vp, _vp, _vp, _int, _int, _i64, _i64]),

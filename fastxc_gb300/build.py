@@ -75,7 +75,8 @@ def _build_apps(nvcc: str, force: bool) -> list[Path]:
 
 def _headers_digest() -> str:
     h = hashlib.sha256()
-    for p in sorted(list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))):
+    for p in sorted(list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h")) +
+                    list(APPS.glob("*.h"))):
         h.update(p.name.encode())
         h.update(p.read_bytes())
     return h.hexdigest()[:16]

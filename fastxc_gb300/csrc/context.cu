@@ -163,4 +163,64 @@ int fxc_ctx_synchronize(fxc_ctx* ctx) {
   return ctx_check_device_error(ctx);
 }
 
+int fxc_device_alloc(fxc_ctx* ctx, size_t bytes, void** out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "out is null");
+  *out = nullptr;
+  FXC_TRY(ctx_enter(ctx));
+  if (bytes == 0) return FXC_OK;
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    *out = nullptr;
+    set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    return FXC_ERR_NOMEM;
+  }
+  return FXC_OK;
+}
+
+int fxc_device_free(fxc_ctx* ctx, void* ptr) {
+  clear_error();
+  if (!ptr) return FXC_OK;
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  FXC_CUDA_TRY(cudaFree(ptr));
+  return FXC_OK;
+}
+
+int fxc_host_alloc(size_t bytes, void** out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "out is null");
+  *out = nullptr;
+  if (bytes == 0) return FXC_OK;
+  cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    *out = nullptr;
+    set_error("page-locked host allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    return FXC_ERR_NOMEM;
+  }
+  return FXC_OK;
+}
+
+int fxc_host_free(void* ptr) {
+  clear_error();
+  if (!ptr) return FXC_OK;
+  FXC_CUDA_TRY(cudaFreeHost(ptr));
+  return FXC_OK;
+}
+
+int fxc_memcpy(fxc_ctx* ctx, void* dst, const void* src, size_t bytes, int kind) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(kind >= FXC_COPY_H2D && kind <= FXC_COPY_D2D, "invalid copy kind %d", kind);
+  if (bytes == 0) return FXC_OK;
+  FXC_CHECK_ARG(dst && src, "null pointer");
+  const cudaMemcpyKind k = kind == FXC_COPY_H2D   ? cudaMemcpyHostToDevice
+                           : kind == FXC_COPY_D2H ? cudaMemcpyDeviceToHost
+                                                  : cudaMemcpyDeviceToDevice;
+  FXC_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
+  return FXC_OK;
+}
+
 }  // extern "C"

@@ -60,7 +60,7 @@ static std::string clean_field(const std::string& s) {
 }
 
 void Progress::init(const char* p, const char* task_name, size_t tot, const char* unit_name) {
-  path = p ? p : "";
+  path = (p && strcmp(p, "NONE") != 0) ? p : "";
   task = task_name;
   unit = unit_name;
   total = tot;

@@ -109,3 +109,67 @@ def read_xcpack_dir(root) -> list[dict]:
                 row["tsv"] = tsv.name
                 out.append(row)
     return out
+
+
+SOURCEPACK_COLUMNS = [
+    "timestamp", "path_id", "component_slot", "source_key", "receiver_key", "src_id", "rec_id",
+    "src_network", "src_station", "src_location", "src_component", "rec_network", "rec_station",
+    "rec_location", "rec_component", "npts", "dt", "dist", "az", "baz", "record_path", "record_offset",
+    "bytes", "storage_kind", "final_pair_path",
+]
+
+
+def sac_header_bytes(npts: int, delta: float, b: float = 0.0, **fields) -> bytes:
+    """632-byte little-endian SAC header: SAC null values (-12345, "-12345  ")
+    except version 6, npts, delta, b, iftype 1, leven 1 and `fields`
+    (names of SAC_FLOAT / SAC_INT / SAC_STR)."""
+    f = np.full(70, -12345.0, "<f4")
+    i = np.full(40, -12345, "<i4")
+    f[0], f[5] = delta, b
+    i[6], i[9], i[15], i[35] = 6, npts, 1, 1
+    s = bytearray(b"-12345  " * 24)
+    s[8:24] = b"-12345".ljust(16)  # kevnm is 16 characters wide
+    for k, v in fields.items():
+        if k in SAC_FLOAT:
+            f[SAC_FLOAT[k]] = v
+        elif k in SAC_INT:
+            i[SAC_INT[k]] = v
+        else:
+            o, n = SAC_STR[k]
+            s[o - 440:o - 440 + n] = str(v).encode()[:n].ljust(n)
+    return f.tobytes() + i.tobytes() + bytes(s)
+
+
+def write_sourcepack(root, name: str, rows) -> Path:
+    """One SourcePack shard: <name>.pack of SAC records and <name>.tsv index.
+    rows: dicts with the index columns (except record_path, record_offset,
+    bytes, npts, dt) plus 'data' (float32 trace) and 'delta'."""
+    root = Path(root).resolve()
+    root.mkdir(parents=True, exist_ok=True)
+    pack, tsv = root / f"{name}.pack", root / f"{name}.tsv"
+    with pack.open("wb") as fh, tsv.open("w") as th:
+        th.write("\t".join(SOURCEPACK_COLUMNS) + "\n")
+        for r in rows:
+            data = np.ascontiguousarray(r["data"], "<f4")
+            blob = sac_header_bytes(data.size, r["delta"], b=-(data.size // 2) * r["delta"]) + data.tobytes()
+            off = fh.tell()
+            fh.write(blob)
+            row = dict(r, record_path=str(pack), record_offset=off, bytes=len(blob), npts=data.size,
+                       dt=f"{r['delta']:g}", storage_kind=r.get("storage_kind", "xcpack"))
+            th.write("\t".join(str(row.get(c, "")) for c in SOURCEPACK_COLUMNS) + "\n")
+    return tsv
+
+
+def read_sourcepack_index(path) -> list[dict]:
+    """Rows of a SourcePack index with their SAC records ('header', 'data')."""
+    out = []
+    with open(path) as fh:
+        for row in csv.DictReader(fh, delimiter="\t"):
+            with open(row["record_path"], "rb") as pf:
+                pf.seek(int(row["record_offset"]))
+                raw = pf.read(int(row["bytes"]))
+            row["header"] = parse_sac_header(raw[:SAC_HEADER_BYTES])
+            row["raw_header"] = raw[:SAC_HEADER_BYTES]
+            row["data"] = np.frombuffer(raw[SAC_HEADER_BYTES:], "<f4").copy()
+            out.append(row)
+    return out

@@ -68,6 +68,21 @@ int fxc_ctx_destroy(fxc_ctx *ctx);
 int fxc_ctx_set_stream(fxc_ctx *ctx, void *stream);
 int fxc_ctx_synchronize(fxc_ctx *ctx);
 
+/* ---- memory helpers ------------------------------------------------------
+ * For callers without a CUDA runtime of their own (the drop-in executables,
+ * ctypes). No reference counterpart: the reference executables call
+ * cudaMalloc / cudaMemcpy directly. fxc_memcpy is asynchronous on the
+ * context's stream (kind: FXC_COPY_H2D, FXC_COPY_D2H, FXC_COPY_D2D);
+ * fxc_device_free synchronises the stream first. */
+#define FXC_COPY_H2D 1
+#define FXC_COPY_D2H 2
+#define FXC_COPY_D2D 3
+int fxc_device_alloc(fxc_ctx *ctx, size_t bytes, void **out);
+int fxc_device_free(fxc_ctx *ctx, void *ptr);
+int fxc_host_alloc(size_t bytes, void **out);
+int fxc_host_free(void *ptr);
+int fxc_memcpy(fxc_ctx *ctx, void *dst, const void *src, size_t bytes, int kind);
+
 /* ---- FFT (replaces every cuFFT plan of the reference, SURVEY table 2.4) --- */
 
 /* Batched complex transform of length n, unnormalised (cuFFT convention:
