@@ -1,12 +1,15 @@
 // Host side of the FFT library: factorisation into Stockham stages and the
 // per-device cache of twiddle tables.
 #include <cmath>
+#include <complex>
+#include <cstdint>
 #include <map>
 #include <mutex>
 #include <utility>
 #include <vector>
 
 #include "fft.cuh"
+#include "fft_any.cuh"
 
 namespace fxc {
 
@@ -158,6 +161,118 @@ int fft_twiddles(int len, const float2** out) {
   }
   cache[key] = d;
   *out = d;
+  return FXC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Bluestein tables
+// ---------------------------------------------------------------------------
+
+// Forward DFT (exp(-)) of a 2-3-5-7-smooth length in double precision:
+// recursive decimation in time by the smallest prime factor.
+static void host_fft(std::vector<std::complex<double>>& a) {
+  const size_t n = a.size();
+  if (n <= 1) return;
+  size_t r = 2;
+  while (n % r) ++r;
+  const size_t l = n / r;
+  std::vector<std::vector<std::complex<double>>> sub(r, std::vector<std::complex<double>>(l));
+  for (size_t j = 0; j < l; ++j)
+    for (size_t q = 0; q < r; ++q) sub[q][j] = a[j * r + q];
+  for (size_t q = 0; q < r; ++q) host_fft(sub[q]);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (size_t k = 0; k < n; ++k) {
+    std::complex<double> acc = 0.0;
+    for (size_t q = 0; q < r; ++q) {
+      const double ang = -two_pi * (double)((q * k) % n) / (double)n;
+      acc += sub[q][k % l] * std::complex<double>(std::cos(ang), std::sin(ang));
+    }
+    a[k] = acc;
+  }
+}
+
+static bool smooth2357(int m) {
+  for (int r : {2, 3, 5, 7})
+    while (m % r == 0) m /= r;
+  return m == 1;
+}
+
+static int upload(const void* h, size_t bytes, void** d) {
+  cudaError_t e = cudaMalloc(d, bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    set_error("cudaMalloc of %zu bytes for FFT tables failed: %s", bytes, cudaGetErrorString(e));
+    return FXC_ERR_NOMEM;
+  }
+  e = cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(*d);
+    set_error("upload of FFT tables failed: %s", cudaGetErrorString(e));
+    return FXC_ERR_CUDA;
+  }
+  return FXC_OK;
+}
+
+int any_plan(int n, int direct_max, int bluestein_max, AnyPlan* out) {
+  FXC_CHECK_ARG(n >= 1, "transform length %d", n);
+  AnyPlan a{};
+  a.n = n;
+  if (n <= direct_max && fft_length_supported(n)) {
+    const float2* tw = nullptr;
+    FXC_TRY(fft_twiddles(n, &tw));
+    FXC_TRY(fft_make_plan(n, tw, 1, &a.p));
+    *out = a;
+    return FXC_OK;
+  }
+  int m = 2 * n - 1;
+  while (!smooth2357(m)) ++m;
+  if (m > bluestein_max) {
+    set_error("transform length %d needs a Bluestein length %d above the in-CTA limit %d", n, m,
+              bluestein_max);
+    return FXC_ERR_UNSUPPORTED;
+  }
+  const float2* tw = nullptr;
+  FXC_TRY(fft_twiddles(m, &tw));
+  FXC_TRY(fft_make_plan(m, tw, 1, &a.p));
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::pair<float2*, float2*>> cache;
+  int dev = 0;
+  FXC_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_pair(dev, n);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    // w_k = exp(-i pi k^2 / n) with k^2 reduced mod 2n; kernel b_j = conj(w_j)
+    // for |j| < n placed circularly in length m; khat = DFT_m(b) / m stored at
+    // the DIF position of each frequency.
+    const double pi = 3.14159265358979323846264338327950288;
+    std::vector<std::complex<double>> w((size_t)n), b((size_t)m, 0.0);
+    for (int k = 0; k < n; ++k) {
+      const uint64_t q = ((uint64_t)k * (uint64_t)k) % (2ull * (uint64_t)n);
+      const double ang = pi * (double)q / (double)n;
+      w[k] = std::complex<double>(std::cos(ang), -std::sin(ang));
+    }
+    b[0] = std::conj(w[0]);
+    for (int j = 1; j < n; ++j) b[j] = b[(size_t)m - j] = std::conj(w[j]);
+    host_fft(b);
+    std::vector<float2> hw((size_t)n), hk((size_t)m);
+    for (int k = 0; k < n; ++k) hw[k] = make_float2((float)w[k].real(), (float)w[k].imag());
+    for (int k = 0; k < m; ++k) {
+      const std::complex<double> v = b[k] / (double)m;
+      hk[fft_digit_pos(a.p, k)] = make_float2((float)v.real(), (float)v.imag());
+    }
+    void *dw = nullptr, *dk = nullptr;
+    FXC_TRY(upload(hw.data(), sizeof(float2) * hw.size(), &dw));
+    const int rc = upload(hk.data(), sizeof(float2) * hk.size(), &dk);
+    if (rc != FXC_OK) {
+      cudaFree(dw);
+      return rc;
+    }
+    it = cache.emplace(key, std::make_pair((float2*)dw, (float2*)dk)).first;
+  }
+  a.chirp = it->second.first;
+  a.khat = it->second.second;
+  *out = a;
   return FXC_OK;
 }
 

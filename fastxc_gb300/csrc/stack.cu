@@ -29,12 +29,14 @@
 
 #include "context.cuh"
 #include "fft.cuh"
+#include "fft_any.cuh"
 #include "fft_launch.cuh"
 
 namespace fxc {
 
-constexpr int kStT = 64;        // threads per row transform CTA
-constexpr int kStNmax = 8192;   // longest stacked trace (complex FFT in shared memory)
+constexpr int kStT = 64;           // threads per row transform CTA
+constexpr int kStNmax = 8192;      // longest directly transformed trace
+constexpr int kStBluestein = 16384;  // longest Bluestein length (any other trace length)
 
 // ---------------------------------------------------------------------------
 // linear stack and prestack
@@ -98,12 +100,12 @@ __global__ void k_prestack(const float* __restrict__ traces, const int64_t* __re
 // ---------------------------------------------------------------------------
 
 // Analytic-signal mask of hilbertTransformKernel: bin 0 and bins >= (N+1)/2
-// -> 0, the others x 2. buf holds the DIF output (digit-reversed points).
-__device__ __forceinline__ void analytic_mask(float2* buf, const FftPlan& p) {
-  const int n = p.n;
+// -> 0, the others x 2. buf holds the any_forward layout.
+__device__ __forceinline__ void analytic_mask(float2* buf, const AnyPlan& a) {
+  const int n = a.n;
   const int half = (n + 1) / 2;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int pos = __ldg(p.perm + k);
+    const int pos = any_pos(a, k);
     float2 v = buf[pos];
     if (k == 0 || k >= half)
       v = make_float2(0.f, 0.f);
@@ -125,16 +127,16 @@ __device__ __forceinline__ float weight_pow(float mag2, float power) {
 __global__ void __launch_bounds__(kStT)
     k_pws(const float* __restrict__ groups, const float* __restrict__ weights,
           const int64_t* __restrict__ goffs, const int32_t* __restrict__ gcounts,
-          const float* __restrict__ linear, FftPlan p, float power, float* __restrict__ out) {
+          const float* __restrict__ linear, AnyPlan a, float power, float* __restrict__ out) {
   extern __shared__ float2 sm[];
-  const int n = p.n;
+  const int n = a.n;
   float2* buf = sm;
-  float2* acc = sm + n;
-  float2* stw = sm + 2 * n;
+  float2* acc = sm + any_buf_elems(a);
+  float2* stw = acc + n;
   const int pair = blockIdx.x;
   const int64_t goff = goffs[pair];
   const int ng = gcounts[pair];
-  fft_twiddles_to_smem<kStT>(p, stw);
+  fft_twiddles_to_smem<kStT>(a.p, stw);
   for (int t = threadIdx.x; t < n; t += kStT) acc[t] = make_float2(0.f, 0.f);
   const float invn = 1.0f / (float)n;
   for (int g = 0; g < ng; ++g) {
@@ -143,10 +145,10 @@ __global__ void __launch_bounds__(kStT)
     __syncthreads();
     for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
     __syncthreads();
-    fft_dif<kStT>(buf, p, stw, false);  // R2C into an N-point row (odd N: full spectrum)
-    analytic_mask(buf, p);
+    any_forward<kStT>(buf, a, stw);  // R2C into an N-point row (odd N: full spectrum)
+    analytic_mask(buf, a);
     __syncthreads();
-    fft_dit<kStT>(buf, p, stw, true);   // C2C inverse, unnormalised, natural order
+    any_inverse<kStT>(buf, a, stw);  // C2C inverse, unnormalised, natural order
     for (int t = threadIdx.x; t < n; t += kStT) {
       // cudaNormalizeComplex: z / nfft, modulus floored at 1e-7
       const float2 z = buf[t];
@@ -174,20 +176,20 @@ __global__ void __launch_bounds__(kStT)
 // Analytic spectrum (natural order) of every row: groups of all pairs, then
 // the linear stack of every pair.
 __global__ void __launch_bounds__(kStT)
-    k_analytic_spectrum(const float* __restrict__ rows, FftPlan p, float2* __restrict__ out) {
+    k_analytic_spectrum(const float* __restrict__ rows, AnyPlan a, float2* __restrict__ out) {
   extern __shared__ float2 sm[];
-  const int n = p.n;
+  const int n = a.n;
   float2* buf = sm;
-  float2* stw = sm + n;
-  fft_twiddles_to_smem<kStT>(p, stw);
+  float2* stw = sm + any_buf_elems(a);
+  fft_twiddles_to_smem<kStT>(a.p, stw);
   const float* x = rows + (int64_t)blockIdx.x * n;
   for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
   __syncthreads();
-  fft_dif<kStT>(buf, p, stw, false);
-  analytic_mask(buf, p);
+  any_forward<kStT>(buf, a, stw);
+  analytic_mask(buf, a);
   __syncthreads();
   float2* o = out + (int64_t)blockIdx.x * n;
-  for (int k = threadIdx.x; k < n; k += kStT) o[k] = buf[__ldg(p.perm + k)];
+  for (int k = threadIdx.x; k < n; k += kStT) o[k] = buf[any_pos(a, k)];
 }
 
 struct TfBand {
@@ -217,15 +219,15 @@ __device__ __forceinline__ float gauss_factor(int c, int f, int n, double scale)
 __global__ void __launch_bounds__(kStT)
     k_tfpws_freq(const float2* __restrict__ Xg, const float2* __restrict__ Xl,
                  const float* __restrict__ weights, const int64_t* __restrict__ goffs,
-                 const int32_t* __restrict__ gcounts, FftPlan p, int f0, TfBand band, float power,
+                 const int32_t* __restrict__ gcounts, AnyPlan a, int f0, TfBand band, float power,
                  float2* __restrict__ spec_out) {
   extern __shared__ float2 sm[];
   __shared__ float sred[kStT / 32];
   __shared__ float sredi[kStT / 32];
-  const int n = p.n;
+  const int n = a.n;
   float2* buf = sm;
-  float2* W = sm + n;
-  float* gs = reinterpret_cast<float*>(sm + 2 * n);
+  float2* W = sm + any_buf_elems(a);
+  float* gs = reinterpret_cast<float*>(W + n);
   float2* stw = reinterpret_cast<float2*>(gs + ((n + 1) & ~1));
   const int f = f0 + blockIdx.x;
   const int pair = blockIdx.y;
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(kStT)
       alpha = 0.5f - 0.5f * cosf(pi * ((band.fmax - freq) / tp));
     }
   }
-  fft_twiddles_to_smem<kStT>(p, stw);
+  fft_twiddles_to_smem<kStT>(a.p, stw);
   for (int c = threadIdx.x; c < n; c += kStT) {
     gs[c] = gauss_factor(c, f, n, 0.1);
     W[c] = make_float2(0.f, 0.f);
@@ -263,10 +265,10 @@ __global__ void __launch_bounds__(kStT)
       if (k >= n) k -= n;
       const float2 v = X[k];
       const float gf = gs[c];
-      buf[__ldg(p.perm + c)] = make_float2(v.x * gf, v.y * gf);
+      buf[any_pos(a, c)] = make_float2(v.x * gf, v.y * gf);
     }
     __syncthreads();
-    fft_dit<kStT>(buf, p, stw, true);  // voice of group g (unnormalised C2C inverse)
+    any_inverse<kStT>(buf, a, stw);  // voice of group g (unnormalised C2C inverse)
     for (int t = threadIdx.x; t < n; t += kStT) {
       // calculateWeightSub
       const float x = buf[t].x, y = buf[t].y;
@@ -283,10 +285,10 @@ __global__ void __launch_bounds__(kStT)
     if (k >= n) k -= n;
     const float2 v = XL[k];
     const float gf = gs[c];
-    buf[__ldg(p.perm + c)] = make_float2(v.x * gf, v.y * gf);
+    buf[any_pos(a, c)] = make_float2(v.x * gf, v.y * gf);
   }
   __syncthreads();
-  fft_dit<kStT>(buf, p, stw, true);  // stack voice
+  any_inverse<kStT>(buf, a, stw);  // stack voice
   // applyWeight + sumOverTimeAxisKernel
   float sr = 0.f, si = 0.f;
   for (int t = threadIdx.x; t < n; t += kStT) {
@@ -322,16 +324,16 @@ __global__ void __launch_bounds__(kStT)
 
 // Final C2C inverse of the output spectrum, real part / N (extractReal).
 __global__ void __launch_bounds__(kStT)
-    k_tfpws_final(const float2* __restrict__ spec, FftPlan p, float* __restrict__ out) {
+    k_tfpws_final(const float2* __restrict__ spec, AnyPlan a, float* __restrict__ out) {
   extern __shared__ float2 sm[];
-  const int n = p.n;
+  const int n = a.n;
   float2* buf = sm;
-  float2* stw = sm + n;
-  fft_twiddles_to_smem<kStT>(p, stw);
+  float2* stw = sm + any_buf_elems(a);
+  fft_twiddles_to_smem<kStT>(a.p, stw);
   const float2* S = spec + (int64_t)blockIdx.x * n;
-  for (int k = threadIdx.x; k < n; k += kStT) buf[__ldg(p.perm + k)] = S[k];
+  for (int k = threadIdx.x; k < n; k += kStT) buf[any_pos(a, k)] = S[k];
   __syncthreads();
-  fft_dit<kStT>(buf, p, stw, true);
+  any_inverse<kStT>(buf, a, stw);
   float* o = out + (int64_t)blockIdx.x * n;
   for (int t = threadIdx.x; t < n; t += kStT) o[t] = buf[t].x / (float)n;
 }
@@ -345,11 +347,9 @@ __global__ void k_tfpws_init(const float2* __restrict__ Xl, int64_t total, int l
     spec[i] = limited ? Xl[i] : make_float2(0.f, 0.f);
 }
 
-static int stack_plan(int n, FftPlan* p) {
-  FXC_CHECK_ARG(n >= 2 && n <= kStNmax, "trace length %d outside [2, %d]", n, kStNmax);
-  const float2* tw = nullptr;
-  FXC_TRY(fft_twiddles(n, &tw));
-  return fft_make_plan(n, tw, 1, p);
+static int stack_plan(int n, AnyPlan* a) {
+  FXC_CHECK_ARG(n >= 2, "trace length %d below 2", n);
+  return any_plan(n, kStNmax, kStBluestein, a);
 }
 
 struct PairGroups {
@@ -432,8 +432,8 @@ int fxc_pws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   if (npairs == 0) return FXC_OK;
   FXC_CHECK_ARG(d_groups && d_weights && h_group_offsets && h_group_counts && d_linear && d_out,
                 "null pointer");
-  FftPlan p;
-  FXC_TRY(stack_plan(nsamples, &p));
+  AnyPlan a;
+  FXC_TRY(stack_plan(nsamples, &a));
   const size_t n8 = sizeof(int64_t) * npairs, n4 = sizeof(int32_t) * npairs;
   const size_t o2 = (n8 + 255) & ~size_t(255);
   FXC_TRY(ctx->scratch2.reserve(o2 + n4 + 256));
@@ -442,10 +442,11 @@ int fxc_pws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   int32_t* d_gcnt = reinterpret_cast<int32_t*>(base + o2);
   FXC_CUDA_TRY(cudaMemcpyAsync(d_goff, h_group_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
   FXC_CUDA_TRY(cudaMemcpyAsync(d_gcnt, h_group_counts, n4, cudaMemcpyHostToDevice, ctx->stream));
-  const size_t smem = sizeof(float2) * (2 * (size_t)nsamples + fft_tw_smem_elems(p));
+  const size_t smem =
+      sizeof(float2) * ((size_t)any_buf_elems(a) + (size_t)nsamples + fft_tw_smem_elems(a.p));
   FXC_TRY(set_smem_limit(k_pws, smem));
   k_pws<<<(unsigned)npairs, kStT, smem, ctx->stream>>>(d_groups, d_weights, d_goff, d_gcnt, d_linear,
-                                                        p, power, d_out);
+                                                        a, power, d_out);
   count_launch();
   FXC_LAUNCH_CHECK();
   FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -463,8 +464,8 @@ int fxc_tfpws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   FXC_CHECK_ARG(d_groups && d_weights && h_group_offsets && h_group_counts && d_linear && d_out,
                 "null pointer");
   FXC_CHECK_ARG(npairs <= 65535, "at most 65535 pairs per call");
-  FftPlan p;
-  FXC_TRY(stack_plan(nsamples, &p));
+  AnyPlan a;
+  FXC_TRY(stack_plan(nsamples, &a));
   const int n = nsamples;
   int64_t total_groups = 0;
   for (int i = 0; i < npairs; ++i) total_groups = std::max<int64_t>(total_groups, h_group_offsets[i] + h_group_counts[i]);
@@ -497,32 +498,33 @@ int fxc_tfpws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   float2* spec = reinterpret_cast<float2*>(base + o_sp);
   FXC_CUDA_TRY(cudaMemcpyAsync(d_goff, h_group_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
   FXC_CUDA_TRY(cudaMemcpyAsync(d_gcnt, h_group_counts, n4, cudaMemcpyHostToDevice, ctx->stream));
-  const size_t sm1 = sizeof(float2) * ((size_t)n + fft_tw_smem_elems(p));
+  const size_t sm1 = sizeof(float2) * ((size_t)any_buf_elems(a) + fft_tw_smem_elems(a.p));
   FXC_TRY(set_smem_limit(k_analytic_spectrum, sm1));
   FXC_CHECK_ARG(total_groups <= 0x7fffffff, "too many groups");
   if (total_groups > 0) {
-    k_analytic_spectrum<<<(unsigned)total_groups, kStT, sm1, ctx->stream>>>(d_groups, p, Xg);
+    k_analytic_spectrum<<<(unsigned)total_groups, kStT, sm1, ctx->stream>>>(d_groups, a, Xg);
     count_launch();
     FXC_LAUNCH_CHECK();
   }
-  k_analytic_spectrum<<<(unsigned)npairs, kStT, sm1, ctx->stream>>>(d_linear, p, Xl);
+  k_analytic_spectrum<<<(unsigned)npairs, kStT, sm1, ctx->stream>>>(d_linear, a, Xl);
   count_launch();
   FXC_LAUNCH_CHECK();
   k_tfpws_init<<<1024, 256, 0, ctx->stream>>>(Xl, (int64_t)npairs * n, band_limited, spec);
   count_launch();
   FXC_LAUNCH_CHECK();
   const int nfreq = n / 2 + 1;
-  const size_t sm2 = sizeof(float2) * (2 * (size_t)n + fft_tw_smem_elems(p)) + sizeof(float) * (size_t)((n + 1) & ~1);
+  const size_t sm2 = sizeof(float2) * ((size_t)any_buf_elems(a) + (size_t)n + fft_tw_smem_elems(a.p)) +
+                     sizeof(float) * (size_t)((n + 1) & ~1);
   FXC_TRY(set_smem_limit(k_tfpws_freq, sm2));
   for (int f0 = 0; f0 < nfreq; f0 += 65535) {
     dim3 g((unsigned)std::min(65535, nfreq - f0), (unsigned)npairs);
-    k_tfpws_freq<<<g, kStT, sm2, ctx->stream>>>(Xg, Xl, d_weights, d_goff, d_gcnt, p, f0, band, power,
+    k_tfpws_freq<<<g, kStT, sm2, ctx->stream>>>(Xg, Xl, d_weights, d_goff, d_gcnt, a, f0, band, power,
                                                 spec);
     count_launch();
     FXC_LAUNCH_CHECK();
   }
   FXC_TRY(set_smem_limit(k_tfpws_final, sm1));
-  k_tfpws_final<<<(unsigned)npairs, kStT, sm1, ctx->stream>>>(spec, p, d_out);
+  k_tfpws_final<<<(unsigned)npairs, kStT, sm1, ctx->stream>>>(spec, a, d_out);
   count_launch();
   FXC_LAUNCH_CHECK();
   FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

@@ -89,3 +89,37 @@ def test_tfpws_matches_oracle(ctx, torch_cuda, band, power):
     err = rel(got, ref)
     print("tfpws rel err", err)
     assert err.max() < 1e-5
+
+
+@pytest.mark.parametrize("n", [4001, 1009, 3937])
+def test_pws_prime_lengths_bluestein(ctx, torch_cuda, n):
+    """NCF lengths with a prime factor above 31 (4001 = lag 200 s at 10 Hz,
+    prime; 3937 = 31 * 127) run through the Bluestein transform."""
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    tr = ncf_traces(3, 8, n, seed=6)
+    g, w, lin, goff, gcnt = _prestacked(ctx, torch, tr, 2, stack.MODE_PWS)
+    out = torch.empty((3, n), dtype=torch.float32, device="cuda")
+    stack.pws(ctx, g, w, goff, gcnt, lin, n, out, 1.0)
+    got = out.cpu().numpy()
+    ref = np.stack([sto.pws(tr[p], 2, 1.0) for p in range(3)])
+    err = rel(got, ref)
+    print("pws bluestein rel err", n, err)
+    assert err.max() < 1e-5
+
+
+@pytest.mark.parametrize("n,band", [(211, None), (401, (0.2, 1.5))])
+def test_tfpws_prime_lengths_bluestein(ctx, torch_cuda, n, band):
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    tr = ncf_traces(2, 6, n, seed=7)
+    g, w, lin, goff, gcnt = _prestacked(ctx, torch, tr, 2, stack.MODE_TFPWS)
+    out = torch.empty((2, n), dtype=torch.float32, device="cuda")
+    stack.tfpws(ctx, g, w, goff, gcnt, lin, n, out, 0.1, band=band, power=1.0)
+    got = out.cpu().numpy()
+    ref = np.stack([sto.tfpws(tr[p], 2, 1.0, band=band, delta=0.1) for p in range(2)])
+    err = rel(got, ref)
+    print("tfpws bluestein rel err", n, err)
+    assert err.max() < 1e-5
