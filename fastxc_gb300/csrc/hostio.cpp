@@ -439,7 +439,10 @@ int stepack_write_batch(const std::string& root_in, int worker_id, size_t batch_
               (unsigned long long)table, (unsigned long long)h.payload_offset,
               (unsigned long long)rpay, (unsigned long long)pay, (unsigned long long)rstep,
               (unsigned long long)pitch, (unsigned long long)nslc_step);
-      fprintf(tf, "%d\t%d\n", nodes[b].nsl_id, nodes[e - 1].nsl_id);
+      auto nsl = [](const Channel& c) {
+        return c.nsl_text.empty() ? std::to_string(c.nsl_id) : clean_field(c.nsl_text);
+      };
+      fprintf(tf, "%s\t%s\n", nsl(nodes[b]).c_str(), nsl(nodes[e - 1]).c_str());
       b = e;
     }
     st = 0;

@@ -113,6 +113,7 @@ static_assert(sizeof(StepackNslc) == 128, "stepack NSLC entry is 128 bytes");
 
 struct Channel {
   std::string timestamp, network, station, location, component;
+  std::string nsl_text;  // nsl_id as written in the SAC index (stepack TSV first/last_nsl_id)
   int nsl_id = 0;
   float stla = 0, stlo = 0;
 };

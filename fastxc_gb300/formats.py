@@ -173,3 +173,31 @@ def read_sourcepack_index(path) -> list[dict]:
             row["data"] = np.frombuffer(raw[SAC_HEADER_BYTES:], "<f4").copy()
             out.append(row)
     return out
+
+
+def read_stepack(pack) -> dict:
+    """Header fields, NSLC entries and payload (complex64 [nstep][nslc][nspec])
+    of one stepack batch file."""
+    raw = Path(pack).read_bytes()
+    h = STEPACK_HDR.unpack_from(raw, 0)
+    names = ["magic", "version", "header_size", "nslc_entry_size", "layout", "batch_seq", "start_group",
+             "group_count", "worker_id", "nstep", "nslc_count", "nspec", "dt", "df", "nslc_table_bytes",
+             "payload_offset", "payload_bytes", "pitch_step_bytes", "first_timestamp", "reserved"]
+    hd = dict(zip(names, h))
+    hd["magic"] = hd["magic"].rstrip(b"\0").decode()
+    hd["first_timestamp"] = hd["first_timestamp"].rstrip(b"\0").decode()
+    ents = []
+    for i in range(hd["nslc_count"]):
+        e = STEPACK_NSLC.unpack_from(raw, hd["header_size"] + i * hd["nslc_entry_size"])
+        ents.append(dict(file_index=e[0], nsl_id=e[1], stla=e[2], stlo=e[3],
+                         network=e[4].rstrip(b"\0").decode(), station=e[5].rstrip(b"\0").decode(),
+                         location=e[6].rstrip(b"\0").decode(), component=e[7].rstrip(b"\0").decode()))
+    pay = np.frombuffer(raw, np.complex64, count=hd["nstep"] * hd["nslc_count"] * hd["nspec"],
+                        offset=hd["payload_offset"]).reshape(hd["nstep"], hd["nslc_count"], hd["nspec"])
+    return {"header": hd, "entries": ents, "payload": pay}
+
+
+def write_sac(path, data: np.ndarray, delta: float, **fields) -> None:
+    """A SAC file: header (sac_header_bytes) + float32 samples."""
+    data = np.ascontiguousarray(data, "<f4")
+    Path(path).write_bytes(sac_header_bytes(data.size, delta, **fields) + data.tobytes())
