@@ -19,6 +19,9 @@
 //     one CTA per pair, the half-length complex row in shared memory, only
 //     cc_size samples written back.
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <map>
 #include <vector>
 
@@ -303,6 +306,99 @@ __global__ void __launch_bounds__(T, 1)
   (void)inv_norm_f;
 }
 
+// Output-pruned finalize for any even nfft (also above the in-CTA FFT
+// limit, e.g. nfft 74 088 at 20 Hz): only the cc_size lags of the cut are
+// formed. With nfft = N = P*Q and k = k1 + P*k2,
+//   x[n] = sum_k1 exp(2 pi i n k1 / N) * Y_k1[n mod Q],
+//   Y_k1 = inverse DFT_Q of the decimated Hermitian spectrum S[k1 + P*k2],
+// so a pair costs P length-Q transforms in shared memory plus P complex
+// multiply-adds per kept lag; the real part is kept (C2R drops the
+// imaginary parts of bins 0 and N/2 the same way). The lag sums live in
+// shared memory (nothing is held in registers across the transforms).
+template <int T>
+__global__ void __launch_bounds__(T, 4)
+    k_xc_finalize_pruned(const float2* __restrict__ stack, int64_t stack_pitch, FftPlan pq, int N,
+                         int half_cc, int cc_size, double inv_norm, float* __restrict__ ncf) {
+  extern __shared__ float2 sm[];
+  const int Q = pq.n;
+  const int P = N / Q;
+  const int nspec = N / 2 + 1;
+  // pq's twiddle table has stride N/Q over the N-point table, so stw also
+  // serves exp(-2 pi i m / N) for the lag phases (tw_lookup(stw, m)).
+  float2* buf = sm;
+  float2* stw = buf + Q;
+  float* acc = reinterpret_cast<float*>(stw + fft_tw_smem_elems(pq));
+  fft_twiddles_to_smem<T>(pq, stw);
+  for (int t = threadIdx.x; t < cc_size; t += T) acc[t] = 0.f;
+  const float2* X = stack + (int64_t)blockIdx.x * stack_pitch;
+  for (int k1 = 0; k1 < P; ++k1) {
+    __syncthreads();
+    for (int k2 = threadIdx.x; k2 < Q; k2 += T) {
+      const int k = k1 + P * k2;
+      float2 v;
+      if (k < nspec) {
+        v = X[k];
+      } else {
+        v = X[N - k];
+        v.y = -v.y;
+      }
+      buf[k2] = v;
+    }
+    __syncthreads();
+    fft_dif<T>(buf, pq, stw, true);  // inverse DFT_Q, digit-reversed positions
+    for (int t = threadIdx.x; t < cc_size; t += T) {
+      int n = N - half_cc + t;
+      if (n >= N) n -= N;
+      const float2 y = buf[__ldg(pq.perm + n % Q)];
+      const int m = (int)(((long long)n * k1) % N);
+      const float2 w = tw_lookup(stw, m);
+      acc[t] += y.x * w.x + y.y * w.y;  // Re(y * conj(w)), w = exp(-2 pi i m / N)
+    }
+  }
+  __syncthreads();
+  float* out = ncf + (int64_t)blockIdx.x * cc_size;
+  for (int t = threadIdx.x; t < cc_size; t += T) out[t] = (float)((double)acc[t] * inv_norm);
+}
+
+// Divisor Q of N for the pruned finalize: minimises N log2 Q + cc_size N / Q
+// (transform work + lag sums) over lengths the in-CTA FFT supports, with
+// Q <= 8192 (64 KB of row buffer).
+static int pruned_q(int N, int cc_size) {
+  int best = 0;
+  double best_cost = 0.0;
+  for (int q = 2; q <= 8192 && q <= N; ++q) {
+    if (N % q || !fft_length_supported(q)) continue;
+    const double cost = (double)N * std::log2((double)q) + (double)cc_size * (double)(N / q) * 4.0;
+    if (best == 0 || cost < best_cost) {
+      best = q;
+      best_cost = cost;
+    }
+  }
+  return best;
+}
+
+static int xc_finalize_pruned_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs,
+                                     int64_t stack_pitch, const fxc_xc_shape* s, float* ncf) {
+  constexpr int T = 256;
+  const int N = s->nfft;
+  const int Q = pruned_q(N, s->cc_size);
+  FXC_CHECK_ARG(Q > 0, "nfft %d has no supported divisor for the pruned finalize", N);
+  FXC_CHECK_ARG(s->cc_size <= 16384, "cc_size %d above 16384", s->cc_size);
+  const float2* twn = nullptr;
+  FXC_TRY(fft_twiddles(N, &twn));
+  FftPlan pq;
+  FXC_TRY(fft_make_plan(Q, twn, N / Q, &pq));
+  const double inv_norm = 1.0 / (double)((float)N * s->dt);
+  const size_t smem =
+      sizeof(float2) * ((size_t)Q + fft_tw_smem_elems(pq)) + sizeof(float) * (size_t)s->cc_size;
+  FXC_TRY(set_smem_limit(k_xc_finalize_pruned<T>, smem));
+  k_xc_finalize_pruned<T><<<(unsigned)npairs, T, smem, ctx->stream>>>(stack, stack_pitch, pq, N, s->half_cc,
+                                                                       s->cc_size, inv_norm, ncf);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
 int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin,
                     int nchan, int nspec, int64_t spec_pitch, const uint8_t* mask, float scale,
                     float2* stack, int64_t stack_pitch, int method) {
@@ -331,14 +427,23 @@ int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, 
   return FXC_OK;
 }
 
+// Lengths the one-CTA FFT also covers use the full transform unless
+// FXC_FINALIZE=pruned selects the pruned form.
+static bool xc_finalize_prefers_pruned(int N) {
+  (void)N;
+  const char* e = getenv("FXC_FINALIZE");
+  return e && !strcmp(e, "pruned");
+}
+
 int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_t stack_pitch,
                        const fxc_xc_shape* s, float* ncf) {
   if (npairs == 0) return FXC_OK;
   const int N = s->nfft;
   FXC_CHECK_ARG(N % 2 == 0 && N >= 2, "nfft %d must be even", N);
   const int M = N / 2;
-  FXC_CHECK_ARG(M <= kFftLargeNmax, "nfft %d above the in-CTA FFT limit %d", N, 2 * kFftLargeNmax);
   FXC_CHECK_ARG(npairs <= 0x7fffffff, "too many pairs for one launch");
+  if (M > kFftLargeNmax || xc_finalize_prefers_pruned(N))
+    return xc_finalize_pruned_launch(ctx, stack, npairs, stack_pitch, s, ncf);
   const float2* twn = nullptr;
   FXC_TRY(fft_twiddles(N, &twn));
   FftPlan p;

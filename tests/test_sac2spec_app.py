@@ -153,3 +153,45 @@ def test_sac2spec_command_line_errors(tmp_path, built_lib):
     (tmp_path / "o" / "stepack" / "old.tsv").write_text("x")
     r = subprocess.run([str(EXE), *base, "-L", "86400/3600/3600/100"], capture_output=True, text=True)
     assert r.returncode == 1 and "stepack_dir_not_empty" in r.stderr
+
+
+@pytest.mark.gpu
+def test_sac2spec_then_xc_fast_chain(tmp_path, built_lib, torch_cuda):
+    """The two drop-ins chained as fastxc runs them: sac2spec's stepack
+    output is xc_fast's input; every NCF matches the FP64 oracle run on the
+    oracle's own spectra (relative L2 1e-5)."""
+    from oracle import xc_oracle as xo
+
+    idx, series = make_inputs(tmp_path)
+    out = tmp_path / "work"
+    filt = G / "filter_d0.1_0.1-2.txt"
+    env = dict(os.environ, FASTXC_LOG_LEVEL="error")
+    r = subprocess.run([str(EXE), "-I", str(idx), "-O", str(out), "-L", f"{SAC_LEN:g}/{WIN:g}/{WIN:g}/{LAG:g}",
+                        "-B", str(filt), "-C", "3", "-W", "2/0", "-N", "3"], env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    paths = [(7, 12, 0.5, 55.5, 10.0, 190.0), (7, 31, 0.6, 66.6, 20.0, 200.0), (12, 31, 0.7, 77.7, 30.0, 210.0)]
+    formats.write_allowed_paths(tmp_path / "allowed_paths.tsv", paths)
+    r = subprocess.run([str(ROOT / "fastxc_gb300" / "bin" / "xc_fast"), "-I", str(out / "stepack"), "-P",
+                        str(tmp_path / "allowed_paths.tsv"), "-O", str(tmp_path / "ncf"), "-C", str(LAG)],
+                       env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    recs = formats.read_xcpack_dir(tmp_path / "ncf" / "xcpack")
+    assert len(recs) == 2 * 3 * 9
+    flt = so.read_filter_file(filt)
+    plan = so.make_plan(SAC_LEN, WIN, WIN, LAG, DELTA, flt, 2, 3, 0)
+    steps = list(range(plan.nstep))
+    shape = xo.finalize_shape(plan.nspec, plan.nstep, DELTA, LAG)
+    spec_cache = {}
+    for rec in recs:
+        ts = rec["timestamp"]
+        if ts not in spec_cache:
+            keys = [(ts, nsl, c) for nsl in ("0007", "0012", "0031") for c in ("BHE", "BHN", "BHZ")]
+            x = np.stack([series[k] for k in keys]).astype(np.float64)
+            sp = so.run_rows(so.windows(x, plan, steps), plan, 3)  # [step][row][nspec]
+            spec_cache[ts] = (sp, {(k[1], k[2]): i for i, k in enumerate(keys)})
+        sp, pos = spec_cache[ts]
+        s = pos[(f"{int(rec['src_id']):04d}", rec["src_component"])]
+        q = pos[(f"{int(rec['rec_id']):04d}", rec["rec_component"])]
+        ref = xo.xc_run(sp, np.array([s]), np.array([q]), 1.0 / plan.nstep, shape)[0]
+        err = np.linalg.norm(rec["data"] - ref) / np.linalg.norm(ref)
+        assert err < 1e-5, (rec["src_id"], rec["rec_id"], err)

@@ -185,3 +185,36 @@ def test_bad_arguments_raise(ctx, torch_cuda):
         PairPlan(ctx, np.array([0], np.int32), np.array([9], np.int32), 6)
     with pytest.raises(FxcError):
         ctx_shape(1, 1, 0.1, 1.0)
+
+
+@pytest.mark.parametrize("nspec,dt,lag", [(1001, 0.1, 20.0), (18523, 0.1, 100.0), (9262, 0.2, 200.0)])
+def test_pruned_finalize_matches_oracle(ctx, torch_cuda, nspec, dt, lag, monkeypatch):
+    """The output-pruned finalize (P length-Q transforms + per-lag sums) on
+    lengths the one-CTA transform also covers."""
+    rng = np.random.default_rng(31)
+    nwin, nsta = 4, 3
+    spec = make_spec(rng, nwin, 3 * nsta, nspec)
+    src, rec = station_pairs(nsta)
+    shape = ctx_shape(nspec, nwin, dt, lag)
+    full, _ = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin)
+    monkeypatch.setenv("FXC_FINALIZE", "pruned")
+    pruned, _ = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin)
+    monkeypatch.delenv("FXC_FINALIZE")
+    ref = xo.xc_run(spec, src, rec, 1.0 / nwin, xo.finalize_shape(nspec, nwin, dt, lag))
+    assert per_row_rel_l2(pruned, ref).max() < NCF_RTOL
+    assert per_row_rel_l2(full, ref).max() < NCF_RTOL
+
+
+@pytest.mark.parametrize("method", [0, 1], ids=["plain", "tensor"])
+def test_20hz_long_transform(ctx, torch_cuda, method):
+    """delta 0.05 s, 3600-s windows, lag 200 s: nfft 76 000-class transforms
+    (nspec 37 045 here, nfft 74 088) above the one-CTA FFT limit, 8001 lags."""
+    rng = np.random.default_rng(32)
+    nwin, nsta, nspec = 3, 2, 37045
+    spec = make_spec(rng, nwin, 3 * nsta, nspec)
+    src, rec = station_pairs(nsta, auto=True)
+    shape = ctx_shape(nspec, nwin, 0.05, 200.0)
+    assert shape.cc_size == 8001 and shape.nfft == 74088
+    got, _ = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin, method=method)
+    ref = xo.xc_run(spec, src, rec, 1.0 / nwin, xo.finalize_shape(nspec, nwin, 0.05, 200.0))
+    assert per_row_rel_l2(got, ref).max() < NCF_RTOL
