@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--nspec", type=int, default=NSPEC, help="smaller values only for profiling runs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-slots", type=int, default=4)
     return ap.parse_args()
 
 
@@ -188,6 +191,39 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "pair-windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def serving_run(args, device: int, rank: int) -> dict:
+    """Poisson stream of correlation jobs (mean args.serve_rate per s for
+    args.serve_seconds): subarrays of 2-200 stations from a 1000-station
+    pool x 1-30 days, delta 0.05/0.1/0.2 s, lag 50-200 s, 10% with PWS;
+    synthetic station-day spectra resident in HBM across jobs."""
+    from fastxc_gb300.serve import Server, poisson_stream
+
+    srv = Server(device=device, slots=args.serve_slots, cache_gib=48.0, work_gib=150.0, chunk_gib=6.0,
+                 synthetic=True, seed=rank, max_wait_s=2.0, keep_results=True)
+    try:
+        # warm-up: geometry, FFT tables and pair plans of each delta
+        for d in (0.05, 0.1, 0.2):
+            jid = srv.submit(np.arange(4, dtype=np.int32), 0, 1, d, 100.0)
+            srv.wait(jid)
+            srv.release(jid)
+        recs, wall = poisson_stream(srv, args.serve_seconds, args.serve_rate, seed=100 + rank)
+        st = srv.stats()
+    finally:
+        srv.close()
+    lat = np.array([r["latency"] for r in recs]) if recs else np.zeros(1)
+    qw = np.array([r["queue"] for r in recs]) if recs else np.zeros(1)
+    pwin = float(sum(r["pair_windows"] for r in recs))
+    return {"jobs": len(recs), "arrival_rate_per_s": args.serve_rate, "arrival_seconds": args.serve_seconds,
+            "slots": args.serve_slots, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "mean_queue_s": float(qw.mean()),
+            "max_latency_s": float(lat.max()), "pair_windows": pwin,
+            "pair_windows_per_s": pwin / wall if wall > 0 else None, "makespan_s": wall,
+            "pws_jobs": int(sum(r["pws"] for r in recs)), "cache_entries_end": int(st.cache_entries),
+            "latency": "submit -> NCFs (and PWS) in host memory, steady clock",
+            "workload": "jobs: 2-200 of 1000 stations x 1-30 days, delta 0.05/0.1/0.2 s, lag 50-200 s, "
+                        "10% PWS; win 3600 s; synthetic seeded spectra cached in HBM"}
 
 
 def profile_traffic(kernel: str, workload: str):
@@ -436,6 +472,17 @@ def main():
         line["e2e"] = {"value": pw * world / el, "unit": "pair-windows/s",
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps}
+
+    if args.serve_seconds > 0:
+        # serving: a Poisson stream of correlation jobs against the engine
+        # (its own HBM arenas; the step's buffers are released first)
+        d_stack = d_packed = d_ncf = spec = mask = None
+        host_spec = host_ncf = hs = hn = None
+        plan = None
+        ctx.close()
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        line["serving"] = serving_run(args, local, rank)
 
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample = cpu_baseline(seconds_target=12.0, threads=1)

@@ -187,3 +187,46 @@ _SIGNATURES.update({
     "fxc_pws_run": (_int, [_vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _f32, _vp]),
     "fxc_tfpws_run": (_int, [_vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _f32, _i32, _f32, _f32, _f32, _f32, _vp]),
 })
+
+
+class ServerConfig(C.Structure):
+    """fxc_server_config (include/fastxc_gb300.h)."""
+
+    _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("cache_gib", C.c_double), ("work_gib", C.c_double),
+                ("chunk_gib", C.c_double), ("synthetic", C.c_int32), ("seed", C.c_uint64), ("win_len", C.c_float),
+                ("lag_max", C.c_float), ("max_wait_s", C.c_double), ("keep_results", C.c_int32)]
+
+
+class Job(C.Structure):
+    """fxc_job."""
+
+    _fields_ = [("stations", C.POINTER(C.c_int32)), ("nsta", C.c_int32), ("day0", C.c_int32), ("ndays", C.c_int32),
+                ("delta", C.c_float), ("lag", C.c_float), ("method", C.c_int32), ("pws", C.c_int32),
+                ("pws_power", C.c_float)]
+
+
+class JobInfo(C.Structure):
+    """fxc_job_info."""
+
+    _fields_ = [("npairs", C.c_int64), ("cc_size", C.c_int64), ("nspec", C.c_int64), ("pair_windows", C.c_int64),
+                ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double), ("status", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    """fxc_server_stats_t."""
+
+    _fields_ = [("jobs_done", C.c_int64), ("pair_windows", C.c_int64), ("queued", C.c_int64),
+                ("cache_entries", C.c_int64), ("cache_used_bytes", C.c_int64), ("work_used_bytes", C.c_int64)]
+
+
+_SIGNATURES.update({
+    "fxc_server_create": (_int, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "fxc_server_destroy": (_int, [_vp]),
+    "fxc_server_geometry": (_int, [_vp, _f32, C.POINTER(_i32), C.POINTER(_i32)]),
+    "fxc_server_put_spectra": (_int, [_vp, _i32, _i32, _f32, _vp]),
+    "fxc_server_submit": (_int, [_vp, C.POINTER(Job), C.POINTER(_i64)]),
+    "fxc_server_wait": (_int, [_vp, _i64, C.POINTER(JobInfo)]),
+    "fxc_server_fetch": (_int, [_vp, _i64, _vp, _vp]),
+    "fxc_server_release": (_int, [_vp, _i64]),
+    "fxc_server_stats": (_int, [_vp, C.POINTER(ServerStats)]),
+})

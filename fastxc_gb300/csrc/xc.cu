@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256, 1)
     k_xc_stack_plain(const float2* __restrict__ spec, int64_t nwin, int nchan, int nspec,
                      int64_t spec_pitch, const uint8_t* __restrict__ mask,
                      const XcTile* __restrict__ tiles, const int32_t* __restrict__ maps,
-                     float scale, float2* __restrict__ stack, int64_t stack_pitch) {
+                     float scale, float2* __restrict__ stack, int64_t stack_pitch, int accumulate) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2* sm = reinterpret_cast<float2*>(smraw);
   uint8_t* smask = smraw + sizeof(float2) * kXcSlots * kXcSlotElems;
@@ -268,8 +268,16 @@ __global__ void __launch_bounds__(256, 1)
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int32_t p = __ldg(map + (qa * 8 + i) * kXcTile + qb * 8 + j);
-      if (p >= 0)
-        stack[(int64_t)p * stack_pitch + f] = make_float2(acc[i][j].x * scale, acc[i][j].y * scale);
+      if (p >= 0) {
+        float2* dst = stack + (int64_t)p * stack_pitch + f;
+        float2 v = make_float2(acc[i][j].x * scale, acc[i][j].y * scale);
+        if (accumulate) {
+          const float2 o = *dst;
+          v.x += o.x;
+          v.y += o.y;
+        }
+        *dst = v;
+      }
     }
 }
 
@@ -401,11 +409,11 @@ static int xc_finalize_pruned_launch(fxc_ctx* ctx, const float2* stack, int64_t 
 
 int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin,
                     int nchan, int nspec, int64_t spec_pitch, const uint8_t* mask, float scale,
-                    float2* stack, int64_t stack_pitch, int method) {
+                    float2* stack, int64_t stack_pitch, int method, int accumulate) {
   if (plan->npairs == 0 || nspec == 0) return FXC_OK;
   if (method == FXC_XC_TENSOR) return xc_stack_tensor_launch(ctx, plan, spec, nwin, nchan, nspec,
                                                              spec_pitch, mask, scale, stack,
-                                                             stack_pitch);
+                                                             stack_pitch, accumulate);
   FXC_CHECK_ARG(method == FXC_XC_PLAIN, "unknown xc method %d", method);
   const int64_t nchunks = ceil_div(nspec, kXcFreqChunk);
   FXC_CHECK_ARG(nchunks <= 65535, "nspec %d too large for the grid", nspec);
@@ -415,12 +423,12 @@ int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, 
     FXC_TRY(set_smem_limit(k_xc_stack_plain<true>, smem));
     k_xc_stack_plain<true><<<grid, 256, smem, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch,
                                                              mask, plan->d_tiles, plan->d_maps,
-                                                             scale, stack, stack_pitch);
+                                                             scale, stack, stack_pitch, accumulate);
   } else {
     FXC_TRY(set_smem_limit(k_xc_stack_plain<false>, smem));
     k_xc_stack_plain<false><<<grid, 256, smem, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch,
                                                               mask, plan->d_tiles, plan->d_maps,
-                                                              scale, stack, stack_pitch);
+                                                              scale, stack, stack_pitch, accumulate);
   }
   count_launch();
   FXC_LAUNCH_CHECK();

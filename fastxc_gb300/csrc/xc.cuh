@@ -40,7 +40,7 @@ namespace fxc {
 
 int xc_stack_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin,
                     int nchan, int nspec, int64_t spec_pitch, const uint8_t* mask, float scale,
-                    float2* stack, int64_t stack_pitch, int method);
+                    float2* stack, int64_t stack_pitch, int method, int accumulate = 0);
 int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
                               int64_t stack_pitch, const fxc_xc_shape* s, const float2* twn,
                               const int* perm, float* ncf);
@@ -49,6 +49,14 @@ int xc_tensor_plan_init(fxc_ctx* ctx, fxc_pairplan* plan);
 void xc_tensor_plan_free(fxc_pairplan* plan);
 int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
                            int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
-                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch);
+                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch,
+                           int accumulate = 0);
+int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, int nspec,
+                   int64_t spec_pitch, const uint8_t* mask, uint4* packed);
+int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
+                   int nspec, float scale, float2* stack, int64_t stack_pitch, int accumulate = 0);
+int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec);
+int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_t stack_pitch,
+                       const fxc_xc_shape* s, float* ncf);
 
 }  // namespace fxc

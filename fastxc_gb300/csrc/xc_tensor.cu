@@ -364,7 +364,7 @@ __device__ __forceinline__ void tmem_ld_wait() {
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_xc_tc_gemm(const uint4* __restrict__ packed, int nkb, int cpad,
                  const TcTile* __restrict__ tiles, const int32_t* __restrict__ maps, int nspec,
-                 float scale, float2* __restrict__ stack, int64_t stack_pitch,
+                 float scale, float2* __restrict__ stack, int64_t stack_pitch, int accumulate,
                  int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* stage_base = smem;
@@ -541,7 +541,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const bool rev = v < -1;
               const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
               const float im_s = rev ? -im[j] : im[j];
-              stack[p * stack_pitch + f] = make_float2(re[j] * scale, im_s * scale);
+              float2* dst = stack + p * stack_pitch + f;
+              float2 v = make_float2(re[j] * scale, im_s * scale);
+              if (accumulate) {
+                const float2 o = *dst;
+                v.x += o.x;
+                v.y += o.y;
+              }
+              *dst = v;
             }
           }
         }
@@ -559,7 +566,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   (void)nspec;
 }
 
-static int64_t packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
+int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
   const int64_t nkb = (nwin + kTcKb - 1) / kTcKb;
   return (int64_t)nspec * kTcPlanes * nkb * kTcKc * round_up(nchan, 8);
 }
@@ -581,13 +588,14 @@ int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, in
 }
 
 int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
-                   int nspec, float scale, float2* stack, int64_t stack_pitch) {
+                   int nspec, float scale, float2* stack, int64_t stack_pitch, int accumulate) {
   const XcTensorPlan* tp = plan->tensor;
   FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
   if (tp->ntiles == 0 || nspec == 0) return FXC_OK;
   FXC_CHECK_ARG(nspec <= 65535, "nspec %d above the tensor grid limit", nspec);
   const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
   if (nkb == 0) {
+    if (accumulate) return FXC_OK;
     // no windows: every stacked bin is zero
     FXC_CUDA_TRY(cudaMemset2DAsync(stack, sizeof(float2) * (size_t)stack_pitch, 0,
                                    sizeof(float2) * (size_t)nspec, (size_t)plan->npairs,
@@ -597,7 +605,8 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
   FXC_TRY(set_smem_limit(k_xc_tc_gemm, kTcSmemBytes));
   dim3 gg((unsigned)tp->ntiles, (unsigned)nspec);
   k_xc_tc_gemm<<<gg, kTcThreads, kTcSmemBytes, ctx->stream>>>(
-      packed, nkb, tp->cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, ctx->d_err);
+      packed, nkb, tp->cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, accumulate,
+      ctx->d_err);
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;
@@ -605,15 +614,16 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
 
 int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
                            int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
-                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch) {
+                           const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch,
+                           int accumulate) {
   const XcTensorPlan* tp = plan->tensor;
   FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
   if (tp->ntiles == 0) return FXC_OK;
-  const int64_t chunks = packed_chunks(nchan, nwin, nspec);
+  const int64_t chunks = xc_packed_chunks(nchan, nwin, nspec);
   if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
   uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
   FXC_TRY(xc_pack_launch(ctx, spec, nwin, nchan, nspec, spec_pitch, mask, packed));
-  return xc_gemm_launch(ctx, plan, packed, nwin, nspec, scale, stack, stack_pitch);
+  return xc_gemm_launch(ctx, plan, packed, nwin, nspec, scale, stack, stack_pitch, accumulate);
 }
 
 }  // namespace fxc
@@ -626,7 +636,7 @@ int fxc_xc_packed_bytes(int32_t nchan, int64_t nwin, int32_t nspec, int64_t* out
   clear_error();
   FXC_CHECK_ARG(out_bytes != nullptr, "out_bytes is null");
   FXC_CHECK_ARG(nchan > 0 && nwin >= 0 && nspec >= 0, "invalid shape");
-  *out_bytes = packed_chunks(nchan, nwin, nspec) * 16;
+  *out_bytes = xc_packed_chunks(nchan, nwin, nspec) * 16;
   return FXC_OK;
 }
 

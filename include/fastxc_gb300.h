@@ -272,6 +272,71 @@ int fxc_tfpws_run(fxc_ctx *ctx, const float *d_groups, const float *d_weights,
                   const float *d_linear, int32_t nsamples, float delta, int32_t band_limited,
                   float fmin, float fmax, float taper_hz, float power, float *d_out);
 
+/* ---- serving: correlation jobs over resident station spectra ------------
+ * No counterpart in the reference (its stages are batch executables). A
+ * server owns one device, `slots` concurrent job slots (each a host thread,
+ * a CUDA stream and a context), an HBM arena of station-day spectra
+ * ([nstep][3 components][nspec] complex per station-day, LRU-evicted when
+ * no running job holds them) and an HBM arena of job working memory. Queued
+ * jobs are admitted first-fit by free working memory as slots free up (a job
+ * older than max_wait_s is not overtaken); admitted jobs run concurrently.
+ * A job: every cross-station component pair (9 per station pair, stations
+ * in the given order, src = the earlier station) of `nsta` stations over
+ * days [day0, day0 + ndays): the mean of the per-window cross spectra, the
+ * +-lag NCF (fxc_xc_finalize), and with pws != 0 also a phase-weighted
+ * stack of the per-day NCFs (fxc_pws_run, weight power pws_power). Spectra
+ * geometry per delta follows the sac2spec planning of a day-long record
+ * with win_len-second windows (shift = win_len) and lag_max. With
+ * synthetic != 0 a missing station-day is generated from a seeded hash (a
+ * pure function of seed, station, day, delta); otherwise it must be put
+ * first. Results of a job depend only on the job and its spectra, not on
+ * which other jobs run beside it. */
+typedef struct fxc_server fxc_server;
+typedef struct fxc_server_config {
+  int32_t device;
+  int32_t slots;        /* concurrent jobs */
+  double cache_gib;     /* spectra arena */
+  double work_gib;      /* job working-memory arena (admission budget) */
+  double chunk_gib;     /* gathered spectra per stacking pass */
+  int32_t synthetic;
+  uint64_t seed;
+  float win_len;        /* seconds */
+  float lag_max;        /* seconds; largest lag a job may ask for */
+  double max_wait_s;    /* <= 0: no anti-starvation bound */
+  int32_t keep_results; /* copy NCFs to host memory for fxc_server_fetch */
+} fxc_server_config;
+typedef struct fxc_job {
+  const int32_t *stations;
+  int32_t nsta;
+  int32_t day0, ndays;
+  float delta;          /* sampling interval of the spectra, s */
+  float lag;            /* NCF half length, s */
+  int32_t method;       /* FXC_XC_PLAIN or FXC_XC_TENSOR */
+  int32_t pws;
+  float pws_power;
+} fxc_job;
+typedef struct fxc_job_info {
+  int64_t npairs, cc_size, nspec, pair_windows;
+  double submit_s, start_s, end_s; /* host steady clock: queued, admitted, results on the host */
+  int32_t status;
+} fxc_job_info;
+typedef struct fxc_server_stats_t {
+  int64_t jobs_done, pair_windows, queued, cache_entries, cache_used_bytes, work_used_bytes;
+} fxc_server_stats_t;
+int fxc_server_create(const fxc_server_config *cfg, fxc_server **out);
+int fxc_server_destroy(fxc_server *s);
+/* nspec and windows per day of the spectra at this delta */
+int fxc_server_geometry(fxc_server *s, float delta, int32_t *nspec, int32_t *nstep);
+/* h_spec: [nstep][3][nspec] complex of one station-day */
+int fxc_server_put_spectra(fxc_server *s, int32_t station, int32_t day, float delta, const float *h_spec);
+int fxc_server_submit(fxc_server *s, const fxc_job *job, int64_t *job_id);
+/* blocks until the job is done (or failed) */
+int fxc_server_wait(fxc_server *s, int64_t job_id, fxc_job_info *info);
+/* h_ncf / h_pws: [npairs][cc_size]; either may be null */
+int fxc_server_fetch(fxc_server *s, int64_t job_id, float *h_ncf, float *h_pws);
+int fxc_server_release(fxc_server *s, int64_t job_id);
+int fxc_server_stats(fxc_server *s, fxc_server_stats_t *out);
+
 /* Allocation-free variant of fxc_xc_run. No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc (a host framework that
  * owns all device memory through its own pool, or a job whose device
