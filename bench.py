@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-wait-limit", type=float, default=240.0)
     return ap.parse_args()
 
 
@@ -206,9 +207,10 @@ def serving_run(args, device: int, rank: int) -> dict:
         # warm-up: geometry, FFT tables and pair plans of each delta
         for d in (0.05, 0.1, 0.2):
             jid = srv.submit(np.arange(4, dtype=np.int32), 0, 1, d, 100.0)
-            srv.wait(jid)
+            srv.wait(jid, timeout_s=120.0)
             srv.release(jid)
-        recs, wall = poisson_stream(srv, args.serve_seconds, args.serve_rate, seed=100 + rank)
+        recs, wall, failures = poisson_stream(srv, args.serve_seconds, args.serve_rate, seed=100 + rank,
+                                              wait_limit_s=args.serve_wait_limit)
         st = srv.stats()
     finally:
         srv.close()
@@ -221,6 +223,7 @@ def serving_run(args, device: int, rank: int) -> dict:
             "max_latency_s": float(lat.max()), "pair_windows": pwin,
             "pair_windows_per_s": pwin / wall if wall > 0 else None, "makespan_s": wall,
             "pws_jobs": int(sum(r["pws"] for r in recs)), "cache_entries_end": int(st.cache_entries),
+            "failed_jobs": len(failures), "failures": failures[:3],
             "latency": "submit -> NCFs (and PWS) in host memory, steady clock",
             "workload": "jobs: 2-200 of 1000 stations x 1-30 days, delta 0.05/0.1/0.2 s, lag 50-200 s, "
                         "10% PWS; win 3600 s; synthetic seeded spectra cached in HBM"}

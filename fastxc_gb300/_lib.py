@@ -225,7 +225,7 @@ _SIGNATURES.update({
     "fxc_server_geometry": (_int, [_vp, _f32, C.POINTER(_i32), C.POINTER(_i32)]),
     "fxc_server_put_spectra": (_int, [_vp, _i32, _i32, _f32, _vp]),
     "fxc_server_submit": (_int, [_vp, C.POINTER(Job), C.POINTER(_i64)]),
-    "fxc_server_wait": (_int, [_vp, _i64, C.POINTER(JobInfo)]),
+    "fxc_server_wait": (_int, [_vp, _i64, C.c_double, C.POINTER(JobInfo)]),
     "fxc_server_fetch": (_int, [_vp, _i64, _vp, _vp]),
     "fxc_server_release": (_int, [_vp, _i64]),
     "fxc_server_stats": (_int, [_vp, C.POINTER(ServerStats)]),

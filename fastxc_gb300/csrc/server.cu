@@ -177,6 +177,17 @@ struct Entry {
   cudaEvent_t last = nullptr;   // recorded after the last use
 };
 
+// Working-memory layout of a job (byte offsets into its work block). Linear
+// jobs: one pair plan over all pairs, K days gathered per pass, the stack
+// accumulated over passes. PWS jobs: pairs in blocks of `blk` whose per-day
+// NCFs (all days) fit the block budget; every block gathers each day again.
+struct Layout {
+  int K = 1;
+  int64_t blk = 0;
+  size_t chunk = 0, packed = 0, stack = 0, ncf = 0, ptrs = 0, traces = 0, groups = 0, wts = 0, lin = 0, out = 0;
+  size_t total = 0;
+};
+
 struct Job {
   int64_t id = 0;
   fxc_job desc{};
@@ -187,6 +198,7 @@ struct Job {
   int64_t npairs = 0;
   size_t work_bytes = 0;
   size_t entry_bytes = 0;
+  Layout layout;
   // state
   int status = 0;  // 0 queued, 1 running, 2 done, < 0 error code
   std::string error;
@@ -221,6 +233,7 @@ struct fxc_server {
   std::map<int64_t, Job*> jobs;
   int64_t next_id = 1;
   int free_slots = 0;
+  int waiters = 0;
   bool stop = false;
   std::vector<std::thread> threads;
   std::vector<fxc_ctx*> ctxs;
@@ -338,6 +351,75 @@ void unpin_entries(fxc_server* s, const std::vector<EntryKey>& keys, cudaStream_
     if (_rc != FXC_OK) return _rc; \
   } while (0)
 
+size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+Layout job_layout(const Job* j, double pws_block_gib) {
+  Layout L;
+  const int nsta = (int)j->stations.size(), nchan = 3 * nsta, D = j->desc.ndays;
+  const bool pws = j->desc.pws != 0;
+  const size_t cc = (size_t)j->cc_size, pitch = (size_t)xc_stack_pitch(j->nspec);
+  L.K = pws ? 1 : j->kdays;
+  L.blk = j->npairs;
+  if (pws) {
+    const double per_pair = (double)D * cc * 8 + (double)D * 4 + (double)cc * 12 + (double)pitch * 8;
+    L.blk = std::max<int64_t>(1, std::min<int64_t>(65535, (int64_t)(pws_block_gib * 1073741824.0 / per_pair)));
+    L.blk = std::min<int64_t>(L.blk, j->npairs);
+  }
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += al256(bytes);
+    return o;
+  };
+  L.chunk = take((size_t)L.K * j->nstep * nchan * j->nspec * 8);
+  L.packed = take(j->desc.method == FXC_XC_TENSOR ? (size_t)xc_packed_chunks(nchan, (int64_t)L.K * j->nstep, j->nspec) * 16 : 0);
+  L.stack = take((size_t)L.blk * pitch * 8);
+  L.ncf = take((size_t)L.blk * cc * 4);
+  L.ptrs = take((size_t)L.K * nsta * sizeof(void*));
+  if (pws) {
+    L.traces = take((size_t)L.blk * D * cc * 4);
+    L.groups = take((size_t)L.blk * D * cc * 4);
+    L.wts = take((size_t)L.blk * D * 4);
+    L.lin = take((size_t)L.blk * cc * 4);
+    L.out = take((size_t)L.blk * cc * 4);
+  }
+  L.total = off;
+  return L;
+}
+
+// Gathers days [day, day + nd) of the job's stations into `chunk`.
+int gather_days(fxc_server* s, Job* j, int day, int nd, cudaStream_t st, const float2** d_ptrs, float2* chunk) {
+  std::vector<const float2*> ptrs;
+  std::vector<EntryKey> keys;
+  {
+    std::unique_lock<std::mutex> lk(s->mu);
+    int rc;
+    // the cache may be full of entries other running jobs hold: wait for them
+    while ((rc = pin_entries(s, j, day, nd, st, &ptrs, &keys)) == FXC_ERR_NOMEM && !s->stop)
+      s->cv.wait_for(lk, std::chrono::milliseconds(2));
+    JOB_TRY(rc);
+  }
+  const int nsta = (int)j->stations.size();
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
+  const int64_t rows = (int64_t)nd * j->nstep * 3 * nsta;
+  k_gather_spectra<<<(unsigned)std::min<int64_t>(rows, 152 * 64), 256, 0, st>>>(d_ptrs, nsta, nd, j->nstep, j->nspec,
+                                                                               chunk);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    unpin_entries(s, keys, st);
+  }
+  // the host pointer table must outlive the upload
+  FXC_CUDA_TRY(cudaStreamSynchronize(st));
+  return FXC_OK;
+}
+
+struct PlanGuard {
+  fxc_pairplan* p = nullptr;
+  ~PlanGuard() { fxc_pairplan_destroy(p); }
+};
+
 int run_job(fxc_server* s, int slot, Job* j, char* work) {
   fxc_ctx* ctx = s->ctxs[slot];
   cudaStream_t st = s->streams[slot];
@@ -346,10 +428,17 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
   const int D = j->desc.ndays;
   const int nspec = j->nspec, nstep = j->nstep;
   const int64_t pitch = xc_stack_pitch(nspec);
-  const bool pws = j->desc.pws != 0;
   const int method = j->desc.method;
-  // pair list: station pairs s < t in job order, components i, j
+  const Layout& L = j->layout;
+  float2* chunk = reinterpret_cast<float2*>(work + L.chunk);
+  uint4* packed = reinterpret_cast<uint4*>(work + L.packed);
+  float2* stack = reinterpret_cast<float2*>(work + L.stack);
+  float* ncf = reinterpret_cast<float*>(work + L.ncf);
+  const float2** d_ptrs = reinterpret_cast<const float2**>(work + L.ptrs);
+  // pair list: station pairs a < b in job order, components i, j
   std::vector<int32_t> src, rec;
+  src.reserve((size_t)j->npairs);
+  rec.reserve((size_t)j->npairs);
   for (int a = 0; a < nsta; ++a)
     for (int b = a + 1; b < nsta; ++b)
       for (int ci = 0; ci < 3; ++ci)
@@ -357,133 +446,68 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
           src.push_back(3 * a + ci);
           rec.push_back(3 * b + cj);
         }
-  fxc_pairplan* plan = nullptr;
-  JOB_TRY(fxc_pairplan_create(ctx, src.data(), rec.data(), (int64_t)src.size(), nchan, &plan));
-  struct PlanGuard {
-    fxc_pairplan* p;
-    ~PlanGuard() { fxc_pairplan_destroy(p); }
-  } guard{plan};
-  const int K = pws ? 1 : j->kdays;
-  // work layout: chunk | packed | stack | ncf | (pws: traces, groups, weights, linear, out)
-  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  const size_t chunk_b = (size_t)K * nstep * nchan * nspec * 8;
-  const size_t packed_b = method == FXC_XC_TENSOR ? (size_t)xc_packed_chunks(nchan, (int64_t)K * nstep, nspec) * 16 : 0;
-  const size_t stack_b = (size_t)j->npairs * pitch * 8;
-  const size_t ncf_b = (size_t)j->npairs * j->cc_size * 4;
-  char* p = work;
-  float2* chunk = reinterpret_cast<float2*>(p);
-  p += al(chunk_b);
-  uint4* packed = reinterpret_cast<uint4*>(p);
-  p += al(packed_b);
-  float2* stack = reinterpret_cast<float2*>(p);
-  p += al(stack_b);
-  float* ncf = reinterpret_cast<float*>(p);
-  p += al(ncf_b);
-  float* traces = nullptr;
-  if (pws) {
-    traces = reinterpret_cast<float*>(p);
-    p += al((size_t)j->npairs * D * j->cc_size * 4);
+  const size_t cc = (size_t)j->cc_size;
+  if (s->cfg.keep_results) {
+    j->ncf.resize((size_t)j->npairs * cc);
+    if (j->desc.pws) j->pws.resize((size_t)j->npairs * cc);
   }
-  const float2** d_ptrs = reinterpret_cast<const float2**>(p);
-  p += al((size_t)K * nsta * sizeof(void*));
-  std::vector<const float2*> ptrs;
-  std::vector<EntryKey> keys;
-  const float scale_all = 1.0f / (float)(D * nstep);
-  for (int d0 = 0; d0 < D; d0 += K) {
-    const int nd = std::min(K, D - d0);
-    {
-      std::unique_lock<std::mutex> lk(s->mu);
-      int rc;
-      // the cache may be full of entries other running jobs hold: wait for one to finish
-      while ((rc = pin_entries(s, j, j->desc.day0 + d0, nd, st, &ptrs, &keys)) == FXC_ERR_NOMEM && !s->stop)
-        s->cv.wait_for(lk, std::chrono::milliseconds(2));
-      JOB_TRY(rc);
+  if (!j->desc.pws) {
+    PlanGuard pg;
+    JOB_TRY(fxc_pairplan_create(ctx, src.data(), rec.data(), j->npairs, nchan, &pg.p));
+    const float scale = 1.0f / (float)(D * nstep);
+    for (int d0 = 0; d0 < D; d0 += L.K) {
+      const int nd = std::min(L.K, D - d0);
+      JOB_TRY(gather_days(s, j, j->desc.day0 + d0, nd, st, d_ptrs, chunk));
+      const int64_t nwin = (int64_t)nd * nstep;
+      if (method == FXC_XC_TENSOR) {
+        JOB_TRY(xc_pack_launch(ctx, chunk, nwin, nchan, nspec, nspec, nullptr, packed));
+        JOB_TRY(xc_gemm_launch(ctx, pg.p, packed, nwin, nspec, scale, stack, pitch, d0 > 0));
+      } else {
+        JOB_TRY(xc_stack_launch(ctx, pg.p, chunk, nwin, nchan, nspec, nspec, nullptr, scale, stack, pitch, method,
+                                d0 > 0));
+      }
     }
-    FXC_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
-    const int64_t nwin = (int64_t)nd * nstep;
-    const int rows = (int)std::min<int64_t>(nwin * nchan, 152 * 64);
-    k_gather_spectra<<<rows, 256, 0, st>>>(d_ptrs, nsta, nd, nstep, nspec, chunk);
-    count_launch();
-    FXC_LAUNCH_CHECK();
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      unpin_entries(s, keys, st);
-    }
-    // the host copy of the pointer table must outlive the async upload
-    FXC_CUDA_TRY(cudaStreamSynchronize(st));
-    if (pws) {
-      // per-day stack -> per-day NCF (trace d of every pair)
-      JOB_TRY(xc_stack_launch(ctx, plan, chunk, nwin, nchan, nspec, nspec, nullptr, 1.0f / (float)nstep, stack,
-                              pitch, method, 0));
-      JOB_TRY(xc_finalize_launch(ctx, stack, j->npairs, pitch, &j->shape, ncf));
-      FXC_CUDA_TRY(cudaMemcpy2DAsync(traces + (size_t)d0 * j->cc_size, (size_t)D * j->cc_size * 4, ncf,
-                                     (size_t)j->cc_size * 4, (size_t)j->cc_size * 4, (size_t)j->npairs,
-                                     cudaMemcpyDeviceToDevice, st));
-    } else if (method == FXC_XC_TENSOR) {
-      JOB_TRY(xc_pack_launch(ctx, chunk, nwin, nchan, nspec, nspec, nullptr, packed));
-      JOB_TRY(xc_gemm_launch(ctx, plan, packed, nwin, nspec, scale_all, stack, pitch, d0 > 0));
-    } else {
-      JOB_TRY(xc_stack_launch(ctx, plan, chunk, nwin, nchan, nspec, nspec, nullptr, scale_all, stack, pitch,
-                              method, d0 > 0));
-    }
-  }
-  const size_t out_n = (size_t)j->npairs * j->cc_size;
-  if (pws) {
-    // linear = mean of the day NCFs (the linear stack), PWS over the days
-    char* q = p;
-    float* g2 = reinterpret_cast<float*>(q);
-    q += al((size_t)j->npairs * D * j->cc_size * 4);
-    float* wts = reinterpret_cast<float*>(q);
-    q += al((size_t)j->npairs * D * 4);
-    float* lin = reinterpret_cast<float*>(q);
-    q += al(out_n * 4);
-    float* out = reinterpret_cast<float*>(q);
-    // prestack (substack 1: group = day NCF, weight 1/D, linear = mean) and
-    // PWS in blocks of at most 65535 pairs
-    const int64_t blk = 65535;
-    std::vector<int64_t> toff((size_t)blk), goff((size_t)blk);
-    std::vector<int32_t> tcnt((size_t)blk, D), gcnt((size_t)blk);
-    for (int64_t i = 0; i < blk; ++i) toff[i] = i * D;
-    const size_t cc = (size_t)j->cc_size;
-    for (int64_t p0 = 0; p0 < j->npairs; p0 += blk) {
-      const int32_t np = (int32_t)std::min(blk, j->npairs - p0);
-      JOB_TRY(fxc_stack_prestack(ctx, traces + (size_t)p0 * D * cc, toff.data(), tcnt.data(), np, j->cc_size, 1, 0,
-                                 g2 + (size_t)p0 * D * cc, wts + (size_t)p0 * D, lin + (size_t)p0 * cc, goff.data(),
-                                 gcnt.data()));
-      JOB_TRY(fxc_pws_run(ctx, g2 + (size_t)p0 * D * cc, wts + (size_t)p0 * D, goff.data(), gcnt.data(), np,
-                          lin + (size_t)p0 * cc, j->cc_size, j->desc.pws_power, out + (size_t)p0 * cc));
-    }
-    if (s->cfg.keep_results) {
-      j->ncf.resize(out_n);
-      j->pws.resize(out_n);
-      FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data(), lin, out_n * 4, cudaMemcpyDeviceToHost, st));
-      FXC_CUDA_TRY(cudaMemcpyAsync(j->pws.data(), out, out_n * 4, cudaMemcpyDeviceToHost, st));
-    }
-  } else {
     JOB_TRY(xc_finalize_launch(ctx, stack, j->npairs, pitch, &j->shape, ncf));
-    if (s->cfg.keep_results) {
-      j->ncf.resize(out_n);
-      FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data(), ncf, out_n * 4, cudaMemcpyDeviceToHost, st));
+    if (s->cfg.keep_results)
+      FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data(), ncf, (size_t)j->npairs * cc * 4, cudaMemcpyDeviceToHost, st));
+  } else {
+    float* traces = reinterpret_cast<float*>(work + L.traces);
+    float* groups = reinterpret_cast<float*>(work + L.groups);
+    float* wts = reinterpret_cast<float*>(work + L.wts);
+    float* lin = reinterpret_cast<float*>(work + L.lin);
+    float* out = reinterpret_cast<float*>(work + L.out);
+    std::vector<int64_t> toff((size_t)L.blk), goff((size_t)L.blk);
+    std::vector<int32_t> tcnt((size_t)L.blk, D), gcnt((size_t)L.blk);
+    for (int64_t i = 0; i < L.blk; ++i) toff[i] = i * D;
+    for (int64_t p0 = 0; p0 < j->npairs; p0 += L.blk) {
+      const int64_t np = std::min<int64_t>(L.blk, j->npairs - p0);
+      PlanGuard pg;
+      JOB_TRY(fxc_pairplan_create(ctx, src.data() + p0, rec.data() + p0, np, nchan, &pg.p));
+      for (int d = 0; d < D; ++d) {
+        // per-day stack -> per-day NCF = trace d of every pair of the block
+        JOB_TRY(gather_days(s, j, j->desc.day0 + d, 1, st, d_ptrs, chunk));
+        JOB_TRY(xc_stack_launch(ctx, pg.p, chunk, nstep, nchan, nspec, nspec, nullptr, 1.0f / (float)nstep, stack,
+                                pitch, method, 0));
+        JOB_TRY(xc_finalize_launch(ctx, stack, np, pitch, &j->shape, ncf));
+        FXC_CUDA_TRY(cudaMemcpy2DAsync(traces + (size_t)d * cc, (size_t)D * cc * 4, ncf, cc * 4, cc * 4, (size_t)np,
+                                       cudaMemcpyDeviceToDevice, st));
+      }
+      // substack 1: group = day NCF (weight 1/D), linear = mean of the days
+      JOB_TRY(fxc_stack_prestack(ctx, traces, toff.data(), tcnt.data(), (int32_t)np, j->cc_size, 1, 0, groups, wts,
+                                 lin, goff.data(), gcnt.data()));
+      JOB_TRY(fxc_pws_run(ctx, groups, wts, goff.data(), gcnt.data(), (int32_t)np, lin, j->cc_size,
+                          j->desc.pws_power, out));
+      if (s->cfg.keep_results) {
+        FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data() + (size_t)p0 * cc, lin, (size_t)np * cc * 4,
+                                     cudaMemcpyDeviceToHost, st));
+        FXC_CUDA_TRY(cudaMemcpyAsync(j->pws.data() + (size_t)p0 * cc, out, (size_t)np * cc * 4,
+                                     cudaMemcpyDeviceToHost, st));
+        FXC_CUDA_TRY(cudaStreamSynchronize(st));
+      }
     }
   }
   FXC_CUDA_TRY(cudaStreamSynchronize(st));
   return ctx_check_device_error(ctx);
-}
-
-// Working-memory estimate of a job (must match run_job's layout).
-size_t job_work_bytes(const Job* j) {
-  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  const int nsta = (int)j->stations.size(), nchan = 3 * nsta, D = j->desc.ndays;
-  const bool pws = j->desc.pws != 0;
-  const int K = pws ? 1 : j->kdays;
-  const size_t out_n = (size_t)j->npairs * j->cc_size;
-  size_t b = al((size_t)K * j->nstep * nchan * j->nspec * 8);
-  if (j->desc.method == FXC_XC_TENSOR) b += al((size_t)xc_packed_chunks(nchan, (int64_t)K * j->nstep, j->nspec) * 16);
-  b += al((size_t)j->npairs * xc_stack_pitch(j->nspec) * 8);
-  b += al(out_n * 4);
-  if (pws) b += 2 * al(out_n * D * 4) + al((size_t)j->npairs * D * 4) + 2 * al(out_n * 4);
-  b += al((size_t)K * nsta * sizeof(void*));
-  return b;
 }
 
 void slot_main(fxc_server* s, int slot) {
@@ -654,7 +678,8 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
     return FXC_ERR_NOMEM;
   }
   j->kdays = std::min<int>(j->kdays, (int)(s->cache.bytes() / 2 / day_entries));
-  j->work_bytes = job_work_bytes(j);
+  j->layout = job_layout(j, s->cfg.chunk_gib);
+  j->work_bytes = j->layout.total;
   if (j->work_bytes > s->work.bytes()) {
     set_error("job needs %zu bytes of working memory, the arena holds %zu", j->work_bytes, s->work.bytes());
     delete j;
@@ -672,14 +697,26 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
   return FXC_OK;
 }
 
-int fxc_server_wait(fxc_server* s, int64_t id, fxc_job_info* info) {
+int fxc_server_wait(fxc_server* s, int64_t id, double timeout_s, fxc_job_info* info) {
   clear_error();
   FXC_CHECK_ARG(s && info, "null argument");
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->jobs.find(id);
   FXC_CHECK_ARG(it != s->jobs.end(), "unknown job %lld", (long long)id);
   Job* j = it->second;
-  s->cv.wait(lk, [&] { return j->status == 2 || j->status < 0; });
+  ++s->waiters;
+  auto done = [&] { return j->status == 2 || j->status < 0 || s->stop; };
+  bool ok = true;
+  if (timeout_s > 0)
+    ok = s->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done);
+  else
+    s->cv.wait(lk, done);
+  --s->waiters;
+  s->cv.notify_all();
+  if (!ok || (s->stop && j->status != 2 && j->status >= 0)) {
+    set_error("job %lld not finished (%s)", (long long)id, s->stop ? "server stopping" : "timeout");
+    return FXC_ERR_TIMEOUT;
+  }
   info->npairs = j->npairs;
   info->cc_size = j->cc_size;
   info->nspec = j->nspec;
@@ -746,6 +783,12 @@ int fxc_server_destroy(fxc_server* s) {
   }
   s->cv.notify_all();
   for (std::thread& t : s->threads) t.join();
+  {
+    // callers blocked in fxc_server_wait return before the jobs go away
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv.notify_all();
+    s->cv.wait(lk, [&] { return s->waiters == 0; });
+  }
   for (fxc_ctx* c : s->ctxs) fxc_ctx_destroy(c);
   for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
   for (auto& kv : s->entries) {

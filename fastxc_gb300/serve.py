@@ -46,9 +46,9 @@ class Server:
         self.L.fxc_server_submit(self.h, C.byref(job), C.byref(jid))
         return jid.value
 
-    def wait(self, jid: int) -> JobInfo:
+    def wait(self, jid: int, timeout_s: float = 0.0) -> JobInfo:
         info = JobInfo()
-        self.L.fxc_server_wait(self.h, jid, C.byref(info))
+        self.L.fxc_server_wait(self.h, jid, timeout_s, C.byref(info))
         return info
 
     def fetch(self, jid: int, info: JobInfo, pws=False):
@@ -69,10 +69,11 @@ class Server:
 
 def poisson_stream(server: Server, seconds: float, rate: float, seed: int = 0, pool: int = 1000,
                    sta_range=(2, 200), day_range=(1, 30), deltas=(0.05, 0.1, 0.2), lag_range=(50.0, 200.0),
-                   pws_frac=0.1, days_total=60, method=1):
+                   pws_frac=0.1, days_total=60, method=1, wait_limit_s=600.0):
     """Submits a Poisson stream of jobs for `seconds` (mean `rate` per s) and
-    waits for all of them. Returns (per-job records, wall seconds from the
-    first submission to the last result)."""
+    waits for all of them (each at most wait_limit_s). Returns (per-job
+    records, wall seconds from the first submission to the last result,
+    failure messages)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     plan = []
@@ -87,11 +88,17 @@ def poisson_stream(server: Server, seconds: float, rate: float, seed: int = 0, p
                          delta=float(rng.choice(deltas)), lag=float(rng.uniform(*lag_range)),
                          pws=bool(rng.random() < pws_frac)))
     records = []
+    failures = []
     lock = threading.Lock()
 
     def waiter(jid, job):
-        info = server.wait(jid)
-        server.release(jid)
+        try:
+            info = server.wait(jid, timeout_s=wait_limit_s)
+            server.release(jid)
+        except Exception as e:  # timed out or failed: reported, not raised
+            with lock:
+                failures.append(str(e))
+            return
         with lock:
             records.append(dict(latency=info.end_s - info.submit_s, queue=info.start_s - info.submit_s,
                                 pair_windows=info.pair_windows, npairs=info.npairs, delta=job["delta"],
@@ -104,12 +111,16 @@ def poisson_stream(server: Server, seconds: float, rate: float, seed: int = 0, p
         dt = job["at"] - (time.perf_counter() - t0)
         if dt > 0:
             time.sleep(dt)
-        jid = server.submit(job["stations"], job["day0"], job["ndays"], job["delta"], job["lag"], method=method,
-                            pws=job["pws"])
+        try:
+            jid = server.submit(job["stations"], job["day0"], job["ndays"], job["delta"], job["lag"], method=method,
+                                pws=job["pws"])
+        except Exception as e:
+            failures.append(f"submit: {e}")
+            continue
         th = threading.Thread(target=waiter, args=(jid, job), daemon=True)
         th.start()
         threads.append(th)
     for th in threads:
         th.join()
     wall = max(r["end"] for r in records) - min(r["submit"] for r in records) if records else 0.0
-    return records, wall
+    return records, wall, failures

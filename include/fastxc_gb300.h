@@ -330,8 +330,10 @@ int fxc_server_geometry(fxc_server *s, float delta, int32_t *nspec, int32_t *nst
 /* h_spec: [nstep][3][nspec] complex of one station-day */
 int fxc_server_put_spectra(fxc_server *s, int32_t station, int32_t day, float delta, const float *h_spec);
 int fxc_server_submit(fxc_server *s, const fxc_job *job, int64_t *job_id);
-/* blocks until the job is done (or failed) */
-int fxc_server_wait(fxc_server *s, int64_t job_id, fxc_job_info *info);
+/* blocks until the job is done or failed, or timeout_s seconds passed
+ * (timeout_s <= 0: no limit; FXC_ERR_TIMEOUT when it ran out or the server
+ * is being destroyed) */
+int fxc_server_wait(fxc_server *s, int64_t job_id, double timeout_s, fxc_job_info *info);
 /* h_ncf / h_pws: [npairs][cc_size]; either may be null */
 int fxc_server_fetch(fxc_server *s, int64_t job_id, float *h_ncf, float *h_pws);
 int fxc_server_release(fxc_server *s, int64_t job_id);

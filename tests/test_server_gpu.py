@@ -57,7 +57,7 @@ def test_job_matches_oracle(server, method):
     stations, days = [40 + method, 7, 19], [3, 4]
     spec, nspec, nstep = put_days(server, rng, stations, days, delta)
     jid = server.submit(stations, 3, 2, delta, lag, method=method)
-    info = server.wait(jid)
+    info = server.wait(jid, timeout_s=300.0)
     got = server.fetch(jid, info)
     server.release(jid)
     # oracle over the job's channels: station order of the job, both days' windows
@@ -74,7 +74,7 @@ def test_pws_job_matches_oracle(server):
     stations, days = [101, 102], [0, 1, 2]
     spec, nspec, nstep = put_days(server, rng, stations, days, delta)
     jid = server.submit(stations, 0, 3, delta, lag, method=0, pws=True, pws_power=power)
-    info = server.wait(jid)
+    info = server.wait(jid, timeout_s=300.0)
     lin, pws = server.fetch(jid, info, pws=True)
     server.release(jid)
     src, rec = job_pairs(2)
@@ -93,7 +93,7 @@ def test_same_result_alone_and_in_mix(built_lib, torch_cuda):
     try:
         a = dict(stations=[11, 3, 250, 77], day0=2, ndays=3, delta=0.1, lag=120.0, method=1)
         jid = s.submit(**a)
-        alone = s.fetch(jid, s.wait(jid))
+        alone = s.fetch(jid, s.wait(jid, timeout_s=300.0))
         s.release(jid)
         mix = [
             dict(stations=list(range(300, 330)), day0=0, ndays=2, delta=0.1, lag=200.0, method=1),
@@ -104,7 +104,7 @@ def test_same_result_alone_and_in_mix(built_lib, torch_cuda):
             a,
         ]
         ids = [s.submit(**m) for m in mix]
-        infos = [s.wait(i) for i in ids]
+        infos = [s.wait(i, timeout_s=300.0) for i in ids]
         for i in (1, 5):
             again = s.fetch(ids[i], infos[i])
             assert np.array_equal(again, alone)
