@@ -154,17 +154,18 @@ __global__ void k_synth_spectra(float2* __restrict__ out, int nstep, int nspec, 
 }
 
 // chunk[w][c][f] = entry[ent(w / nstep, c / 3)][w % nstep][c % 3][f]
+// chunk[w][c][0, fw) = entry[w / nstep][c / 3][w % nstep][c % 3][f0, f0 + fw)
 __global__ void k_gather_spectra(const float2* const* __restrict__ entries, int nsta, int ndays,
-                                 int nstep, int nspec, float2* __restrict__ chunk) {
+                                 int nstep, int nspec, int f0, int fw, float2* __restrict__ chunk) {
   const int nchan = 3 * nsta;
   const int64_t rows = (int64_t)ndays * nstep * nchan;
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     const int c = (int)(r % nchan);
     const int64_t w = r / nchan;
     const int d = (int)(w / nstep), ws = (int)(w % nstep);
-    const float2* src = entries[(int64_t)d * nsta + c / 3] + ((int64_t)ws * 3 + c % 3) * nspec;
-    float2* dst = chunk + r * nspec;
-    for (int f = threadIdx.x; f < nspec; f += blockDim.x) dst[f] = __ldg(src + f);
+    const float2* src = entries[(int64_t)d * nsta + c / 3] + ((int64_t)ws * 3 + c % 3) * nspec + f0;
+    float2* dst = chunk + r * fw;
+    for (int f = threadIdx.x; f < fw; f += blockDim.x) dst[f] = __ldg(src + f);
   }
 }
 
@@ -193,7 +194,7 @@ struct Job {
   fxc_job desc{};
   std::vector<int32_t> stations;
   // geometry
-  int nspec = 0, nstep = 0, cc_size = 0, kdays = 1;
+  int nspec = 0, nstep = 0, cc_size = 0, kdays = 1, fchunk = 0;
   fxc_xc_shape shape{};
   int64_t npairs = 0;
   size_t work_bytes = 0;
@@ -371,8 +372,9 @@ Layout job_layout(const Job* j, double pws_block_gib) {
     off += al256(bytes);
     return o;
   };
-  L.chunk = take((size_t)L.K * j->nstep * nchan * j->nspec * 8);
-  L.packed = take(j->desc.method == FXC_XC_TENSOR ? (size_t)xc_packed_chunks(nchan, (int64_t)L.K * j->nstep, j->nspec) * 16 : 0);
+  const int fw = pws ? j->nspec : j->fchunk;  // bins gathered per pass
+  L.chunk = take((size_t)L.K * j->nstep * nchan * fw * 8);
+  L.packed = take(j->desc.method == FXC_XC_TENSOR ? (size_t)xc_packed_chunks(nchan, (int64_t)L.K * j->nstep, fw) * 16 : 0);
   L.stack = take((size_t)L.blk * pitch * 8);
   L.ncf = take((size_t)L.blk * cc * 4);
   L.ptrs = take((size_t)L.K * nsta * sizeof(void*));
@@ -387,32 +389,38 @@ Layout job_layout(const Job* j, double pws_block_gib) {
   return L;
 }
 
-// Gathers days [day, day + nd) of the job's stations into `chunk`.
-int gather_days(fxc_server* s, Job* j, int day, int nd, cudaStream_t st, const float2** d_ptrs, float2* chunk) {
+// Pins days [day, day + nd) of the job's stations (filled on a miss) and
+// uploads their entry pointers to d_ptrs.
+int pin_days(fxc_server* s, Job* j, int day, int nd, cudaStream_t st, const float2** d_ptrs,
+             std::vector<EntryKey>* keys) {
   std::vector<const float2*> ptrs;
-  std::vector<EntryKey> keys;
   {
     std::unique_lock<std::mutex> lk(s->mu);
     int rc;
     // the cache may be full of entries other running jobs hold: wait for them
-    while ((rc = pin_entries(s, j, day, nd, st, &ptrs, &keys)) == FXC_ERR_NOMEM && !s->stop)
+    while ((rc = pin_entries(s, j, day, nd, st, &ptrs, keys)) == FXC_ERR_NOMEM && !s->stop)
       s->cv.wait_for(lk, std::chrono::milliseconds(2));
     JOB_TRY(rc);
   }
-  const int nsta = (int)j->stations.size();
   FXC_CUDA_TRY(cudaMemcpyAsync(d_ptrs, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, st));
-  const int64_t rows = (int64_t)nd * j->nstep * 3 * nsta;
-  k_gather_spectra<<<(unsigned)std::min<int64_t>(rows, 152 * 64), 256, 0, st>>>(d_ptrs, nsta, nd, j->nstep, j->nspec,
-                                                                               chunk);
-  count_launch();
-  FXC_LAUNCH_CHECK();
-  {
-    std::lock_guard<std::mutex> lk(s->mu);
-    unpin_entries(s, keys, st);
-  }
   // the host pointer table must outlive the upload
   FXC_CUDA_TRY(cudaStreamSynchronize(st));
   return FXC_OK;
+}
+
+int gather_bins(Job* j, int nd, int f0, int fw, cudaStream_t st, const float2** d_ptrs, float2* chunk) {
+  const int nsta = (int)j->stations.size();
+  const int64_t rows = (int64_t)nd * j->nstep * 3 * nsta;
+  k_gather_spectra<<<(unsigned)std::min<int64_t>(rows, 152 * 64), 256, 0, st>>>(d_ptrs, nsta, nd, j->nstep, j->nspec,
+                                                                               f0, fw, chunk);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+void unpin_days(fxc_server* s, const std::vector<EntryKey>& keys, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  unpin_entries(s, keys, st);
 }
 
 struct PlanGuard {
@@ -457,15 +465,25 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
     const float scale = 1.0f / (float)(D * nstep);
     for (int d0 = 0; d0 < D; d0 += L.K) {
       const int nd = std::min(L.K, D - d0);
-      JOB_TRY(gather_days(s, j, j->desc.day0 + d0, nd, st, d_ptrs, chunk));
+      std::vector<EntryKey> keys;
+      JOB_TRY(pin_days(s, j, j->desc.day0 + d0, nd, st, d_ptrs, &keys));
       const int64_t nwin = (int64_t)nd * nstep;
-      if (method == FXC_XC_TENSOR) {
-        JOB_TRY(xc_pack_launch(ctx, chunk, nwin, nchan, nspec, nspec, nullptr, packed));
-        JOB_TRY(xc_gemm_launch(ctx, pg.p, packed, nwin, nspec, scale, stack, pitch, d0 > 0));
-      } else {
-        JOB_TRY(xc_stack_launch(ctx, pg.p, chunk, nwin, nchan, nspec, nspec, nullptr, scale, stack, pitch, method,
-                                d0 > 0));
+      int rc = FXC_OK;
+      // bins in passes of fchunk: each pass stacks all windows of the pinned
+      // days for its bins into stack[:, f0 : f0 + fw)
+      for (int f0 = 0; f0 < nspec && rc == FXC_OK; f0 += j->fchunk) {
+        const int fw = std::min(j->fchunk, nspec - f0);
+        rc = gather_bins(j, nd, f0, fw, st, d_ptrs, chunk);
+        if (rc == FXC_OK && method == FXC_XC_TENSOR) {
+          rc = xc_pack_launch(ctx, chunk, nwin, nchan, fw, fw, nullptr, packed);
+          if (rc == FXC_OK) rc = xc_gemm_launch(ctx, pg.p, packed, nwin, fw, scale, stack + f0, pitch, d0 > 0);
+        } else if (rc == FXC_OK) {
+          rc = xc_stack_launch(ctx, pg.p, chunk, nwin, nchan, fw, fw, nullptr, scale, stack + f0, pitch, method,
+                               d0 > 0);
+        }
       }
+      unpin_days(s, keys, st);
+      JOB_TRY(rc);
     }
     JOB_TRY(xc_finalize_launch(ctx, stack, j->npairs, pitch, &j->shape, ncf));
     if (s->cfg.keep_results)
@@ -485,7 +503,11 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
       JOB_TRY(fxc_pairplan_create(ctx, src.data() + p0, rec.data() + p0, np, nchan, &pg.p));
       for (int d = 0; d < D; ++d) {
         // per-day stack -> per-day NCF = trace d of every pair of the block
-        JOB_TRY(gather_days(s, j, j->desc.day0 + d, 1, st, d_ptrs, chunk));
+        std::vector<EntryKey> keys;
+        JOB_TRY(pin_days(s, j, j->desc.day0 + d, 1, st, d_ptrs, &keys));
+        const int rc = gather_bins(j, 1, 0, nspec, st, d_ptrs, chunk);
+        unpin_days(s, keys, st);
+        JOB_TRY(rc);
         JOB_TRY(xc_stack_launch(ctx, pg.p, chunk, nstep, nchan, nspec, nspec, nullptr, 1.0f / (float)nstep, stack,
                                 pitch, method, 0));
         JOB_TRY(xc_finalize_launch(ctx, stack, np, pitch, &j->shape, ncf));
@@ -666,10 +688,8 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
   j->cc_size = j->shape.cc_size;
   j->npairs = 9LL * job->nsta * (job->nsta - 1) / 2;
   j->entry_bytes = (size_t)j->nstep * 3 * j->nspec * 8;
-  // days per chunk: the gathered block stays within chunk_gib
-  const double per_day = (double)j->nstep * 3 * job->nsta * j->nspec * 8 * (job->method == FXC_XC_TENSOR ? 2 : 1);
-  j->kdays = std::max(1, std::min(job->ndays, (int)(s->cfg.chunk_gib * 1073741824.0 / per_day)));
-  // one chunk's station-days are pinned together: they must fit the spectra arena
+  // days per pass: the pinned station-days of one pass stay within half the
+  // spectra arena; bins per pass: the gathered block stays within chunk_gib
   const size_t day_entries = (size_t)job->nsta * j->entry_bytes;
   if (day_entries > s->cache.bytes() / 2) {
     set_error("one day of %d stations needs %zu bytes of spectra, above half the arena (%zu)", job->nsta,
@@ -677,7 +697,12 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
     delete j;
     return FXC_ERR_NOMEM;
   }
-  j->kdays = std::min<int>(j->kdays, (int)(s->cache.bytes() / 2 / day_entries));
+  j->kdays = std::max(1, std::min<int>(job->ndays, (int)(s->cache.bytes() / 2 / day_entries)));
+  {
+    const double per_bin = (double)j->kdays * j->nstep * 3 * job->nsta * 8 * (job->method == FXC_XC_TENSOR ? 2 : 1);
+    int fc = (int)(s->cfg.chunk_gib * 1073741824.0 / per_bin) / 64 * 64;
+    j->fchunk = std::max(64, std::min(fc, j->nspec));
+  }
   j->layout = job_layout(j, s->cfg.chunk_gib);
   j->work_bytes = j->layout.total;
   if (j->work_bytes > s->work.bytes()) {
