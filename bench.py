@@ -65,9 +65,9 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from fastxc_gb300.replicas import dist_env as env
+
+    rank, world, local = env()
     return rank, world, local
 
 
@@ -266,6 +266,7 @@ def main():
     from fastxc_gb300 import lib
     from fastxc_gb300._lib import FXC_XC_PLAIN, FXC_XC_TENSOR, FxcError
     from fastxc_gb300.core import Context, PairPlan, xc_shape
+    from fastxc_gb300 import replicas
     from fastxc_gb300.synthetic import cross_station_pairs, spectra_device, station_array
 
     nspec = args.nspec
@@ -293,8 +294,12 @@ def main():
         methods["tensor"] = FXC_XC_TENSOR
     except FxcError:
         pass
+    autotune = None
     if args.method == "auto":
-        head = "tensor" if "tensor" in methods else "plain"
+        m, ms_plain, ms_tensor = ctx.xc_autotune(plan, spec, nwin, nchan, nspec, nspec)
+        head = "tensor" if m == FXC_XC_TENSOR and "tensor" in methods else "plain"
+        autotune = {"method": head, "sample_bins": min(nspec, 512), "sample_ms_plain": ms_plain,
+                    "sample_ms_tensor": ms_tensor}
     else:
         head = args.method
         if head not in methods:
@@ -351,11 +356,7 @@ def main():
         barrier()
         if name == head:
             clocks = sampler.stop()
-        total_ms = t_start.elapsed_time(t_end)
-        if world > 1:
-            t = torch.tensor([total_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms = replicas.reduce_max(t_start.elapsed_time(t_end), device=dev)
         pack_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
         kern_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
         fin_ms = statistics.mean(e[2].elapsed_time(e[3]) for e in evs)
@@ -383,7 +384,7 @@ def main():
 
     pw = npairs * nwin
     hr = results[head]
-    value = pw * world / (hr["total_ms"] / args.steps / 1e3)
+    value = replicas.whole_job_rate(pw, world, hr["total_ms"] / args.steps / 1e3)
 
     # roofline of the dominant kernel: the tcgen05 GEMM (tensor) or the plain
     # stack kernel, each timed with CUDA events on the launching stream
@@ -445,6 +446,7 @@ def main():
                            "pack_ms": v["pack_ms"], "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"]}
                        for k, v in results.items()},
         "roofline": roofline,
+        "autotune": autotune,
         "gpu_launches": hr["launches"],
         "clocks": clocks,
     }
@@ -467,12 +469,8 @@ def main():
         e2e_steps = max(1, min(args.steps, 5))
         for _ in range(e2e_steps):
             ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
-        el = (time.perf_counter() - t0) / e2e_steps
-        if world > 1:
-            t = torch.tensor([el], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
-        line["e2e"] = {"value": pw * world / el, "unit": "pair-windows/s",
+        el = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, device=dev)
+        line["e2e"] = {"value": replicas.whole_job_rate(pw, world, el), "unit": "pair-windows/s",
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps}
 

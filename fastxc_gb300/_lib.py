@@ -220,6 +220,8 @@ class ServerStats(C.Structure):
 
 
 _SIGNATURES.update({
+    "fxc_xc_autotune": (_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, C.POINTER(_i32), C.POINTER(_f32),
+                                C.POINTER(_f32)]),
     "fxc_server_create": (_int, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "fxc_server_destroy": (_int, [_vp]),
     "fxc_server_geometry": (_int, [_vp, _f32, C.POINTER(_i32), C.POINTER(_i32)]),

@@ -7,9 +7,9 @@
 // Output (native/xc/pack_io/pack_writer.cu): <ncf>/xcpack/<ts>.iAAAAAA.jBBBBBB.wWWW.pPPP.{xcpack,tsv},
 // <ts>.done per timestamp, _SUCCESS at the end; exit code 0 / 1.
 //
-// Environment: FASTXC_XC_METHOD=plain|tensor (default tensor for >= 64
-// channels, plain below), FASTXC_XC_BLOCK=<files per block> (default: the
-// whole timestamp in one block), FASTXC_LOG_LEVEL.
+// Environment: FASTXC_XC_METHOD=plain|tensor (default: autotuned per
+// timestamp shape with fxc_xc_autotune), FASTXC_XC_BLOCK=<files per block>
+// (default: the whole timestamp in one block), FASTXC_LOG_LEVEL.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -21,6 +21,25 @@
 #include "fastxc_gb300.h"
 
 using namespace fxcio;
+
+// Autotunes the stack method on the timestamp's first 512 bins (copied to
+// the device for the timing runs only).
+static int autotune_host(fxc_ctx* ctx, fxc_pairplan* plan, const std::vector<float>& payload, int nstep,
+                         int32_t nch, int nspec, int* method) {
+  const int sample = nspec < 512 ? nspec : 512;
+  const size_t rows = (size_t)nstep * nch;
+  std::vector<float> h(rows * sample * 2);
+  for (size_t r = 0; r < rows; ++r)
+    memcpy(h.data() + r * sample * 2, payload.data() + r * (size_t)nspec * 2, sizeof(float) * 2 * sample);
+  void* d = nullptr;
+  int rc = fxc_device_alloc(ctx, h.size() * sizeof(float), &d);
+  if (rc == FXC_OK) rc = fxc_memcpy(ctx, d, h.data(), h.size() * sizeof(float), FXC_COPY_H2D);
+  int32_t m = FXC_XC_PLAIN;
+  if (rc == FXC_OK) rc = fxc_xc_autotune(ctx, plan, (const float*)d, nstep, nch, sample, sample, &m, nullptr, nullptr);
+  fxc_device_free(ctx, d);
+  *method = m;
+  return rc;
+}
 
 static void usage() {
   fprintf(stderr,
@@ -135,12 +154,13 @@ int main(int argc, char** argv) {
     }
     std::vector<float> ncf((size_t)src.size() * shape.cc_size);
     if (!src.empty()) {
-      int method = (nch >= 64) ? FXC_XC_TENSOR : FXC_XC_PLAIN;
+      int method = -1;  // autotuned unless FASTXC_XC_METHOD names one
       if (menv && !strcmp(menv, "plain")) method = FXC_XC_PLAIN;
       if (menv && !strcmp(menv, "tensor")) method = FXC_XC_TENSOR;
       fxc_pairplan* plan = nullptr;
-      if (fxc_pairplan_create(ctx, src.data(), rec.data(), (int64_t)src.size(), (int32_t)nch, &plan) !=
-              FXC_OK ||
+      int rc = fxc_pairplan_create(ctx, src.data(), rec.data(), (int64_t)src.size(), (int32_t)nch, &plan);
+      if (rc == FXC_OK && method < 0) rc = autotune_host(ctx, plan, payload, nstep, (int32_t)nch, nspec, &method);
+      if (rc != FXC_OK ||
           fxc_xc_run_host(ctx, plan, payload.data(), nstep, (int32_t)nch, nspec, nullptr,
                           1.0f / (float)nstep, &shape, ncf.data(), method) != FXC_OK) {
         FXLOG_ERROR("xc_gpu_failed", "timestamp=\"%s\" error=\"%s\"", ti.timestamp.c_str(), fxc_last_error());

@@ -90,6 +90,13 @@ class Context:
         lib().fxc_xc_stack(self.handle, plan.handle, _ptr(d_spec), nwin, nchan, nspec, spec_pitch,
                            _ptr(d_mask), float(scale), _ptr(d_stack), stack_pitch, method)
 
+    def xc_autotune(self, plan: "PairPlan", d_spec, nwin, nchan, nspec, spec_pitch):
+        """(method, plain sample ms, tensor sample ms) from fxc_xc_autotune."""
+        m, a, b = C.c_int32(), C.c_float(), C.c_float()
+        lib().fxc_xc_autotune(self.handle, plan.handle, _ptr(d_spec), nwin, nchan, nspec, spec_pitch, C.byref(m),
+                              C.byref(a), C.byref(b))
+        return int(m.value), float(a.value), float(b.value)
+
     @staticmethod
     def xc_packed_bytes(nchan, nwin, nspec) -> int:
         out = C.c_int64()

@@ -374,7 +374,7 @@ Layout job_layout(const Job* j, double pws_block_gib) {
   };
   const int fw = pws ? j->nspec : j->fchunk;  // bins gathered per pass
   L.chunk = take((size_t)L.K * j->nstep * nchan * fw * 8);
-  L.packed = take(j->desc.method == FXC_XC_TENSOR ? (size_t)xc_packed_chunks(nchan, (int64_t)L.K * j->nstep, fw) * 16 : 0);
+  L.packed = take(j->desc.method != FXC_XC_PLAIN ? (size_t)xc_packed_chunks(nchan, (int64_t)L.K * j->nstep, fw) * 16 : 0);
   L.stack = take((size_t)L.blk * pitch * 8);
   L.ncf = take((size_t)L.blk * cc * 4);
   L.ptrs = take((size_t)L.K * nsta * sizeof(void*));
@@ -436,7 +436,7 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
   const int D = j->desc.ndays;
   const int nspec = j->nspec, nstep = j->nstep;
   const int64_t pitch = xc_stack_pitch(nspec);
-  const int method = j->desc.method;
+  int method = j->desc.method;  // < 0: autotuned on the first gathered block
   const Layout& L = j->layout;
   float2* chunk = reinterpret_cast<float2*>(work + L.chunk);
   uint4* packed = reinterpret_cast<uint4*>(work + L.packed);
@@ -474,6 +474,12 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
       for (int f0 = 0; f0 < nspec && rc == FXC_OK; f0 += j->fchunk) {
         const int fw = std::min(j->fchunk, nspec - f0);
         rc = gather_bins(j, nd, f0, fw, st, d_ptrs, chunk);
+        if (rc == FXC_OK && method < 0) {
+          int32_t m = FXC_XC_PLAIN;
+          rc = fxc_xc_autotune(ctx, pg.p, reinterpret_cast<const float*>(chunk), nwin, nchan, fw, fw, &m, nullptr,
+                               nullptr);
+          method = m;
+        }
         if (rc == FXC_OK && method == FXC_XC_TENSOR) {
           rc = xc_pack_launch(ctx, chunk, nwin, nchan, fw, fw, nullptr, packed);
           if (rc == FXC_OK) rc = xc_gemm_launch(ctx, pg.p, packed, nwin, fw, scale, stack + f0, pitch, d0 > 0);
@@ -505,9 +511,15 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
         // per-day stack -> per-day NCF = trace d of every pair of the block
         std::vector<EntryKey> keys;
         JOB_TRY(pin_days(s, j, j->desc.day0 + d, 1, st, d_ptrs, &keys));
-        const int rc = gather_bins(j, 1, 0, nspec, st, d_ptrs, chunk);
+        int rc = gather_bins(j, 1, 0, nspec, st, d_ptrs, chunk);
         unpin_days(s, keys, st);
         JOB_TRY(rc);
+        if (method < 0) {
+          int32_t m = FXC_XC_PLAIN;
+          JOB_TRY(fxc_xc_autotune(ctx, pg.p, reinterpret_cast<const float*>(chunk), nstep, nchan, nspec, nspec, &m,
+                                  nullptr, nullptr));
+          method = m;
+        }
         JOB_TRY(xc_stack_launch(ctx, pg.p, chunk, nstep, nchan, nspec, nspec, nullptr, 1.0f / (float)nstep, stack,
                                 pitch, method, 0));
         JOB_TRY(xc_finalize_launch(ctx, stack, np, pitch, &j->shape, ncf));
@@ -669,7 +681,8 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
   clear_error();
   FXC_CHECK_ARG(s && job && id && job->stations, "null argument");
   FXC_CHECK_ARG(job->nsta >= 2 && job->ndays >= 1, "a job needs >= 2 stations and >= 1 day");
-  FXC_CHECK_ARG(job->method == FXC_XC_PLAIN || job->method == FXC_XC_TENSOR, "unknown method");
+  FXC_CHECK_ARG(job->method == FXC_XC_PLAIN || job->method == FXC_XC_TENSOR || job->method == -1,
+                "unknown method %d", job->method);
   FXC_CHECK_ARG(job->lag > 0 && job->lag <= s->cfg.lag_max, "lag %g outside (0, %g]", job->lag, s->cfg.lag_max);
   Job* j = new Job();
   j->desc = *job;
@@ -699,7 +712,7 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
   }
   j->kdays = std::max(1, std::min<int>(job->ndays, (int)(s->cache.bytes() / 2 / day_entries)));
   {
-    const double per_bin = (double)j->kdays * j->nstep * 3 * job->nsta * 8 * (job->method == FXC_XC_TENSOR ? 2 : 1);
+    const double per_bin = (double)j->kdays * j->nstep * 3 * job->nsta * 8 * (job->method != FXC_XC_PLAIN ? 2 : 1);
     int fc = (int)(s->cfg.chunk_gib * 1073741824.0 / per_bin) / 64 * 64;
     j->fchunk = std::max(64, std::min(fc, j->nspec));
   }

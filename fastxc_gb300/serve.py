@@ -69,7 +69,7 @@ class Server:
 
 def poisson_stream(server: Server, seconds: float, rate: float, seed: int = 0, pool: int = 1000,
                    sta_range=(2, 200), day_range=(1, 30), deltas=(0.05, 0.1, 0.2), lag_range=(50.0, 200.0),
-                   pws_frac=0.1, days_total=60, method=1, wait_limit_s=600.0):
+                   pws_frac=0.1, days_total=60, method=-1, wait_limit_s=600.0):
     """Submits a Poisson stream of jobs for `seconds` (mean `rate` per s) and
     waits for all of them (each at most wait_limit_s). Returns (per-job
     records, wall seconds from the first submission to the last result,

@@ -272,6 +272,16 @@ int fxc_tfpws_run(fxc_ctx *ctx, const float *d_groups, const float *d_weights,
                   const float *d_linear, int32_t nsamples, float delta, int32_t band_limited,
                   float fmin, float fmax, float taper_hz, float power, float *d_out);
 
+/* Autotuner of the stack method (tile shape): times the plain FP32 kernel
+ * (16 x 16 channel tiles) and the tcgen05 BF16 hi/lo contraction (128 x N
+ * tiles + pack) on the first min(nspec, 512) bins of d_spec and returns the
+ * faster in *method (FXC_XC_PLAIN / FXC_XC_TENSOR) with the sample times
+ * (ms, -1 when a candidate does not apply; ms_* may be null). Decisions are
+ * cached per (device, channels, windows, pairs, tiles) for the process. No
+ * reference counterpart (the reference has one kernel). Synchronous. */
+int fxc_xc_autotune(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, int64_t nwin, int32_t nchan,
+                    int32_t nspec, int64_t spec_pitch, int32_t *method, float *ms_plain, float *ms_tensor);
+
 /* ---- serving: correlation jobs over resident station spectra ------------
  * No counterpart in the reference (its stages are batch executables). A
  * server owns one device, `slots` concurrent job slots (each a host thread,
@@ -311,7 +321,7 @@ typedef struct fxc_job {
   int32_t day0, ndays;
   float delta;          /* sampling interval of the spectra, s */
   float lag;            /* NCF half length, s */
-  int32_t method;       /* FXC_XC_PLAIN or FXC_XC_TENSOR */
+  int32_t method;       /* FXC_XC_PLAIN, FXC_XC_TENSOR, or -1: autotuned per job shape */
   int32_t pws;
   float pws_power;
 } fxc_job;

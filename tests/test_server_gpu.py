@@ -100,7 +100,7 @@ def test_same_result_alone_and_in_mix(built_lib, torch_cuda):
             a,
             dict(stations=[5, 6, 7], day0=1, ndays=4, delta=0.2, lag=50.0, method=0, pws=True),
             dict(stations=[11, 3], day0=2, ndays=1, delta=0.05, lag=200.0, method=0),
-            dict(stations=list(range(20, 60)), day0=3, ndays=1, delta=0.2, lag=100.0, method=1),
+            dict(stations=list(range(20, 60)), day0=3, ndays=1, delta=0.2, lag=100.0, method=-1),
             a,
         ]
         ids = [s.submit(**m) for m in mix]

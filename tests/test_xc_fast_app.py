@@ -52,7 +52,7 @@ def make_inputs(tmp, nsta=4, nstep=6, nspec=1001, split=True, seed=0):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method,block", [("plain", None), ("tensor", None), ("plain", "5")])
+@pytest.mark.parametrize("method,block", [("plain", None), ("tensor", None), ("plain", "5"), ("auto", None)])
 def test_xc_fast_end_to_end(tmp_path, built_lib, torch_cuda, method, block):
     import os
 
