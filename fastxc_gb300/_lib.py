@@ -184,6 +184,8 @@ _SIGNATURES.update({
 _SIGNATURES.update({
     "fxc_linear_stack": (_int, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
     "fxc_stack_prestack": (_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "fxc_pws_stream_add": (_int, [_vp, _vp, _i64, _i32, _i32, _f32, _vp, _vp]),
+    "fxc_pws_stream_finish": (_int, [_vp, _vp, _vp, _i32, _i32, _f32, _vp]),
     "fxc_pws_run": (_int, [_vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _f32, _vp]),
     "fxc_tfpws_run": (_int, [_vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _f32, _i32, _f32, _f32, _f32, _f32, _vp]),
 })

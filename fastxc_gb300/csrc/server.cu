@@ -179,13 +179,13 @@ struct Entry {
 };
 
 // Working-memory layout of a job (byte offsets into its work block). Linear
-// jobs: one pair plan over all pairs, K days gathered per pass, the stack
-// accumulated over passes. PWS jobs: pairs in blocks of `blk` whose per-day
-// NCFs (all days) fit the block budget; every block gathers each day again.
+// jobs: K days pinned per pass group, bins gathered fchunk at a time, the
+// stack accumulated over the day groups. PWS jobs: one day at a time (all
+// bins), streaming phasor / linear sums over the days.
 struct Layout {
   int K = 1;
-  int64_t blk = 0;
-  size_t chunk = 0, packed = 0, stack = 0, ncf = 0, ptrs = 0, traces = 0, groups = 0, wts = 0, lin = 0, out = 0;
+  int64_t blk = 0;  // pairs held at once (all of the job's)
+  size_t chunk = 0, packed = 0, stack = 0, ncf = 0, ptrs = 0, traces = 0, lin = 0, out = 0;
   size_t total = 0;
 };
 
@@ -354,18 +354,13 @@ void unpin_entries(fxc_server* s, const std::vector<EntryKey>& keys, cudaStream_
 
 size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
-Layout job_layout(const Job* j, double pws_block_gib) {
+Layout job_layout(const Job* j) {
   Layout L;
-  const int nsta = (int)j->stations.size(), nchan = 3 * nsta, D = j->desc.ndays;
+  const int nsta = (int)j->stations.size(), nchan = 3 * nsta;
   const bool pws = j->desc.pws != 0;
   const size_t cc = (size_t)j->cc_size, pitch = (size_t)xc_stack_pitch(j->nspec);
   L.K = pws ? 1 : j->kdays;
   L.blk = j->npairs;
-  if (pws) {
-    const double per_pair = (double)D * cc * 8 + (double)D * 4 + (double)cc * 12 + (double)pitch * 8;
-    L.blk = std::max<int64_t>(1, std::min<int64_t>(65535, (int64_t)(pws_block_gib * 1073741824.0 / per_pair)));
-    L.blk = std::min<int64_t>(L.blk, j->npairs);
-  }
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t o = off;
@@ -379,9 +374,7 @@ Layout job_layout(const Job* j, double pws_block_gib) {
   L.ncf = take((size_t)L.blk * cc * 4);
   L.ptrs = take((size_t)L.K * nsta * sizeof(void*));
   if (pws) {
-    L.traces = take((size_t)L.blk * D * cc * 4);
-    L.groups = take((size_t)L.blk * D * cc * 4);
-    L.wts = take((size_t)L.blk * D * 4);
+    L.traces = take((size_t)L.blk * cc * 8);  // streaming phasor sums (complex)
     L.lin = take((size_t)L.blk * cc * 4);
     L.out = take((size_t)L.blk * cc * 4);
   }
@@ -459,35 +452,37 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
     j->ncf.resize((size_t)j->npairs * cc);
     if (j->desc.pws) j->pws.resize((size_t)j->npairs * cc);
   }
+  PlanGuard pg;
+  JOB_TRY(fxc_pairplan_create(ctx, src.data(), rec.data(), j->npairs, nchan, &pg.p));
+  // one stacking pass: bins [f0, f0 + fw) of the nd pinned days into
+  // stack[:, f0 : f0 + fw) (added to it when accumulate)
+  auto pass = [&](int nd, int f0, int fw, float scale, int accumulate) -> int {
+    const int64_t nwin = (int64_t)nd * nstep;
+    int rc = gather_bins(j, nd, f0, fw, st, d_ptrs, chunk);
+    if (rc == FXC_OK && method < 0) {
+      int32_t m = FXC_XC_PLAIN;
+      rc = fxc_xc_autotune(ctx, pg.p, reinterpret_cast<const float*>(chunk), nwin, nchan, fw, fw, &m, nullptr, nullptr);
+      method = m;
+    }
+    if (rc != FXC_OK) return rc;
+    if (method == FXC_XC_TENSOR) {
+      rc = xc_pack_launch(ctx, chunk, nwin, nchan, fw, fw, nullptr, packed);
+      if (rc == FXC_OK) rc = xc_gemm_launch(ctx, pg.p, packed, nwin, fw, scale, stack + f0, pitch, accumulate);
+      return rc;
+    }
+    return xc_stack_launch(ctx, pg.p, chunk, nwin, nchan, fw, fw, nullptr, scale, stack + f0, pitch, FXC_XC_PLAIN,
+                           accumulate);
+  };
   if (!j->desc.pws) {
-    PlanGuard pg;
-    JOB_TRY(fxc_pairplan_create(ctx, src.data(), rec.data(), j->npairs, nchan, &pg.p));
     const float scale = 1.0f / (float)(D * nstep);
     for (int d0 = 0; d0 < D; d0 += L.K) {
       const int nd = std::min(L.K, D - d0);
       std::vector<EntryKey> keys;
       JOB_TRY(pin_days(s, j, j->desc.day0 + d0, nd, st, d_ptrs, &keys));
-      const int64_t nwin = (int64_t)nd * nstep;
       int rc = FXC_OK;
-      // bins in passes of fchunk: each pass stacks all windows of the pinned
-      // days for its bins into stack[:, f0 : f0 + fw)
-      for (int f0 = 0; f0 < nspec && rc == FXC_OK; f0 += j->fchunk) {
-        const int fw = std::min(j->fchunk, nspec - f0);
-        rc = gather_bins(j, nd, f0, fw, st, d_ptrs, chunk);
-        if (rc == FXC_OK && method < 0) {
-          int32_t m = FXC_XC_PLAIN;
-          rc = fxc_xc_autotune(ctx, pg.p, reinterpret_cast<const float*>(chunk), nwin, nchan, fw, fw, &m, nullptr,
-                               nullptr);
-          method = m;
-        }
-        if (rc == FXC_OK && method == FXC_XC_TENSOR) {
-          rc = xc_pack_launch(ctx, chunk, nwin, nchan, fw, fw, nullptr, packed);
-          if (rc == FXC_OK) rc = xc_gemm_launch(ctx, pg.p, packed, nwin, fw, scale, stack + f0, pitch, d0 > 0);
-        } else if (rc == FXC_OK) {
-          rc = xc_stack_launch(ctx, pg.p, chunk, nwin, nchan, fw, fw, nullptr, scale, stack + f0, pitch, method,
-                               d0 > 0);
-        }
-      }
+      // all windows of the pinned days per pass, bins in passes of fchunk
+      for (int f0 = 0; f0 < nspec && rc == FXC_OK; f0 += j->fchunk)
+        rc = pass(nd, f0, std::min(j->fchunk, nspec - f0), scale, d0 > 0);
       unpin_days(s, keys, st);
       JOB_TRY(rc);
     }
@@ -495,49 +490,27 @@ int run_job(fxc_server* s, int slot, Job* j, char* work) {
     if (s->cfg.keep_results)
       FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data(), ncf, (size_t)j->npairs * cc * 4, cudaMemcpyDeviceToHost, st));
   } else {
-    float* traces = reinterpret_cast<float*>(work + L.traces);
-    float* groups = reinterpret_cast<float*>(work + L.groups);
-    float* wts = reinterpret_cast<float*>(work + L.wts);
+    // PWS over the days, streamed: per day the NCF of every pair, its unit
+    // analytic phasor and the NCF itself are added (weight 1/D) to running
+    // sums; PWS = linear x |phasor sum|^power at the end
+    float* acc = reinterpret_cast<float*>(work + L.traces);
     float* lin = reinterpret_cast<float*>(work + L.lin);
     float* out = reinterpret_cast<float*>(work + L.out);
-    std::vector<int64_t> toff((size_t)L.blk), goff((size_t)L.blk);
-    std::vector<int32_t> tcnt((size_t)L.blk, D), gcnt((size_t)L.blk);
-    for (int64_t i = 0; i < L.blk; ++i) toff[i] = i * D;
-    for (int64_t p0 = 0; p0 < j->npairs; p0 += L.blk) {
-      const int64_t np = std::min<int64_t>(L.blk, j->npairs - p0);
-      PlanGuard pg;
-      JOB_TRY(fxc_pairplan_create(ctx, src.data() + p0, rec.data() + p0, np, nchan, &pg.p));
-      for (int d = 0; d < D; ++d) {
-        // per-day stack -> per-day NCF = trace d of every pair of the block
-        std::vector<EntryKey> keys;
-        JOB_TRY(pin_days(s, j, j->desc.day0 + d, 1, st, d_ptrs, &keys));
-        int rc = gather_bins(j, 1, 0, nspec, st, d_ptrs, chunk);
-        unpin_days(s, keys, st);
-        JOB_TRY(rc);
-        if (method < 0) {
-          int32_t m = FXC_XC_PLAIN;
-          JOB_TRY(fxc_xc_autotune(ctx, pg.p, reinterpret_cast<const float*>(chunk), nstep, nchan, nspec, nspec, &m,
-                                  nullptr, nullptr));
-          method = m;
-        }
-        JOB_TRY(xc_stack_launch(ctx, pg.p, chunk, nstep, nchan, nspec, nspec, nullptr, 1.0f / (float)nstep, stack,
-                                pitch, method, 0));
-        JOB_TRY(xc_finalize_launch(ctx, stack, np, pitch, &j->shape, ncf));
-        FXC_CUDA_TRY(cudaMemcpy2DAsync(traces + (size_t)d * cc, (size_t)D * cc * 4, ncf, cc * 4, cc * 4, (size_t)np,
-                                       cudaMemcpyDeviceToDevice, st));
-      }
-      // substack 1: group = day NCF (weight 1/D), linear = mean of the days
-      JOB_TRY(fxc_stack_prestack(ctx, traces, toff.data(), tcnt.data(), (int32_t)np, j->cc_size, 1, 0, groups, wts,
-                                 lin, goff.data(), gcnt.data()));
-      JOB_TRY(fxc_pws_run(ctx, groups, wts, goff.data(), gcnt.data(), (int32_t)np, lin, j->cc_size,
-                          j->desc.pws_power, out));
-      if (s->cfg.keep_results) {
-        FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data() + (size_t)p0 * cc, lin, (size_t)np * cc * 4,
-                                     cudaMemcpyDeviceToHost, st));
-        FXC_CUDA_TRY(cudaMemcpyAsync(j->pws.data() + (size_t)p0 * cc, out, (size_t)np * cc * 4,
-                                     cudaMemcpyDeviceToHost, st));
-        FXC_CUDA_TRY(cudaStreamSynchronize(st));
-      }
+    FXC_CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)j->npairs * cc * 8, st));
+    FXC_CUDA_TRY(cudaMemsetAsync(lin, 0, (size_t)j->npairs * cc * 4, st));
+    for (int d = 0; d < D; ++d) {
+      std::vector<EntryKey> keys;
+      JOB_TRY(pin_days(s, j, j->desc.day0 + d, 1, st, d_ptrs, &keys));
+      const int rc = pass(1, 0, nspec, 1.0f / (float)nstep, 0);
+      unpin_days(s, keys, st);
+      JOB_TRY(rc);
+      JOB_TRY(xc_finalize_launch(ctx, stack, j->npairs, pitch, &j->shape, ncf));
+      JOB_TRY(fxc_pws_stream_add(ctx, ncf, (int64_t)cc, (int32_t)j->npairs, j->cc_size, 1.0f / (float)D, acc, lin));
+    }
+    JOB_TRY(fxc_pws_stream_finish(ctx, acc, lin, (int32_t)j->npairs, j->cc_size, j->desc.pws_power, out));
+    if (s->cfg.keep_results) {
+      FXC_CUDA_TRY(cudaMemcpyAsync(j->ncf.data(), lin, (size_t)j->npairs * cc * 4, cudaMemcpyDeviceToHost, st));
+      FXC_CUDA_TRY(cudaMemcpyAsync(j->pws.data(), out, (size_t)j->npairs * cc * 4, cudaMemcpyDeviceToHost, st));
     }
   }
   FXC_CUDA_TRY(cudaStreamSynchronize(st));
@@ -716,7 +689,7 @@ int fxc_server_submit(fxc_server* s, const fxc_job* job, int64_t* id) {
     int fc = (int)(s->cfg.chunk_gib * 1073741824.0 / per_bin) / 64 * 64;
     j->fchunk = std::max(64, std::min(fc, j->nspec));
   }
-  j->layout = job_layout(j, s->cfg.chunk_gib);
+  j->layout = job_layout(j);
   j->work_bytes = j->layout.total;
   if (j->work_bytes > s->work.bytes()) {
     set_error("job needs %zu bytes of working memory, the arena holds %zu", j->work_bytes, s->work.bytes());

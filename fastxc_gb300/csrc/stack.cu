@@ -169,6 +169,48 @@ __global__ void __launch_bounds__(kStT)
   }
 }
 
+// Streaming PWS: one group (e.g. one day's NCF of every pair) per call.
+// acc[p] += w * unit analytic phasor of row p, lin[p] += w * row p; the
+// same per-sample arithmetic as k_pws, summed call by call.
+__global__ void __launch_bounds__(kStT)
+    k_pws_stream_add(const float* __restrict__ rows, int64_t rows_pitch, AnyPlan a, float w,
+                     float2* __restrict__ acc, float* __restrict__ lin) {
+  extern __shared__ float2 sm[];
+  const int n = a.n;
+  float2* buf = sm;
+  float2* stw = sm + any_buf_elems(a);
+  fft_twiddles_to_smem<kStT>(a.p, stw);
+  const float* x = rows + (int64_t)blockIdx.x * rows_pitch;
+  for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
+  __syncthreads();
+  any_forward<kStT>(buf, a, stw);
+  analytic_mask(buf, a);
+  __syncthreads();
+  any_inverse<kStT>(buf, a, stw);
+  const float invn = 1.0f / (float)n;
+  float2* ac = acc + (int64_t)blockIdx.x * n;
+  float* li = lin + (int64_t)blockIdx.x * n;
+  for (int t = threadIdx.x; t < n; t += kStT) {
+    const float2 z = buf[t];
+    const float re = z.x * invn, im = z.y * invn;
+    float mod = sqrtf(re * re + im * im);
+    mod = (mod > 1e-7f) ? mod : 1e-7f;
+    float2 v = ac[t];
+    v.x += (re / mod) * w;
+    v.y += (im / mod) * w;
+    ac[t] = v;
+    li[t] += x[t] * w;
+  }
+}
+
+__global__ void k_pws_stream_finish(const float2* __restrict__ acc, const float* __restrict__ lin, int64_t total,
+                                    float power, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = acc[i];
+    out[i] = lin[i] * weight_pow(a.x * a.x + a.y * a.y, power);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // TF-PWS
 // ---------------------------------------------------------------------------
@@ -420,6 +462,38 @@ int fxc_stack_prestack(fxc_ctx* ctx, const float* d_traces, const int64_t* h_tra
   FXC_LAUNCH_CHECK();
   // the host arrays outlive the call; keep the copies ordered before return
   FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
+}
+
+int fxc_pws_stream_add(fxc_ctx* ctx, const float* d_rows, int64_t rows_pitch, int32_t npairs, int32_t nsamples,
+                       float weight, float* d_acc, float* d_lin) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0 && nsamples >= 2 && rows_pitch >= nsamples, "invalid shape");
+  if (npairs == 0) return FXC_OK;
+  FXC_CHECK_ARG(d_rows && d_acc && d_lin, "null pointer");
+  AnyPlan a;
+  FXC_TRY(stack_plan(nsamples, &a));
+  const size_t smem = sizeof(float2) * ((size_t)any_buf_elems(a) + fft_tw_smem_elems(a.p));
+  FXC_TRY(set_smem_limit(k_pws_stream_add, smem));
+  k_pws_stream_add<<<(unsigned)npairs, kStT, smem, ctx->stream>>>(d_rows, rows_pitch, a, weight,
+                                                                  reinterpret_cast<float2*>(d_acc), d_lin);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+int fxc_pws_stream_finish(fxc_ctx* ctx, const float* d_acc, const float* d_lin, int32_t npairs, int32_t nsamples,
+                          float power, float* d_out) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(npairs >= 0 && nsamples >= 1, "invalid shape");
+  if (npairs == 0) return FXC_OK;
+  FXC_CHECK_ARG(d_acc && d_lin && d_out, "null pointer");
+  k_pws_stream_finish<<<1024, 256, 0, ctx->stream>>>(reinterpret_cast<const float2*>(d_acc), d_lin,
+                                                     (int64_t)npairs * nsamples, power, d_out);
+  count_launch();
+  FXC_LAUNCH_CHECK();
   return FXC_OK;
 }
 

@@ -43,6 +43,17 @@ def pws(ctx: Context, d_groups, d_weights, goff, gcnt, d_linear, nsamples: int, 
                       _ptr(d_linear), nsamples, float(power), _ptr(d_out))
 
 
+def pws_stream_add(ctx: Context, d_rows, rows_pitch: int, npairs: int, nsamples: int, weight: float, d_acc,
+                   d_lin) -> None:
+    """Adds one group per pair (row p of d_rows) to the streaming PWS sums."""
+    lib().fxc_pws_stream_add(ctx.handle, _ptr(d_rows), rows_pitch, npairs, nsamples, float(weight), _ptr(d_acc),
+                             _ptr(d_lin))
+
+
+def pws_stream_finish(ctx: Context, d_acc, d_lin, npairs: int, nsamples: int, power: float, d_out) -> None:
+    lib().fxc_pws_stream_finish(ctx.handle, _ptr(d_acc), _ptr(d_lin), npairs, nsamples, float(power), _ptr(d_out))
+
+
 def tfpws(ctx: Context, d_groups, d_weights, goff, gcnt, d_linear, nsamples: int, d_out, delta: float,
           band=None, taper_hz: float = -1.0, power: float = 1.0) -> None:
     goff = np.ascontiguousarray(goff, np.int64)

@@ -261,6 +261,20 @@ int fxc_pws_run(fxc_ctx *ctx, const float *d_groups, const float *d_weights,
                 const int64_t *h_group_offsets, const int32_t *h_group_counts, int32_t npairs,
                 const float *d_linear, int32_t nsamples, float power, float *d_out);
 
+/* Streaming PWS for groups that arrive one at a time (one day's NCF of
+ * every pair per call): d_acc ([npairs][nsamples] complex) and d_lin
+ * ([npairs][nsamples]) start zeroed; each add accumulates weight x the unit
+ * analytic phasor (modulus floor 1e-7) of row p of d_rows (row pitch
+ * rows_pitch floats) into d_acc and weight x the row into d_lin; finish
+ * writes out = lin * |acc|^power. With weight 1/G over G groups this is
+ * fxc_stack_prestack (substack 1) + fxc_pws_run without holding the G
+ * groups. Asynchronous on the context's stream. No reference counterpart
+ * (the reference stacks whole SourcePack groups). */
+int fxc_pws_stream_add(fxc_ctx *ctx, const float *d_rows, int64_t rows_pitch, int32_t npairs, int32_t nsamples,
+                       float weight, float *d_acc, float *d_lin);
+int fxc_pws_stream_finish(fxc_ctx *ctx, const float *d_acc, const float *d_lin, int32_t npairs, int32_t nsamples,
+                          float power, float *d_out);
+
 /* S-transform time-frequency PWS (compute_tfpws_from_prestack,
  * native/tfpws/core/tfpws_compute.cu:19-366): for every frequency of the
  * nsamples/2+1 bins the Gaussian voices (scale 0.1) of the groups and of

@@ -123,3 +123,24 @@ def test_tfpws_prime_lengths_bluestein(ctx, torch_cuda, n, band):
     err = rel(got, ref)
     print("tfpws bluestein rel err", n, err)
     assert err.max() < 1e-5
+
+
+@pytest.mark.parametrize("n,power", [(2001, 1.0), (4001, 2.0)])
+def test_streaming_pws_matches_oracle(ctx, torch_cuda, n, power):
+    """One group per call (weight 1/G): the same PWS as prestack(1) + run."""
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    npairs, G = 4, 7
+    tr = ncf_traces(npairs, G, n, seed=8)
+    acc = torch.zeros((npairs, 2 * n), dtype=torch.float32, device="cuda")
+    lin = torch.zeros((npairs, n), dtype=torch.float32, device="cuda")
+    for g in range(G):
+        rows = torch.from_numpy(np.ascontiguousarray(tr[:, g, :])).cuda()
+        stack.pws_stream_add(ctx, rows, n, npairs, n, 1.0 / G, acc, lin)
+    out = torch.empty((npairs, n), dtype=torch.float32, device="cuda")
+    stack.pws_stream_finish(ctx, acc, lin, npairs, n, power, out)
+    ctx.synchronize()
+    ref = np.stack([sto.pws(tr[p], 1, power) for p in range(npairs)])
+    assert rel(out.cpu().numpy(), ref).max() < 1e-5
+    assert rel(lin.cpu().numpy(), tr.mean(axis=1)).max() < 1e-6
