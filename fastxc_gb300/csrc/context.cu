@@ -147,6 +147,7 @@ int fxc_ctx_destroy(fxc_ctx* ctx) {
   ctx->scratch3.release();
   ctx->scratch4.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   delete ctx;
   return FXC_OK;
 }

@@ -640,27 +640,95 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   FXC_TRY(ctx_enter(ctx));
   FXC_CHECK_ARG(plan != nullptr && shape != nullptr, "null plan or shape");
   FXC_CHECK_ARG(h_spec != nullptr && h_ncf != nullptr, "null host pointer");
+  FXC_CHECK_ARG(method == FXC_XC_PLAIN || method == FXC_XC_TENSOR, "unknown xc method %d", method);
   if (plan->npairs == 0) return FXC_OK;
-  const size_t spec_bytes = sizeof(float2) * (size_t)nwin * (size_t)nchan * (size_t)spec_pitch;
+  // The windows stream through a ring of device buffers on a copy stream;
+  // each chunk is packed (tensor) or stacked with accumulation (plain) on the
+  // compute stream as soon as it lands, so the host-to-device copy -- the
+  // bound of this call -- overlaps the compute.
+  const int nspec = shape->nspec;
+  const int64_t wchunk = 64;  // windows per chunk (two 32-window K-blocks)
+  const int kRing = 3;
+  const size_t row_bytes = sizeof(float2) * (size_t)nchan * (size_t)spec_pitch;  // one window
+  const size_t chunk_bytes = row_bytes * (size_t)wchunk;
   const size_t mask_bytes = h_mask ? (size_t)nwin * (size_t)nchan : 0;
   const size_t ncf_bytes = sizeof(float) * (size_t)plan->npairs * (size_t)shape->cc_size;
-  const size_t a = 256;
-  const size_t off_mask = (spec_bytes + a - 1) / a * a;
-  const size_t off_ncf = off_mask + (mask_bytes + a - 1) / a * a;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t off_mask = al(chunk_bytes) * kRing;
+  const size_t off_ncf = off_mask + al(mask_bytes);
   FXC_TRY(ctx->scratch2.reserve(off_ncf + ncf_bytes));
   char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
-  FXC_CUDA_TRY(cudaMemcpyAsync(base, h_spec, spec_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  const int64_t pitch = xc_stack_pitch(nspec);
+  FXC_TRY(ctx->scratch.reserve(sizeof(float2) * (size_t)pitch * (size_t)plan->npairs));
+  float2* stack = reinterpret_cast<float2*>(ctx->scratch.ptr);
+  uint4* packed = nullptr;
+  if (method == FXC_XC_TENSOR) {
+    FXC_CHECK_ARG(plan->tensor != nullptr, "pair plan has no tensor tiles");
+    const int64_t chunks = xc_packed_chunks(nchan, nwin, nspec);
+    if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
+    packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
+  }
+  if (!ctx->copy_stream) FXC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  cudaStream_t cs = ctx->copy_stream;
+  // the copy stream starts after work already queued on the compute stream
+  cudaEvent_t start_ev;
+  FXC_CUDA_TRY(cudaEventCreateWithFlags(&start_ev, cudaEventDisableTiming));
+  const int64_t nchunks = (nwin + wchunk - 1) / wchunk;
+  std::vector<cudaEvent_t> landed((size_t)kRing), used((size_t)kRing);
+  for (int r = 0; r < kRing; ++r) {
+    cudaEventCreateWithFlags(&landed[r], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&used[r], cudaEventDisableTiming);
+  }
+  int rc = FXC_OK;
+  auto cuda_ok = [&](cudaError_t e) {
+    if (e != cudaSuccess && rc == FXC_OK) {
+      set_error("CUDA error in the host-buffer xc pipeline: %s", cudaGetErrorString(e));
+      rc = FXC_ERR_CUDA;
+    }
+    return rc == FXC_OK;
+  };
+  cuda_ok(cudaEventRecord(start_ev, ctx->stream));
+  cuda_ok(cudaStreamWaitEvent(cs, start_ev, 0));
   const uint8_t* d_mask = nullptr;
   if (h_mask) {
-    FXC_CUDA_TRY(
-        cudaMemcpyAsync(base + off_mask, h_mask, mask_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    cuda_ok(cudaMemcpyAsync(base + off_mask, h_mask, mask_bytes, cudaMemcpyHostToDevice, cs));
     d_mask = reinterpret_cast<const uint8_t*>(base + off_mask);
   }
+  for (int64_t c = 0; c < nchunks && rc == FXC_OK; ++c) {
+    const int r = (int)(c % kRing);
+    const int64_t w0 = c * wchunk, nw = std::min(wchunk, nwin - w0);
+    char* slot = base + al(chunk_bytes) * r;
+    if (c >= kRing) cuda_ok(cudaStreamWaitEvent(cs, used[r], 0));  // slot consumed
+    cuda_ok(cudaMemcpyAsync(slot, reinterpret_cast<const char*>(h_spec) + row_bytes * (size_t)w0,
+                            row_bytes * (size_t)nw, cudaMemcpyHostToDevice, cs));
+    cuda_ok(cudaEventRecord(landed[r], cs));
+    cuda_ok(cudaStreamWaitEvent(ctx->stream, landed[r], 0));
+    if (rc != FXC_OK) break;
+    const float2* spec = reinterpret_cast<const float2*>(slot);
+    if (method == FXC_XC_TENSOR) {
+      rc = xc_pack_launch(ctx, spec, nwin, nchan, nspec, spec_pitch, d_mask, packed, (int)(w0 / kTcKbWindows),
+                          (int)((w0 + nw + kTcKbWindows - 1) / kTcKbWindows), w0);
+    } else {
+      rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch,
+                           d_mask ? d_mask + (size_t)w0 * nchan : nullptr, scale, stack, pitch, FXC_XC_PLAIN,
+                           c > 0);
+    }
+    cuda_ok(cudaEventRecord(used[r], ctx->stream));
+  }
+  if (rc == FXC_OK && method == FXC_XC_TENSOR)
+    rc = xc_gemm_launch(ctx, plan, packed, nwin, nspec, scale, stack, pitch);
   float* d_ncf = reinterpret_cast<float*>(base + off_ncf);
-  FXC_TRY(fxc_xc_run(ctx, plan, reinterpret_cast<const float*>(base), nwin, nchan, spec_pitch,
-                     d_mask, scale, shape, d_ncf, method));
-  FXC_CUDA_TRY(cudaMemcpyAsync(h_ncf, d_ncf, ncf_bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (rc == FXC_OK) rc = xc_finalize_launch(ctx, stack, plan->npairs, pitch, shape, d_ncf);
+  if (rc == FXC_OK) cuda_ok(cudaMemcpyAsync(h_ncf, d_ncf, ncf_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  cudaStreamSynchronize(cs);
+  cudaStreamSynchronize(ctx->stream);
+  cudaEventDestroy(start_ev);
+  for (int r = 0; r < kRing; ++r) {
+    cudaEventDestroy(landed[r]);
+    cudaEventDestroy(used[r]);
+  }
+  FXC_TRY(rc);
+  FXC_CUDA_TRY(cudaGetLastError());
   return ctx_check_device_error(ctx);
 }
 

@@ -9,6 +9,7 @@ namespace fxc {
 
 constexpr int kXcTile = 16;       // channels per tile side
 constexpr int kXcFreqChunk = 64;  // bins per CTA of the plain kernel
+constexpr int kTcKbWindows = 32;  // windows per K-block of the packed tensor operands
 
 struct XcTile {
   int32_t a_base;      // first src channel of the tile
@@ -51,8 +52,11 @@ int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2*
                            int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
                            const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch,
                            int accumulate = 0);
+// Packs K-blocks [kb0, kb1) (kb1 < 0: all); spec holds windows from w_base
+// on (w_base <= kb0 * 32).
 int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, int nspec,
-                   int64_t spec_pitch, const uint8_t* mask, uint4* packed);
+                   int64_t spec_pitch, const uint8_t* mask, uint4* packed, int kb0 = 0, int kb1 = -1,
+                   int64_t w_base = 0);
 int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
                    int nspec, float scale, float2* stack, int64_t stack_pitch, int accumulate = 0);
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec);

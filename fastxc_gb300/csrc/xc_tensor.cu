@@ -43,7 +43,7 @@
 
 namespace fxc {
 
-constexpr int kTcKb = 32;             // windows per K-block
+constexpr int kTcKb = kTcKbWindows;   // windows per K-block (32)
 constexpr int kTcKc = kTcKb / 8;      // 16-byte core-matrix chunks per K-block row
 constexpr int kTcM = 128;             // MMA M (src channel rows per tile)
 constexpr int kTcNmax = 256;          // MMA N limit (rec channel rows per tile)
@@ -195,12 +195,12 @@ __device__ __forceinline__ float bf16_bits_to_float(uint16_t b) {
 
 __global__ void __launch_bounds__(256)
     k_xc_pack(const float2* __restrict__ spec, int64_t nwin, int nchan, int nspec,
-              int64_t spec_pitch, const uint8_t* __restrict__ mask, int nkb, int cpad,
-              uint4* __restrict__ packed) {
+              int64_t spec_pitch, const uint8_t* __restrict__ mask, int nkb, int cpad, int kb0,
+              int64_t w_base, uint4* __restrict__ packed) {
   extern __shared__ float2 psm[];  // [kTcKb][kPackC][kPackF + 1]
   const int f0 = blockIdx.x * kPackF;
   const int c0 = blockIdx.y * kPackC;
-  const int kb = blockIdx.z;
+  const int kb = kb0 + blockIdx.z;  // spec holds windows from w_base on
   const int tid = threadIdx.x;
   {
     const int f = tid % kPackF;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256)
       const int64_t w = w0 + k;
       bool ok = okcf && w < nwin;
       if (ok && mask) ok = __ldg(mask + w * nchan + ch) != 0;
-      v[k] = ok ? __ldg(spec + (w * nchan + ch) * spec_pitch + f0 + f) : make_float2(0.f, 0.f);
+      v[k] = ok ? __ldg(spec + ((w - w_base) * nchan + ch) * spec_pitch + f0 + f) : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int k = 0; k < kTcKb; ++k) psm[(k * kPackC + c) * (kPackF + 1) + f] = v[k];
@@ -572,16 +572,19 @@ int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
 }
 
 int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, int nspec,
-                   int64_t spec_pitch, const uint8_t* mask, uint4* packed) {
+                   int64_t spec_pitch, const uint8_t* mask, uint4* packed, int kb0, int kb1,
+                   int64_t w_base) {
   const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
-  if (nkb == 0 || nspec == 0) return FXC_OK;
+  if (kb1 < 0) kb1 = nkb;
+  if (nkb == 0 || nspec == 0 || kb1 <= kb0) return FXC_OK;
   const int cpad = (int)round_up(nchan, 8);
   FXC_CHECK_ARG((cpad + kPackC - 1) / kPackC <= 65535 && nkb <= 65535, "pack grid too large");
+  FXC_CHECK_ARG(kb0 >= 0 && kb1 <= nkb && w_base <= (int64_t)kb0 * kTcKb, "pack block range invalid");
   dim3 pg((unsigned)((nspec + kPackF - 1) / kPackF), (unsigned)((cpad + kPackC - 1) / kPackC),
-          (unsigned)nkb);
+          (unsigned)(kb1 - kb0));
   FXC_TRY(set_smem_limit(k_xc_pack, kPackSmem));
   k_xc_pack<<<pg, 256, kPackSmem, ctx->stream>>>(spec, nwin, nchan, nspec, spec_pitch, mask, nkb,
-                                                 cpad, packed);
+                                                 cpad, kb0, w_base, packed);
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;

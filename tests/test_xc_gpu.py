@@ -165,16 +165,25 @@ def test_empty_pair_list(ctx, torch_cuda):
     ctx.synchronize()
 
 
-def test_host_entry_matches_device_entry(ctx, torch_cuda):
+@pytest.mark.parametrize("nwin,method,masked", [(4, 0, False), (150, 0, True), (150, 1, True), (200, 1, False)])
+def test_host_entry_matches_oracle_and_device_entry(ctx, torch_cuda, nwin, method, masked):
+    """The host-buffer entry streams windows in 64-window chunks through a
+    ring of device buffers (ragged last chunk, gap mask): same NCFs as the
+    FP64 oracle; the tensor method packs chunk by chunk and equals the
+    device entry bit for bit."""
     rng = np.random.default_rng(5)
-    nwin, nsta, nspec = 4, 4, 1001
+    nsta, nspec = 4, 1001
     spec = make_spec(rng, nwin, 3 * nsta, nspec)
+    mask = (rng.random((nwin, 3 * nsta)) > 0.1).astype(np.uint8) if masked else None
     src, rec = station_pairs(nsta)
     shape = ctx_shape(nspec, nwin, 0.1, 20.0)
-    dev, plan = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin)
+    dev, plan = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin, mask=mask, method=method)
     host = np.zeros_like(dev)
-    ctx.xc_run_host(plan, spec, nwin, 3 * nsta, nspec, None, 1.0 / nwin, shape, host)
-    assert np.array_equal(host, dev)
+    ctx.xc_run_host(plan, spec, nwin, 3 * nsta, nspec, mask, 1.0 / nwin, shape, host, method)
+    ref = xo.xc_run(spec, src, rec, 1.0 / nwin, xo.finalize_shape(nspec, nwin, 0.1, 20.0), mask=mask)
+    assert per_row_rel_l2(host, ref).max() < NCF_RTOL
+    if method == 1:
+        assert np.array_equal(host, dev)
 
 
 def test_bad_arguments_raise(ctx, torch_cuda):
