@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--nspec", type=int, default=NSPEC, help="smaller values only for profiling runs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-stages", action="store_true", help="skip the sac2spec / stacking stage timings")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -227,6 +228,103 @@ def serving_run(args, device: int, rank: int) -> dict:
             "latency": "submit -> NCFs (and PWS) in host memory, steady clock",
             "workload": "jobs: 2-200 of 1000 stations x 1-30 days, delta 0.05/0.1/0.2 s, lag 50-200 s, "
                         "10% PWS; win 3600 s; synthetic seeded spectra cached in HBM"}
+
+
+def _timed(torch, stream, fn, reps=3, warm=1):
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> dict:
+    """The other stages of the path on their own configurations, timed with
+    CUDA events on the launching stream (inputs resident, larger than L2):
+      sac2spec: one day of 64 stations x 3 components at 10 Hz (192 rows x
+        864 000 samples, 24 one-hour windows, RAM + whitening after);
+      linear stack / PWS: 256 station pairs x 9 components, 720 NCF
+        windows of 2001 lags each (13.3 GB), PWS power 2;
+      TF-PWS: 128 of those pairs, substacks of 10 (72 groups), 0.05-5 Hz."""
+    from fastxc_gb300 import sac2spec as s2s
+    from fastxc_gb300 import stack
+    from fastxc_gb300.core import Context
+
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    ctx = Context(local, stream.cuda_stream)
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    try:
+        # --- sac2spec -------------------------------------------------------
+        F = s2s.read_filter_file(ROOT / "tests" / "golden" / "filter_d0.1_0.1-2.txt")
+        plan = s2s.plan(86400, 3600, 3600, 100, 0.1, F, s2s.WHITEN_AFTER, s2s.NORM_RUNABS)
+        resp = torch.from_numpy(s2s.filter_response(plan, F)).to(dev)
+        rows, npts = 192, plan.npts
+        series = torch.randn((rows, npts), generator=g, device=dev, dtype=torch.float32)
+        steps = np.arange(plan.nstep, dtype=np.int32)
+        spec = torch.empty((plan.nstep, rows, plan.nspec), dtype=torch.complex64, device=dev)
+        ms = _timed(torch, stream, lambda: s2s.run(ctx, plan, series, npts, npts, rows, 3, steps, resp, spec,
+                                                   plan.nspec))
+        units = rows * plan.nstep
+        alg = units * (plan.segment_pts * 4 + plan.nspec * 8)
+        out["sac2spec"] = {"channel_windows_per_s": units / (ms / 1e3), "ms": ms,
+                           "workload": f"{rows} rows x {npts} samples, {plan.nstep} windows of {plan.segment_pts}, "
+                                       f"nspec {plan.nspec}, RAM + whiten after",
+                           "algorithmic_bytes": alg, "hbm_frac": alg / (ms / 1e3) / 1e9 / hbm_gbs,
+                           "note": "algorithmic bytes = window read + spectrum write; FFT-bound, see DESIGN"}
+        del series, spec, resp
+        torch.cuda.empty_cache()
+        # --- linear stack + PWS (config 3) ----------------------------------
+        npairs, ntr, n = 2304, 720, 2001
+        t = torch.randn((npairs * ntr, n), generator=g, device=dev, dtype=torch.float32)
+        offs = np.arange(npairs, dtype=np.int64) * ntr
+        cnts = np.full(npairs, ntr, np.int32)
+        lin = torch.empty((npairs, n), dtype=torch.float32, device=dev)
+        ms = _timed(torch, stream, lambda: stack.linear_stack(ctx, t, offs, cnts, n, lin))
+        nbytes = t.numel() * 4 + lin.numel() * 4
+        out["linear_stack"] = {"traces_per_s": npairs * ntr / (ms / 1e3), "ms": ms, "bytes": nbytes,
+                               "hbm_gbs": nbytes / (ms / 1e3) / 1e9, "hbm_frac": nbytes / (ms / 1e3) / 1e9 / hbm_gbs,
+                               "workload": f"{npairs} pairs x {ntr} traces x {n} lags (FP64 accumulation)"}
+        res = {}
+
+        def pws_once():
+            d_g, d_w, d_l, goff, gcnt = stack.prestack(ctx, torch, t, offs, cnts, n, 1, stack.MODE_PWS)
+            stack.pws(ctx, d_g, d_w, goff, gcnt, d_l, n, lin, 2.0)
+            res["g"] = d_g
+
+        ms = _timed(torch, stream, pws_once, reps=2)
+        nbytes = t.numel() * 4 * 3 + lin.numel() * 4  # traces read, groups written and read, stack written
+        out["pws"] = {"traces_per_s": npairs * ntr / (ms / 1e3), "ms": ms, "power": 2.0,
+                      "hbm_gbs_algorithmic": nbytes / (ms / 1e3) / 1e9,
+                      "hbm_frac": nbytes / (ms / 1e3) / 1e9 / hbm_gbs,
+                      "workload": f"{npairs} pairs x {ntr} traces x {n} lags, substack 1 (prestack + PWS)"}
+        res.clear()
+        # --- TF-PWS (subset) ---------------------------------------------------
+        tp = 128
+        d_g, d_w, d_l, goff, gcnt = stack.prestack(ctx, torch, t[: tp * ntr], offs[:tp], cnts[:tp], n, 10,
+                                                   stack.MODE_TFPWS)
+        o = torch.empty((tp, n), dtype=torch.float32, device=dev)
+        ms = _timed(torch, stream, lambda: stack.tfpws(ctx, d_g, d_w, goff, gcnt, d_l, n, o, 0.1, band=(0.05, 5.0)),
+                    reps=1, warm=1)
+        ng = int(gcnt[0])
+        # S-transform work: (G + 1) inverse transforms of n per (pair, frequency)
+        flops = tp * (ng + 1) * (n // 2 + 1) * 5.0 * n * np.log2(n)
+        out["tfpws"] = {"pairs_per_s": tp / (ms / 1e3), "ms": ms, "groups": ng, "pairs": tp,
+                        "fft_flops": flops, "tflops": flops / (ms / 1e3) / 1e12,
+                        "fp32_frac": flops / (ms / 1e3) / 1e12 / fp32_tflops,
+                        "extrapolated_2304_pairs_s": 2304 / (tp / (ms / 1e3)),
+                        "workload": f"{tp} pairs x {ntr} traces -> {ng} groups of 10, {n} lags, 0.05-5 Hz band"}
+        del t, lin, d_g, d_w, d_l, o
+        torch.cuda.empty_cache()
+    finally:
+        ctx.close()
+    return out
 
 
 def profile_traffic(kernel: str, workload: str):
@@ -474,15 +572,19 @@ def main():
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps}
 
+    # the step's buffers are released before the stage timings and the
+    # serving stream (which uses its own HBM arenas)
+    d_stack = d_packed = d_ncf = spec = mask = None
+    host_spec = host_ncf = hs = hn = None
+    plan = None
+    ctx.close()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    if not args.no_stages and world == 1:
+        line["stages"] = stages_run(torch, dev, local, peaks.get("hbm_gbs", 6800.0),
+                                    152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12)
     if args.serve_seconds > 0:
         # serving: a Poisson stream of correlation jobs against the engine
-        # (its own HBM arenas; the step's buffers are released first)
-        d_stack = d_packed = d_ncf = spec = mask = None
-        host_spec = host_ncf = hs = hn = None
-        plan = None
-        ctx.close()
-        torch.cuda.synchronize()
-        torch.cuda.empty_cache()
         line["serving"] = serving_run(args, local, rank)
 
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -267,13 +267,30 @@ __device__ __forceinline__ float2 tw_lookup(const float2* stw, int k) {
   return cmul(stw[kTwFine + (k >> kTwFineShift)], stw[k & (kTwFine - 1)]);
 }
 
+// x[t] *= w^(t*jt), t = 1..R-1: a table lookup for t = 1, 9, 17, ... and
+// complex products with w^jt in between (at most 7 products per lookup, so
+// the rounding stays within a few ulp); no twiddle array is kept.
+template <int R>
+__device__ __forceinline__ void apply_twiddles(const float2* stw, int jt, float2 (&x)[R]) {
+  const float2 w1 = tw_lookup(stw, jt);
+  float2 w = w1;
+#pragma unroll
+  for (int t = 1; t < R; ++t) {
+    if (t > 1) w = ((t - 1) & 7) == 0 ? tw_lookup(stw, t * jt) : cmul(w, w1);
+    x[t] = cmul(x[t], w);
+  }
+}
+
 template <int R, int T, bool DIT>
 __device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float2* stw,
                                           int tw_step, bool conj_in, bool conj_out) {
   const int nb = n / R;
   const int B = L * R;
+  // b / L by a multiply-high with m = floor(2^32 / L) + 1 (exact for b, L
+  // below 2^16 as here); L == 1 has no twiddles
+  const uint32_t m = L > 1 ? (uint32_t)(0x100000000ull / (uint32_t)L) + 1u : 0u;
   for (int b = threadIdx.x; b < nb; b += T) {
-    const int blk = b / L;
+    const int blk = L > 1 ? (int)__umulhi((uint32_t)b, m) : b;
     const int j = b - blk * L;
     const int base = blk * B + j;
     float2 x[R];
@@ -282,15 +299,9 @@ __device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float
       float2 e = buf[base + t * L];
       x[t] = conj_in ? conjf2(e) : e;
     }
-    if (DIT && j != 0) {
-#pragma unroll
-      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], tw_lookup(stw, t * j * tw_step));
-    }
+    if (DIT && j != 0) apply_twiddles<R>(stw, j * tw_step, x);
     dft_any<R>(x);
-    if (!DIT && j != 0) {
-#pragma unroll
-      for (int t = 1; t < R; ++t) x[t] = cmul(x[t], tw_lookup(stw, t * j * tw_step));
-    }
+    if (!DIT && j != 0) apply_twiddles<R>(stw, j * tw_step, x);
 #pragma unroll
     for (int t = 0; t < R; ++t) buf[base + t * L] = conj_out ? conjf2(x[t]) : x[t];
   }

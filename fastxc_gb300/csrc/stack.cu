@@ -42,16 +42,34 @@ constexpr int kStBluestein = 16384;  // longest Bluestein length (any other trac
 // linear stack and prestack
 // ---------------------------------------------------------------------------
 
-// out[p, t] = float(sum_k double(tr[off_p + k, t]) / count_p)
-__global__ void k_linear_stack(const float* __restrict__ traces, const int64_t* __restrict__ offs,
-                               const int32_t* __restrict__ counts, int n, float* __restrict__ out) {
+// out[p, t] = float(sum_k double(tr[off_p + k, t]) / count_p), the sum in
+// trace order (as _linear_stack_group accumulates). Each thread owns kLsV
+// samples (kLsT apart, coalesced) so kLsV independent FP64 chains and loads
+// are in flight per trace.
+constexpr int kLsT = 256, kLsV = 4;
+__global__ void __launch_bounds__(kLsT)
+    k_linear_stack(const float* __restrict__ traces, const int64_t* __restrict__ offs,
+                   const int32_t* __restrict__ counts, int n, float* __restrict__ out) {
   const int p = blockIdx.y;
   const int64_t off = offs[p];
   const int cnt = counts[p];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    double acc = 0.0;
-    for (int k = 0; k < cnt; ++k) acc += (double)traces[(off + k) * n + t];
-    out[(int64_t)p * n + t] = cnt > 0 ? (float)(acc / (double)cnt) : 0.f;
+  const int t0 = blockIdx.x * (kLsT * kLsV) + threadIdx.x;
+  double acc[kLsV];
+#pragma unroll
+  for (int v = 0; v < kLsV; ++v) acc[v] = 0.0;
+  const float* base = traces + off * n;
+  for (int k = 0; k < cnt; ++k) {
+    const float* row = base + (int64_t)k * n;
+#pragma unroll
+    for (int v = 0; v < kLsV; ++v) {
+      const int t = t0 + v * kLsT;
+      if (t < n) acc[v] += (double)__ldg(row + t);
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < kLsV; ++v) {
+    const int t = t0 + v * kLsT;
+    if (t < n) out[(int64_t)p * n + t] = cnt > 0 ? (float)(acc[v] / (double)cnt) : 0.f;
   }
 }
 
@@ -419,8 +437,8 @@ int fxc_linear_stack(fxc_ctx* ctx, const float* d_traces, const int64_t* h_offse
   int32_t* d_cnt = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(ctx->scratch2.ptr) + ((ob + 255) & ~size_t(255)));
   FXC_CUDA_TRY(cudaMemcpyAsync(d_off, h_offsets, ob, cudaMemcpyHostToDevice, ctx->stream));
   FXC_CUDA_TRY(cudaMemcpyAsync(d_cnt, h_counts, cb, cudaMemcpyHostToDevice, ctx->stream));
-  dim3 g((unsigned)((nsamples + 255) / 256), (unsigned)npairs);
-  k_linear_stack<<<g, 256, 0, ctx->stream>>>(d_traces, d_off, d_cnt, nsamples, d_out);
+  dim3 g((unsigned)((nsamples + kLsT * kLsV - 1) / (kLsT * kLsV)), (unsigned)npairs);
+  k_linear_stack<<<g, kLsT, 0, ctx->stream>>>(d_traces, d_off, d_cnt, nsamples, d_out);
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;
