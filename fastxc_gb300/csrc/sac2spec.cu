@@ -169,6 +169,22 @@ __device__ __forceinline__ void real_roundtrip_pointwise(float2* buf, const FftP
 // InvNormalize2DKernel weight: 1 / (width * dt) with width*dt in float.
 __host__ __device__ inline double inv_norm(int n, float dt) { return 1.0 / (double)((float)n * dt); }
 
+// Row buffer of a transform CTA: shared memory, or -- for rows longer than
+// shared memory holds (20 Hz data: 72 000-sample windows) -- this CTA's
+// slice of an L2-resident global scratch (grows != null). The stage code is
+// the same; __syncthreads orders the global accesses within the CTA. The
+// twiddle table and small arrays stay in shared memory (from smraw on).
+struct RowBuf {
+  float2* grows;
+  int64_t gelems;
+};
+__device__ __forceinline__ float2* row_buffer(float2* smraw, const RowBuf& rb) {
+  return rb.grows ? rb.grows + (int64_t)blockIdx.x * rb.gelems : smraw;
+}
+__device__ __forceinline__ float2* after_row(float2* smraw, const RowBuf& rb, int row_elems) {
+  return rb.grows ? smraw : smraw + row_elems;
+}
+
 // ---------------------------------------------------------------------------
 // k_s2s_front: window load, preprocess, prefilter, one-bit / RAM weight
 // ---------------------------------------------------------------------------
@@ -177,12 +193,13 @@ __global__ void __launch_bounds__(kS2sT, 1)
     k_s2s_front(const float* __restrict__ series, int64_t series_pitch, int64_t series_len,
                 const int* __restrict__ steps, S2sDev d, FftPlan pf, const float2* __restrict__ twf,
                 const float* __restrict__ resp, int mode, int raw_win, float* __restrict__ xout,
-                float* __restrict__ wout) {
+                float* __restrict__ wout, RowBuf rb) {
   // mode: 0 = write x only, 1 = one-bit, 2 = x and smoothed |x| weight
-  extern __shared__ float2 sbuf[];
+  extern __shared__ float2 smraw[];
   __shared__ double sred[32];
   const int Mf = pf.n;
-  float2* stw = sbuf + Mf;
+  float2* sbuf = row_buffer(smraw, rb);
+  float2* stw = after_row(smraw, rb, Mf);
   float* xs = reinterpret_cast<float*>(sbuf);
   const int r = blockIdx.x;
   const int sidx = r / d.nrows, row = r % d.nrows;
@@ -264,10 +281,11 @@ __global__ void __launch_bounds__(kS2sT, 1)
 __global__ void __launch_bounds__(kS2sT, 1)
     k_s2s_mfband(const float* __restrict__ xin, S2sDev d, FftPlan pf, const float2* __restrict__ twf,
                  const float* __restrict__ resp, int raw_win, float* __restrict__ xb,
-                 float* __restrict__ wb) {
-  extern __shared__ float2 sbuf[];
+                 float* __restrict__ wb, RowBuf rb) {
+  extern __shared__ float2 smraw[];
   const int Mf = pf.n;
-  float2* stw = sbuf + Mf;
+  float2* sbuf = row_buffer(smraw, rb);
+  float2* stw = after_row(smraw, rb, Mf);
   float* xs = reinterpret_cast<float*>(sbuf);
   const int r = blockIdx.x;
   const int seg = d.seg;
@@ -319,10 +337,11 @@ __global__ void k_s2s_mfsum(const float* __restrict__ xb, const float* __restric
 __global__ void __launch_bounds__(kS2sT, 1)
     k_s2s_whiten_a(const float* __restrict__ xin, const float* __restrict__ win_w, S2sDev d,
                    FftPlan ps, const float2* __restrict__ tws, int ww, float2* __restrict__ Xout,
-                   float* __restrict__ Aout, int64_t fpitch) {
-  extern __shared__ float2 sbuf[];
+                   float* __restrict__ Aout, int64_t fpitch, RowBuf rb) {
+  extern __shared__ float2 smraw[];
   const int Ms = ps.n;
-  float2* stw = sbuf + Ms;
+  float2* sbuf = row_buffer(smraw, rb);
+  float2* stw = after_row(smraw, rb, Ms);
   float* amp = reinterpret_cast<float*>(stw + fft_tw_smem_elems(ps));
   float* xs = reinterpret_cast<float*>(sbuf);
   const int r = blockIdx.x;
@@ -408,10 +427,11 @@ __global__ void __launch_bounds__(kS2sT, 1)
                    S2sDev d, FftPlan ps, const float2* __restrict__ tws, FftPlan po,
                    const float2* __restrict__ two, int to_time, int time_mode, int raw_win,
                    float* __restrict__ xout, float* __restrict__ wout, float2* __restrict__ out,
-                   int64_t out_pitch) {
-  extern __shared__ float2 sbuf[];
+                   int64_t out_pitch, RowBuf rb) {
+  extern __shared__ float2 smraw[];
   const int Mbuf = max(ps.n, po.n);
-  float2* stw = sbuf + Mbuf;
+  float2* sbuf = row_buffer(smraw, rb);
+  float2* stw = after_row(smraw, rb, Mbuf);
   float* xs = reinterpret_cast<float*>(sbuf);
   const int r = blockIdx.x;
   const int row = r % d.nrows;
@@ -467,10 +487,11 @@ __global__ void __launch_bounds__(kS2sT, 1)
 __global__ void __launch_bounds__(kS2sT, 1)
     k_s2s_output(const float* __restrict__ xin, const float* __restrict__ win_w, S2sDev d,
                  FftPlan po, const float2* __restrict__ two, float2* __restrict__ out,
-                 int64_t out_pitch) {
-  extern __shared__ float2 sbuf[];
+                 int64_t out_pitch, RowBuf rb) {
+  extern __shared__ float2 smraw[];
   const int Mo = po.n;
-  float2* stw = sbuf + Mo;
+  float2* sbuf = row_buffer(smraw, rb);
+  float2* stw = after_row(smraw, rb, Mo);
   float* xs = reinterpret_cast<float*>(sbuf);
   const int r = blockIdx.x;
   const int row = r % d.nrows;
@@ -490,8 +511,8 @@ __global__ void __launch_bounds__(kS2sT, 1)
 // ---------------------------------------------------------------------------
 
 static int make_real_plan(int n, FftPlan* p, const float2** tw) {
-  FXC_CHECK_ARG(n % 2 == 0 && n / 2 <= kFftLargeNmax, "real transform length %d not supported "
-                "(must be even and at most %d)", n, 2 * kFftLargeNmax);
+  FXC_CHECK_ARG(n % 2 == 0 && n / 2 <= 65536, "real transform length %d not supported (must be even and "
+                "at most 131072)", n);
   FXC_TRY(fft_twiddles(n, tw));
   return fft_make_plan(n / 2, *tw, 2, p);
 }
@@ -671,9 +692,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   const int seg = plan->segment_pts;
   const bool wh_before = plan->whiten == 1 || plan->whiten == 3;
   const bool wh_after = plan->whiten == 2 || plan->whiten == 3;
-  if (wh_before || wh_after)
-    FXC_CHECK_ARG(seg % 2 == 0 && seg / 2 <= kFftLargeNmax,
-                  "whitening needs an even segment length <= %d (got %d)", 2 * kFftLargeNmax, seg);
+  if (wh_before || wh_after) FXC_CHECK_ARG(seg % 2 == 0, "whitening needs an even segment length (got %d)", seg);
   for (int i = 0; i < nsteps; ++i)
     FXC_CHECK_ARG(h_steps[i] >= 0 && h_steps[i] < plan->nstep, "step %d out of range", h_steps[i]);
   const int64_t nr = (int64_t)nsteps * nrows;
@@ -735,17 +754,36 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   const size_t rpitch = (size_t)plan->filter_nfft / 2 + 1;
   const float* resp0 = d_responses;
 
-  const size_t smf = sizeof(float2) * ((size_t)pf.n + fft_tw_smem_elems(pf));
-  const size_t smo = sizeof(float2) * ((size_t)po.n + fft_tw_smem_elems(po));
+  // shared memory of each transform kernel: [row buffer] + twiddles (+ the
+  // whitening amplitude row); a kernel whose total exceeds one CTA's shared
+  // memory keeps its row buffer in the L2-resident global scratch instead
   const int Mbuf = (wh_before || wh_after) ? std::max(ps.n, po.n) : po.n;
-  const size_t smb = sizeof(float2) * ((size_t)Mbuf + std::max(fft_tw_smem_elems(po),
-                                       (wh_before || wh_after) ? fft_tw_smem_elems(ps) : 0));
-  const size_t sma = (wh_before || wh_after)
-                         ? sizeof(float2) * ((size_t)ps.n + fft_tw_smem_elems(ps)) +
-                               sizeof(float) * (size_t)(ps.n + 1)
-                         : 0;
-  FXC_CHECK_ARG(smf <= 227 * 1024 && smo <= 227 * 1024 && smb <= 227 * 1024 && sma <= 227 * 1024,
-                "row transform too long for one CTA's shared memory");
+  const size_t twf_b = sizeof(float2) * fft_tw_smem_elems(pf), two_b = sizeof(float2) * fft_tw_smem_elems(po);
+  const size_t tws_b = (wh_before || wh_after) ? sizeof(float2) * fft_tw_smem_elems(ps) : 0;
+  const size_t amp_b = (wh_before || wh_after) ? sizeof(float) * (size_t)(ps.n + 1) : 0;
+  const size_t kSmemMax = 227 * 1024;
+  struct Sm {
+    size_t row, rest;
+    bool global() const { return row + rest > 227 * 1024; }
+    size_t bytes() const { return global() ? rest : row + rest; }
+  };
+  const Sm smf_{sizeof(float2) * (size_t)pf.n, twf_b};
+  const Sm smo_{sizeof(float2) * (size_t)po.n, two_b};
+  const Sm smb_{sizeof(float2) * (size_t)Mbuf, std::max(two_b, tws_b)};
+  const Sm sma_{sizeof(float2) * (size_t)((wh_before || wh_after) ? ps.n : 0), tws_b + amp_b};
+  FXC_CHECK_ARG(smf_.rest <= kSmemMax && smo_.rest <= kSmemMax && smb_.rest <= kSmemMax && sma_.rest <= kSmemMax,
+                "transform tables too large for one CTA's shared memory");
+  int64_t gelems = 0;
+  for (const Sm* k : {&smf_, &smo_, &smb_, &sma_})
+    if (k->global()) gelems = std::max<int64_t>(gelems, (int64_t)(k->row / sizeof(float2)));
+  float2* grows = nullptr;
+  if (gelems > 0) {
+    gelems = (gelems + 31) / 32 * 32;
+    FXC_TRY(ctx->scratch.reserve(sizeof(float2) * (size_t)nr * (size_t)gelems));
+    grows = reinterpret_cast<float2*>(ctx->scratch.ptr);
+  }
+  auto rb_of = [&](const Sm& k) { return RowBuf{k.global() ? grows : nullptr, gelems}; };
+  const size_t smf = smf_.bytes(), smo = smo_.bytes(), smb = smb_.bytes(), sma = sma_.bytes();
 
   // front: preprocess + prefilter (+ one-bit / RAM weight unless whitening comes first)
   int mode = 0;
@@ -756,7 +794,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   FXC_TRY(set_smem_limit(k_s2s_front, smf));
   k_s2s_front<<<(unsigned)nr, kS2sT, smf, ctx->stream>>>(d_series, series_pitch, series_len,
                                                          d_steps, d, pf, twf, resp0, mode,
-                                                         plan->runabs_win, x, w);
+                                                         plan->runabs_win, x, w, rb_of(smf_));
   count_launch();
   FXC_LAUNCH_CHECK();
   const float* wgt = (mode == 2) ? w : nullptr;
@@ -764,7 +802,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   if (wh_before) {
     FXC_TRY(set_smem_limit(k_s2s_whiten_a, sma));
     k_s2s_whiten_a<<<(unsigned)nr, kS2sT, sma, ctx->stream>>>(x, nullptr, d, ps, tws,
-                                                              plan->whiten_win, X, A, fpitch);
+                                                              plan->whiten_win, X, A, fpitch, rb_of(sma_));
     count_launch();
     FXC_LAUNCH_CHECK();
     int tmode = 0;
@@ -773,7 +811,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
     FXC_TRY(set_smem_limit(k_s2s_whiten_b, smb));
     k_s2s_whiten_b<<<(unsigned)nr, kS2sT, smb, ctx->stream>>>(X, A, fpitch, d, ps, tws, po, two, 1,
                                                               tmode, plan->runabs_win, x, w,
-                                                              nullptr, 0);
+                                                              nullptr, 0, rb_of(smb_));
     count_launch();
     FXC_LAUNCH_CHECK();
     wgt = (tmode == 2) ? w : nullptr;
@@ -788,7 +826,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
       if (win < 1) win = 1;
       k_s2s_mfband<<<(unsigned)nr, kS2sT, smf, ctx->stream>>>(
           x, d, pf, twf, resp0 + (size_t)(b + 1) * rpitch, win, xb + (size_t)b * nr * seg,
-          wb + (size_t)b * nr * seg);
+          wb + (size_t)b * nr * seg, rb_of(smf_));
       count_launch();
       FXC_LAUNCH_CHECK();
     }
@@ -803,18 +841,19 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   if (wh_after) {
     FXC_TRY(set_smem_limit(k_s2s_whiten_a, sma));
     k_s2s_whiten_a<<<(unsigned)nr, kS2sT, sma, ctx->stream>>>(x, wgt, d, ps, tws, plan->whiten_win,
-                                                              X, A, fpitch);
+                                                              X, A, fpitch, rb_of(sma_));
     count_launch();
     FXC_LAUNCH_CHECK();
     FXC_TRY(set_smem_limit(k_s2s_whiten_b, smb));
     k_s2s_whiten_b<<<(unsigned)nr, kS2sT, smb, ctx->stream>>>(X, A, fpitch, d, ps, tws, po, two, 0,
                                                               0, 0, nullptr, nullptr, out,
-                                                              out_pitch);
+                                                              out_pitch, rb_of(smb_));
     count_launch();
     FXC_LAUNCH_CHECK();
   } else {
     FXC_TRY(set_smem_limit(k_s2s_output, smo));
-    k_s2s_output<<<(unsigned)nr, kS2sT, smo, ctx->stream>>>(x, wgt, d, po, two, out, out_pitch);
+    k_s2s_output<<<(unsigned)nr, kS2sT, smo, ctx->stream>>>(x, wgt, d, po, two, out, out_pitch,
+                                                            rb_of(smo_));
     count_launch();
     FXC_LAUNCH_CHECK();
   }

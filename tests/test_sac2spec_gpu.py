@@ -129,3 +129,15 @@ def test_sac2spec_rejects_bad_steps(ctx, torch_cuda):
 
     with pytest.raises(FxcError):
         run_case(ctx, torch_cuda, "filter_d0.1_0.1-2.txt", 0.1, so.WHITEN_AFTER, so.NORM_RUNABS, 0, [24])
+
+
+@pytest.mark.parametrize("whiten,normalize", [(so.WHITEN_AFTER, so.NORM_RUNABS), (so.WHITEN_BOTH, so.NORM_NONE)])
+def test_sac2spec_20hz_rows_above_shared_memory(ctx, torch_cuda, whiten, normalize):
+    """delta 0.05 s with 3600-s windows: 72 000-sample rows (output nfft
+    74 088) whose transforms exceed one CTA's shared memory and run on the
+    L2-resident global row buffer."""
+    torch = torch_cuda
+    got, ref = run_case(ctx, torch, "filter_d0.05_0.05-5.txt", 0.05, whiten, normalize, 0, [0, 7], nsta=2)
+    err = row_err(got, ref)
+    print("20 Hz rows rel err", err.max())
+    assert err.max() < 1e-5
