@@ -34,6 +34,7 @@
 //      the context's device error word, the CTA drains its copies and frees
 //      TMEM before it exits.
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <vector>
 
@@ -69,6 +70,7 @@ struct XcTensorPlan {
   int64_t ntiles = 0;
   TcTile* d_tiles = nullptr;
   int32_t* d_maps = nullptr;  // per tile [128][n]: p, -(p+2) for a reversed pair, -1 none
+  std::vector<TcTile> h_tiles;
 };
 
 static int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
@@ -134,6 +136,7 @@ int xc_tensor_plan_init(fxc_ctx*, fxc_pairplan* plan) {
     }
   }
   tp->ntiles = (int64_t)tiles.size();
+  tp->h_tiles = tiles;
   if (!tiles.empty()) {
     cudaError_t e1 = cudaMalloc(&tp->d_tiles, sizeof(TcTile) * tiles.size());
     cudaError_t e2 = cudaMalloc(&tp->d_maps, sizeof(int32_t) * maps.size());
@@ -566,6 +569,242 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   (void)nspec;
 }
 
+// ---------------------------------------------------------------------------
+// Whole-bin GEMM for up to 192 channels
+// ---------------------------------------------------------------------------
+// When the channel count C <= 192 the upper triangle of one bin is at most
+// two tiles: T0 = rows [0, 128) x cols [0, C) and T1 = rows [128, C) x cols
+// [128, C). Their four FP32 accumulators (Re/Im, N0 + N1 <= 256 columns
+// each) fill the 512 TMEM columns exactly, so one CTA computes the whole
+// bin from ONE load of the bin's C rows per K-block: the stage buffer holds
+// 256 rows per (plane, 8-window chunk) -- rows [C, 256) stay zero -- and
+// the four operands are descriptors into it (A0 = rows 0..127, B0 = rows
+// 0..N0-1, A1 = rows 128..255, B1 = rows 128..128+N1-1). Against one CTA
+// per (tile, bin) this halves the operand traffic and pays the per-CTA
+// setup and the epilogue once per bin.
+constexpr int kBinRows = 256;
+constexpr int kBinStages = 3;
+constexpr int kBinStageBytes = kTcPlanes * kTcKc * kBinRows * 16;  // 64 KB
+constexpr size_t kBinSmemBytes = (size_t)kBinStages * kBinStageBytes + 256;
+static_assert(kBinSmemBytes <= 227 * 1024, "whole-bin ring exceeds shared memory");
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_xc_tc_gemm_bin(const uint4* __restrict__ packed, int nkb, int cpad, int nchan,
+                     const TcTile* __restrict__ tiles, int ntiles, const int32_t* __restrict__ maps,
+                     float scale, float2* __restrict__ stack, int64_t stack_pitch, int accumulate,
+                     int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* stage_base = smem;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)kBinStages * kBinStageBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kBinStages + 1);
+  const uint32_t bar_full0 = smem_u32(bars);
+  const uint32_t bar_empty0 = smem_u32(bars + kBinStages);
+  const uint32_t bar_acc = smem_u32(bars + 2 * kBinStages);
+  const int f = blockIdx.x;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const TcTile t0 = tiles[0];
+  const bool two = ntiles > 1;
+  const int n0 = t0.n, n1 = two ? tiles[1].n : 0;
+  const uint32_t chunk_bytes = (uint32_t)kBinRows * 16;  // one (plane, kc) chunk
+
+  // zero the rows the copies never write (C .. 255) of every chunk once
+  for (int s = 0; s < kBinStages; ++s) {
+    uint4* st = reinterpret_cast<uint4*>(stage_base + (size_t)s * kBinStageBytes);
+    const int per = kBinRows - nchan;
+    for (int i = threadIdx.x; i < kTcPlanes * kTcKc * per; i += kTcThreads) {
+      const int ch = i / per, r = nchan + i % per;
+      st[(size_t)ch * kBinRows + r] = make_uint4(0, 0, 0, 0);
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kBinStages; ++s) {
+      mbar_init(bar_full0 + 8 * s, 1);
+      mbar_init(bar_empty0 + 8 * s, 1);
+    }
+    mbar_init(bar_acc, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  // TMEM columns: T0 Re [0, n0), T0 Im [n0, 2 n0), T1 Re [2 n0, 2 n0 + n1), T1 Im after
+  const uint32_t c_re0 = 0, c_im0 = (uint32_t)n0, c_re1 = 2u * n0, c_im1 = 2u * n0 + n1;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t tx = (uint32_t)kTcPlanes * kTcKc * (uint32_t)nchan * 16u;
+      int issued = 0;
+      bool failed = false;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kBinStages;
+        const uint32_t ph = (uint32_t)(kb / kBinStages) & 1u;
+        if (!mbar_wait(bar_empty0 + 8 * s, ph ^ 1u)) {
+          failed = true;
+          break;
+        }
+        const uint32_t full = bar_full0 + 8 * s;
+        mbar_expect_tx(full, tx);
+        const uint32_t st = smem_u32(stage_base + (size_t)s * kBinStageBytes);
+        for (int pl = 0; pl < kTcPlanes; ++pl) {
+          const int64_t pbase = (((int64_t)f * kTcPlanes + pl) * nkb + kb) * kTcKc * cpad;
+          for (int kc = 0; kc < kTcKc; ++kc)
+            bulk_g2s(st + (pl * kTcKc + kc) * chunk_bytes, packed + pbase + (int64_t)kc * cpad,
+                     (uint32_t)nchan * 16u, full);
+        }
+        ++issued;
+      }
+      if (failed) {
+        atomicExch(err, 1);
+        const int lo = issued > kBinStages ? issued - kBinStages : 0;
+        for (int kb = lo; kb < issued; ++kb)
+          (void)mbar_wait(bar_full0 + 8 * (kb % kBinStages), (uint32_t)(kb / kBinStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idp0 = umma_idesc(kTcM, n0, false), idn0 = umma_idesc(kTcM, n0, true);
+      const uint32_t idp1 = umma_idesc(kTcM, two ? n1 : 16, false), idn1 = umma_idesc(kTcM, two ? n1 : 16, true);
+      const uint32_t lbo = kTcKc * chunk_bytes / kTcKc;  // next 8-window chunk of the same plane
+      const uint32_t sbo = 128;
+      bool failed = false;
+      bool first = true;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kBinStages;
+        const uint32_t ph = (uint32_t)(kb / kBinStages) & 1u;
+        if (!mbar_wait(bar_full0 + 8 * s, ph)) {
+          failed = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem_u32(stage_base + (size_t)s * kBinStageBytes);
+#pragma unroll
+        for (int ks = 0; ks < kTcKc / 2; ++ks) {
+          uint64_t P0[4], P1[4];  // rows 0.. and rows 128.. of each plane at this K step
+#pragma unroll
+          for (int pl = 0; pl < 4; ++pl) {
+            const uint32_t base = st + (pl * kTcKc + ks * 2) * chunk_bytes;
+            P0[pl] = umma_desc(base, lbo, sbo);
+            P1[pl] = umma_desc(base + kTcM * 16, lbo, sbo);
+          }
+          const uint32_t acc = first ? 0u : 1u;
+          // tile 0: rows 0..127 x cols 0..n0-1
+          umma_bf16(tmem + c_re0, P0[0], P0[0], idp0, acc);
+          umma_bf16(tmem + c_re0, P0[0], P0[1], idp0, 1);
+          umma_bf16(tmem + c_re0, P0[1], P0[0], idp0, 1);
+          umma_bf16(tmem + c_re0, P0[2], P0[2], idp0, 1);
+          umma_bf16(tmem + c_re0, P0[2], P0[3], idp0, 1);
+          umma_bf16(tmem + c_re0, P0[3], P0[2], idp0, 1);
+          umma_bf16(tmem + c_im0, P0[0], P0[2], idp0, acc);
+          umma_bf16(tmem + c_im0, P0[0], P0[3], idp0, 1);
+          umma_bf16(tmem + c_im0, P0[1], P0[2], idp0, 1);
+          umma_bf16(tmem + c_im0, P0[2], P0[0], idn0, 1);
+          umma_bf16(tmem + c_im0, P0[2], P0[1], idn0, 1);
+          umma_bf16(tmem + c_im0, P0[3], P0[0], idn0, 1);
+          if (two) {
+            // tile 1: rows 128..255 (zero past C) x cols 128..128+n1-1
+            umma_bf16(tmem + c_re1, P1[0], P1[0], idp1, acc);
+            umma_bf16(tmem + c_re1, P1[0], P1[1], idp1, 1);
+            umma_bf16(tmem + c_re1, P1[1], P1[0], idp1, 1);
+            umma_bf16(tmem + c_re1, P1[2], P1[2], idp1, 1);
+            umma_bf16(tmem + c_re1, P1[2], P1[3], idp1, 1);
+            umma_bf16(tmem + c_re1, P1[3], P1[2], idp1, 1);
+            umma_bf16(tmem + c_im1, P1[0], P1[2], idp1, acc);
+            umma_bf16(tmem + c_im1, P1[0], P1[3], idp1, 1);
+            umma_bf16(tmem + c_im1, P1[1], P1[2], idp1, 1);
+            umma_bf16(tmem + c_im1, P1[2], P1[0], idn1, 1);
+            umma_bf16(tmem + c_im1, P1[2], P1[1], idn1, 1);
+            umma_bf16(tmem + c_im1, P1[3], P1[0], idn1, 1);
+          }
+          first = false;
+        }
+        umma_commit(bar_empty0 + 8 * s);
+      }
+      if (failed) atomicExch(err, 1);
+      umma_commit(bar_acc);
+    }
+  } else {
+    // epilogue: lane quarter q = warp % 4 holds rows q*32.. of both tiles;
+    // the two warps of a quarter take alternate 16-column chunks of the
+    // combined column space [0, n0) + [n0, n0 + n1)
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const bool ok = mbar_wait(bar_acc, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+      atomicExch(err, 1);
+    } else {
+      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+      const int ncols = n0 + n1;
+      for (int cc = 16 * half; cc < ncols; cc += 32) {
+        const bool in1 = cc >= n0;  // warp-uniform
+        const int c0 = in1 ? cc - n0 : cc;
+        const TcTile& tt = in1 ? tiles[1] : t0;
+        const int n = in1 ? n1 : n0;
+        float re[16], im[16];
+        tmem_ld16(lane_base + (in1 ? c_re1 : c_re0) + (uint32_t)c0, re);
+        tmem_ld16(lane_base + (in1 ? c_im1 : c_im0) + (uint32_t)c0, im);
+        tmem_ld_wait();
+        const int row = q * 32 + lane;
+        if (row < tt.am) {
+          const int4* m4 = reinterpret_cast<const int4*>(maps + tt.map_offset + (int64_t)row * n + c0);
+          int32_t mv[16];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const int4 t = __ldg(m4 + v);
+            mv[4 * v] = t.x;
+            mv[4 * v + 1] = t.y;
+            mv[4 * v + 2] = t.z;
+            mv[4 * v + 3] = t.w;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int32_t v = mv[j];
+            if (v != -1) {
+              const bool rev = v < -1;
+              const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
+              const float im_s = rev ? -im[j] : im[j];
+              float2* dst = stack + p * stack_pitch + f;
+              float2 o = make_float2(re[j] * scale, im_s * scale);
+              if (accumulate) {
+                const float2 prev = *dst;
+                o.x += prev.x;
+                o.y += prev.y;
+              }
+              *dst = o;
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// True when the plan's tiles are exactly the whole-bin geometry (C <= 192,
+// no duplicated pairs needing extra tile layers).
+static bool whole_bin_plan(const XcTensorPlan* tp) {
+  const int C = tp->nchan;
+  if (C < 1 || C > 192 || tp->h_tiles.empty()) return false;
+  const auto& t = tp->h_tiles;
+  if (C <= kTcM) return t.size() == 1 && t[0].a0 == 0 && t[0].b0 == 0 && t[0].am == C && t[0].bn == C;
+  return t.size() == 2 && t[0].a0 == 0 && t[0].b0 == 0 && t[0].am == kTcM && t[0].bn == C && t[1].a0 == kTcM &&
+         t[1].b0 == kTcM && t[1].am == C - kTcM && t[1].bn == C - kTcM;
+}
+
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
   const int64_t nkb = (nwin + kTcKb - 1) / kTcKb;
   return (int64_t)nspec * kTcPlanes * nkb * kTcKc * round_up(nchan, 8);
@@ -603,6 +842,15 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
     FXC_CUDA_TRY(cudaMemset2DAsync(stack, sizeof(float2) * (size_t)stack_pitch, 0,
                                    sizeof(float2) * (size_t)nspec, (size_t)plan->npairs,
                                    ctx->stream));
+    return FXC_OK;
+  }
+  if (whole_bin_plan(tp) && !getenv("FXC_GEMM_TILED")) {
+    FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin, kBinSmemBytes));
+    k_xc_tc_gemm_bin<<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
+        packed, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, stack, stack_pitch,
+        accumulate, ctx->d_err);
+    count_launch();
+    FXC_LAUNCH_CHECK();
     return FXC_OK;
   }
   FXC_TRY(set_smem_limit(k_xc_tc_gemm, kTcSmemBytes));
