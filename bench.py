@@ -500,13 +500,16 @@ def main():
             for b0 in range(a0, nchan, 256):
                 sum_n += (min(256, nchan - b0) + 15) // 16 * 16
         issued = float(nspec) * nkb * 24 * 2 * 128 * 16 * sum_n
+        # up to 192 channels one CTA runs both triangle tiles of a bin
+        gemm_kernel = ("k_xc_tc_gemm_bin" if nchan <= 192 and not os.environ.get("FXC_GEMM_TILED")
+                       else "k_xc_tc_gemm")
         kms = hr["stack_ms"]
         achieved = issued / (kms / 1e3) / 1e12
         peak = peaks.get("bf16_tflops_sustained", 1700.0)
         peak_src = ("measured sustained bf16 (cuBLAS, MEASURED_PEAKS.json)" if "bf16_tflops_sustained" in peaks
                     else "fallback 1.7 PFLOP/s sustained")
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": profile_traffic("k_xc_tc_gemm", wkey), "peak_source": peak_src, "kernel": "k_xc_tc_gemm",
+                    "traffic": profile_traffic(gemm_kernel, wkey), "peak_source": peak_src, "kernel": gemm_kernel,
                     "algorithmic": "issued MMA flops = nspec x ceil(nwin/32) x 24 x (2 x 128 x 16 x n) summed over tiles "
                                    "(3 bf16 hi/lo products, Re and Im, upper-triangle tiles)",
                     "useful_tflops": useful_flop / (kms / 1e3) / 1e12, "kernel_ms": kms,
