@@ -263,22 +263,31 @@ __global__ void __launch_bounds__(256, 1)
   if (!colok) return;
   const int f = f0 + col;
   const int32_t* map = maps + tile.map_offset;
+  // per row of 8 pairs: the previous values (accumulate) are loaded together
+  // before any store -- the pairs are distinct -- so a row costs one DRAM
+  // round trip rather than eight
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < 8; ++i) {
+    int64_t off[8];
+    float2 v[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int32_t p = __ldg(map + (qa * 8 + i) * kXcTile + qb * 8 + j);
-      if (p >= 0) {
-        float2* dst = stack + (int64_t)p * stack_pitch + f;
-        float2 v = make_float2(acc[i][j].x * scale, acc[i][j].y * scale);
-        if (accumulate) {
-          const float2 o = *dst;
-          v.x += o.x;
-          v.y += o.y;
-        }
-        *dst = v;
+      off[j] = p >= 0 ? (int64_t)p * stack_pitch + f : -1;
+      v[j] = make_float2(acc[i][j].x * scale, acc[i][j].y * scale);
+    }
+    if (accumulate) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float2 o = off[j] >= 0 ? __ldcg(stack + off[j]) : make_float2(0.f, 0.f);
+        v[j].x += o.x;
+        v[j].y += o.y;
       }
     }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (off[j] >= 0) stack[off[j]] = v[j];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -504,6 +513,34 @@ int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
 
 int64_t xc_stack_pitch(int nspec) { return (int64_t)((nspec + 3) / 4) * 4; }
 
+// dst[i] += src[i] over n complex values, two per thread step (n even: the
+// stack pitch is a multiple of 4 bins)
+__global__ void __launch_bounds__(256) k_xc_stack_add(float4* __restrict__ dst, const float4* __restrict__ src,
+                                                      int64_t n4) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    const float4 a = __ldcs(src + i);
+    float4 b = dst[i];
+    b.x += a.x;
+    b.y += a.y;
+    b.z += a.z;
+    b.w += a.w;
+    dst[i] = b;
+  }
+}
+
+int xc_stack_add_launch(fxc_ctx* ctx, float2* dst, const float2* src, int64_t n) {
+  if (n <= 0) return FXC_OK;
+  FXC_CHECK_ARG(n % 2 == 0, "stack add length %lld is odd", (long long)n);
+  const int64_t n4 = n / 2;
+  const int64_t blocks = std::min<int64_t>((n4 + 255) / 256, (int64_t)ctx->num_sms * 8);
+  k_xc_stack_add<<<(unsigned)blocks, 256, 0, ctx->stream>>>(reinterpret_cast<float4*>(dst),
+                                                            reinterpret_cast<const float4*>(src), n4);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
 }  // namespace fxc
 
 using namespace fxc;
@@ -642,29 +679,53 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   FXC_CHECK_ARG(h_spec != nullptr && h_ncf != nullptr, "null host pointer");
   FXC_CHECK_ARG(method == FXC_XC_PLAIN || method == FXC_XC_TENSOR, "unknown xc method %d", method);
   if (plan->npairs == 0) return FXC_OK;
-  // The windows stream through a ring of device buffers on a copy stream;
-  // each chunk is packed (tensor) or stacked with accumulation (plain) on the
-  // compute stream as soon as it lands, so the host-to-device copy -- the
-  // bound of this call -- overlaps the compute.
+  // The windows stream through a ring of device buffers on a copy stream and
+  // are consumed on the compute stream as they land, so the host-to-device
+  // copy -- the bound of this call -- hides most of the compute:
+  //   plain   each chunk is stacked into the running sum (the plain kernel's
+  //           read-modify-write is coalesced along the bins);
+  //   tensor  each chunk is packed as it lands; a group of up to
+  //           kGroupChunks chunks is contracted into a partial stack, which
+  //           a coalesced add folds into the running one. The last chunk is
+  //           a group of its own, so what follows the last copy is one
+  //           chunk's contraction, one add, the finalize and the last NCF
+  //           block's copy back.
   const int nspec = shape->nspec;
   const int64_t wchunk = 64;  // windows per chunk (two 32-window K-blocks)
   const int kRing = 3;
+  const int64_t kGroupChunks = 4;
+  const int64_t nchunks = (nwin + wchunk - 1) / wchunk;
+  const bool tensor = method == FXC_XC_TENSOR;
   const size_t row_bytes = sizeof(float2) * (size_t)nchan * (size_t)spec_pitch;  // one window
   const size_t chunk_bytes = row_bytes * (size_t)wchunk;
   const size_t mask_bytes = h_mask ? (size_t)nwin * (size_t)nchan : 0;
   const size_t ncf_bytes = sizeof(float) * (size_t)plan->npairs * (size_t)shape->cc_size;
+  const int64_t pitch = xc_stack_pitch(nspec);
+  const size_t stack_bytes = sizeof(float2) * (size_t)pitch * (size_t)plan->npairs;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t off_mask = al(chunk_bytes) * kRing;
   const size_t off_ncf = off_mask + al(mask_bytes);
-  FXC_TRY(ctx->scratch2.reserve(off_ncf + ncf_bytes));
+  const size_t off_part = off_ncf + al(ncf_bytes);
+  FXC_TRY(ctx->scratch2.reserve(off_part + (tensor && nchunks > 1 ? stack_bytes : 0)));
   char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
-  const int64_t pitch = xc_stack_pitch(nspec);
-  FXC_TRY(ctx->scratch.reserve(sizeof(float2) * (size_t)pitch * (size_t)plan->npairs));
+  FXC_TRY(ctx->scratch.reserve(stack_bytes));
   float2* stack = reinterpret_cast<float2*>(ctx->scratch.ptr);
+  float2* partial = reinterpret_cast<float2*>(base + off_part);
+  // tensor groups: chunk c closes a group when it is the last or the
+  // next-to-last chunk, or the kGroupChunks-th of its group
+  std::vector<int64_t> group_first((size_t)std::max<int64_t>(nchunks, 1), 0);
   uint4* packed = nullptr;
-  if (method == FXC_XC_TENSOR) {
+  if (tensor) {
     FXC_CHECK_ARG(plan->tensor != nullptr, "pair plan has no tensor tiles");
-    const int64_t chunks = xc_packed_chunks(nchan, nwin, nspec);
+    int64_t first = 0, most = 0;
+    for (int64_t c = 0; c < nchunks; ++c) {
+      group_first[(size_t)c] = first;
+      if (c >= nchunks - 2 || c + 1 - first == kGroupChunks) {
+        most = std::max(most, std::min(nwin, (c + 1) * wchunk) - first * wchunk);
+        first = c + 1;
+      }
+    }
+    const int64_t chunks = xc_packed_chunks(nchan, most, nspec);  // the largest group's operands
     if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
     packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
   }
@@ -673,7 +734,6 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   // the copy stream starts after work already queued on the compute stream
   cudaEvent_t start_ev;
   FXC_CUDA_TRY(cudaEventCreateWithFlags(&start_ev, cudaEventDisableTiming));
-  const int64_t nchunks = (nwin + wchunk - 1) / wchunk;
   std::vector<cudaEvent_t> landed((size_t)kRing), used((size_t)kRing);
   for (int r = 0; r < kRing; ++r) {
     cudaEventCreateWithFlags(&landed[r], cudaEventDisableTiming);
@@ -694,6 +754,9 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
     cuda_ok(cudaMemcpyAsync(base + off_mask, h_mask, mask_bytes, cudaMemcpyHostToDevice, cs));
     d_mask = reinterpret_cast<const uint8_t*>(base + off_mask);
   }
+  if (nchunks == 0)  // no windows: every stacked bin is zero
+    cuda_ok(cudaMemset2DAsync(stack, sizeof(float2) * (size_t)pitch, 0, sizeof(float2) * (size_t)nspec,
+                              (size_t)plan->npairs, ctx->stream));
   for (int64_t c = 0; c < nchunks && rc == FXC_OK; ++c) {
     const int r = (int)(c % kRing);
     const int64_t w0 = c * wchunk, nw = std::min(wchunk, nwin - w0);
@@ -705,21 +768,47 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
     cuda_ok(cudaStreamWaitEvent(ctx->stream, landed[r], 0));
     if (rc != FXC_OK) break;
     const float2* spec = reinterpret_cast<const float2*>(slot);
-    if (method == FXC_XC_TENSOR) {
-      rc = xc_pack_launch(ctx, spec, nwin, nchan, nspec, spec_pitch, d_mask, packed, (int)(w0 / kTcKbWindows),
-                          (int)((w0 + nw + kTcKbWindows - 1) / kTcKbWindows), w0);
+    if (tensor) {
+      // pack into the group's operand layout; the slot is free again once
+      // packed (the GEMM reads the packed copy)
+      const int64_t g0 = group_first[(size_t)c];
+      const bool closes = c == nchunks - 1 || group_first[(size_t)c + 1] == c + 1;
+      const int64_t gw0 = g0 * wchunk;
+      int64_t glast = c;  // the group's last chunk
+      while (glast < nchunks - 1 && group_first[(size_t)glast + 1] == g0) ++glast;
+      const int64_t gnw = std::min(nwin, (glast + 1) * wchunk) - gw0;
+      const int kb0 = (int)((w0 - gw0) / kTcKbWindows);
+      const int kb1 = (int)((w0 - gw0 + nw + kTcKbWindows - 1) / kTcKbWindows);
+      rc = xc_pack_launch(ctx, spec, gnw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)gw0 * nchan : nullptr,
+                          packed, kb0, kb1, w0 - gw0);
+      cuda_ok(cudaEventRecord(used[r], ctx->stream));
+      if (rc == FXC_OK && closes) {
+        const bool first_group = g0 == 0;
+        rc = xc_gemm_launch(ctx, plan, packed, gnw, nspec, scale, first_group ? stack : partial, pitch);
+        if (rc == FXC_OK && !first_group) rc = xc_stack_add_launch(ctx, stack, partial, plan->npairs * pitch);
+      }
     } else {
-      rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch,
-                           d_mask ? d_mask + (size_t)w0 * nchan : nullptr, scale, stack, pitch, FXC_XC_PLAIN,
-                           c > 0);
+      rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,
+                           scale, stack, pitch, FXC_XC_PLAIN, c > 0);
+      cuda_ok(cudaEventRecord(used[r], ctx->stream));
     }
-    cuda_ok(cudaEventRecord(used[r], ctx->stream));
   }
-  if (rc == FXC_OK && method == FXC_XC_TENSOR)
-    rc = xc_gemm_launch(ctx, plan, packed, nwin, nspec, scale, stack, pitch);
+  // finalize in pair blocks; each block's NCFs go back on the copy stream
+  // while the next block is transformed
   float* d_ncf = reinterpret_cast<float*>(base + off_ncf);
-  if (rc == FXC_OK) rc = xc_finalize_launch(ctx, stack, plan->npairs, pitch, shape, d_ncf);
-  if (rc == FXC_OK) cuda_ok(cudaMemcpyAsync(h_ncf, d_ncf, ncf_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  const int64_t nblk = std::min<int64_t>(4, plan->npairs);
+  const int64_t per_blk = (plan->npairs + nblk - 1) / nblk;
+  for (int64_t b = 0; b < nblk && rc == FXC_OK; ++b) {
+    const int64_t p0 = b * per_blk, np = std::min(per_blk, plan->npairs - p0);
+    if (np <= 0) break;
+    const size_t off = (size_t)p0 * (size_t)shape->cc_size;
+    rc = xc_finalize_launch(ctx, stack + (size_t)p0 * (size_t)pitch, np, pitch, shape, d_ncf + off);
+    const int r = (int)(b % kRing);
+    cuda_ok(cudaEventRecord(landed[r], ctx->stream));
+    cuda_ok(cudaStreamWaitEvent(cs, landed[r], 0));
+    cuda_ok(cudaMemcpyAsync(h_ncf + off, d_ncf + off, sizeof(float) * (size_t)np * (size_t)shape->cc_size,
+                            cudaMemcpyDeviceToHost, cs));
+  }
   cudaStreamSynchronize(cs);
   cudaStreamSynchronize(ctx->stream);
   cudaEventDestroy(start_ev);

@@ -305,6 +305,38 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   }
 }
 
+// Scatter 16 accumulator columns of one TMEM row to the stack: column j goes
+// to pair p = mv[j] (conjugated for -(p + 2), skipped for -1) at bin f. With
+// accumulate the 16 previous values are all loaded before any store -- the
+// pairs of a row are distinct, and issuing the loads together keeps one DRAM
+// round trip per call instead of one per pair.
+__device__ __forceinline__ void store_pairs16(float2* __restrict__ stack, int64_t stack_pitch, int64_t f,
+                                              const int32_t* mv, const float* re, const float* im, float scale,
+                                              int accumulate) {
+  int64_t off[16];
+  float2 o[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int32_t v = mv[j];
+    const bool rev = v < -1;
+    off[j] = v == -1 ? -1 : (rev ? (int64_t)(-v - 2) : (int64_t)v) * stack_pitch + f;
+    o[j] = make_float2(re[j] * scale, (rev ? -im[j] : im[j]) * scale);
+  }
+  if (accumulate) {
+    float2 prev[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) prev[j] = off[j] >= 0 ? __ldcg(stack + off[j]) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      o[j].x += prev[j].x;
+      o[j].y += prev[j].y;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    if (off[j] >= 0) stack[off[j]] = o[j];
+}
+
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
                                          uint32_t bar) {
   asm volatile(
@@ -535,26 +567,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tmem_ld16(lane_base + (uint32_t)c0, re);
         tmem_ld16(lane_base + kTcAccImCol + (uint32_t)c0, im);
         tmem_ld_wait();
-        if (row_ok) {
-          const int32_t* mv = reinterpret_cast<const int32_t*>(mcur);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int32_t v = mv[j];  // padding columns (b >= bn) hold -1
-            if (v != -1) {
-              const bool rev = v < -1;
-              const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
-              const float im_s = rev ? -im[j] : im[j];
-              float2* dst = stack + p * stack_pitch + f;
-              float2 v = make_float2(re[j] * scale, im_s * scale);
-              if (accumulate) {
-                const float2 o = *dst;
-                v.x += o.x;
-                v.y += o.y;
-              }
-              *dst = v;
-            }
-          }
-        }
+        if (row_ok)  // padding columns (b >= bn) hold -1
+          store_pairs16(stack, stack_pitch, f, reinterpret_cast<const int32_t*>(mcur), re, im, scale,
+                        accumulate);
 #pragma unroll
         for (int k = 0; k < 4; ++k) mcur[k] = mnxt[k];
       }
@@ -765,23 +780,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mv[4 * v + 2] = t.z;
             mv[4 * v + 3] = t.w;
           }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int32_t v = mv[j];
-            if (v != -1) {
-              const bool rev = v < -1;
-              const int64_t p = rev ? (int64_t)(-v - 2) : (int64_t)v;
-              const float im_s = rev ? -im[j] : im[j];
-              float2* dst = stack + p * stack_pitch + f;
-              float2 o = make_float2(re[j] * scale, im_s * scale);
-              if (accumulate) {
-                const float2 prev = *dst;
-                o.x += prev.x;
-                o.y += prev.y;
-              }
-              *dst = o;
-            }
-          }
+          store_pairs16(stack, stack_pitch, f, mv, re, im, scale, accumulate);
         }
       }
     }

@@ -165,12 +165,15 @@ def test_empty_pair_list(ctx, torch_cuda):
     ctx.synchronize()
 
 
-@pytest.mark.parametrize("nwin,method,masked", [(4, 0, False), (150, 0, True), (150, 1, True), (200, 1, False)])
+@pytest.mark.parametrize("nwin,method,masked",
+                         [(4, 0, False), (150, 0, True), (150, 1, True), (200, 1, False), (400, 1, True)])
 def test_host_entry_matches_oracle_and_device_entry(ctx, torch_cuda, nwin, method, masked):
     """The host-buffer entry streams windows in 64-window chunks through a
-    ring of device buffers (ragged last chunk, gap mask): same NCFs as the
-    FP64 oracle; the tensor method packs chunk by chunk and equals the
-    device entry bit for bit."""
+    ring of device buffers (ragged last chunk, gap mask) and stacks them as
+    they land -- chunk by chunk (plain), or in groups of up to four chunks
+    folded into the running stack (tensor; 400 windows make groups of 4, 2
+    and 1 chunks): same NCFs as the FP64 oracle, and as the device entry up
+    to the FP32 summation order."""
     rng = np.random.default_rng(5)
     nsta, nspec = 4, 1001
     spec = make_spec(rng, nwin, 3 * nsta, nspec)
@@ -182,8 +185,7 @@ def test_host_entry_matches_oracle_and_device_entry(ctx, torch_cuda, nwin, metho
     ctx.xc_run_host(plan, spec, nwin, 3 * nsta, nspec, mask, 1.0 / nwin, shape, host, method)
     ref = xo.xc_run(spec, src, rec, 1.0 / nwin, xo.finalize_shape(nspec, nwin, 0.1, 20.0), mask=mask)
     assert per_row_rel_l2(host, ref).max() < NCF_RTOL
-    if method == 1:
-        assert np.array_equal(host, dev)
+    assert per_row_rel_l2(host, dev).max() < 1e-5
 
 
 def test_bad_arguments_raise(ctx, torch_cuda):
