@@ -146,6 +146,7 @@ int fxc_ctx_destroy(fxc_ctx* ctx) {
   ctx->scratch2.release();
   ctx->scratch3.release();
   ctx->scratch4.release();
+  ctx->scratch5.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   delete ctx;

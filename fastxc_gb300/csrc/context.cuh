@@ -27,6 +27,7 @@ struct fxc_ctx {
   fxc::Scratch scratch2;  // host-call staging (device copies of host inputs)
   fxc::Scratch scratch3;  // packed bf16 hi/lo operands of the tensor-core path
   fxc::Scratch scratch4;  // sac2spec intermediate rows (time rows, weights, spectra)
+  fxc::Scratch scratch5;  // bin-major stack rows of the whole-bin tensor-core contraction
   int* d_err = nullptr;   // device error word: set by kernels whose bounded waits time out
   cudaStream_t copy_stream = nullptr;  // host<->device copies of the host-buffer entry points
 };

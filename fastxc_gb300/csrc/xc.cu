@@ -685,11 +685,12 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   //   plain   each chunk is stacked into the running sum (the plain kernel's
   //           read-modify-write is coalesced along the bins);
   //   tensor  each chunk is packed as it lands; a group of up to
-  //           kGroupChunks chunks is contracted into a partial stack, which
-  //           a coalesced add folds into the running one. The last chunk is
-  //           a group of its own, so what follows the last copy is one
-  //           chunk's contraction, one add, the finalize and the last NCF
-  //           block's copy back.
+  //           kGroupChunks chunks is contracted and accumulated into the
+  //           running stack (the whole-bin contraction accumulates in its
+  //           coalesced transpose; the tiled one writes a partial stack that
+  //           a coalesced add folds in). The last chunk is a group of its
+  //           own, so what follows the last copy is one chunk's contraction,
+  //           the finalize and the last NCF block's copy back.
   const int nspec = shape->nspec;
   const int64_t wchunk = 64;  // windows per chunk (two 32-window K-blocks)
   const int kRing = 3;
@@ -706,7 +707,8 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   const size_t off_mask = al(chunk_bytes) * kRing;
   const size_t off_ncf = off_mask + al(mask_bytes);
   const size_t off_part = off_ncf + al(ncf_bytes);
-  FXC_TRY(ctx->scratch2.reserve(off_part + (tensor && nchunks > 1 ? stack_bytes : 0)));
+  const bool use_partial = tensor && nchunks > 1 && !xc_gemm_accumulate_is_cheap(plan);
+  FXC_TRY(ctx->scratch2.reserve(off_part + (use_partial ? stack_bytes : 0)));
   char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
   FXC_TRY(ctx->scratch.reserve(stack_bytes));
   float2* stack = reinterpret_cast<float2*>(ctx->scratch.ptr);
@@ -784,8 +786,12 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
       cuda_ok(cudaEventRecord(used[r], ctx->stream));
       if (rc == FXC_OK && closes) {
         const bool first_group = g0 == 0;
-        rc = xc_gemm_launch(ctx, plan, packed, gnw, nspec, scale, first_group ? stack : partial, pitch);
-        if (rc == FXC_OK && !first_group) rc = xc_stack_add_launch(ctx, stack, partial, plan->npairs * pitch);
+        if (first_group || !use_partial) {
+          rc = xc_gemm_launch(ctx, plan, packed, gnw, nspec, scale, stack, pitch, first_group ? 0 : 1);
+        } else {
+          rc = xc_gemm_launch(ctx, plan, packed, gnw, nspec, scale, partial, pitch);
+          if (rc == FXC_OK) rc = xc_stack_add_launch(ctx, stack, partial, plan->npairs * pitch);
+        }
       }
     } else {
       rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,

@@ -606,12 +606,18 @@ static_assert(kBinSmemBytes <= 227 * 1024, "whole-bin ring exceeds shared memory
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_xc_tc_gemm_bin(const uint4* __restrict__ packed, int nkb, int cpad, int nchan,
                      const TcTile* __restrict__ tiles, int ntiles, const int32_t* __restrict__ maps,
-                     float scale, float2* __restrict__ stack, int64_t stack_pitch, int accumulate,
+                     float scale, float2* __restrict__ binmajor, int64_t bin_pitch, int npairs,
                      int* __restrict__ err) {
+  // Output: row f of the bin-major stack, binmajor[f * bin_pitch + p] for
+  // p < npairs. Once every MMA has completed the operand stages are idle, so
+  // the epilogue scatters the pairs into them by pair index and then writes
+  // the row out in contiguous 16-byte stores (the [pair][bin] layout would
+  // need one 8-byte store per pair, each in a sector of its own).
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* stage_base = smem;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)kBinStages * kBinStageBytes);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kBinStages + 1);
+  int* epi_failed = reinterpret_cast<int*>(tmem_slot + 1);
   const uint32_t bar_full0 = smem_u32(bars);
   const uint32_t bar_empty0 = smem_u32(bars + kBinStages);
   const uint32_t bar_acc = smem_u32(bars + 2 * kBinStages);
@@ -638,6 +644,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(bar_empty0 + 8 * s, 1);
     }
     mbar_init(bar_acc, 1);
+    *epi_failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -750,12 +757,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // epilogue: lane quarter q = warp % 4 holds rows q*32.. of both tiles;
     // the two warps of a quarter take alternate 16-column chunks of the
     // combined column space [0, n0) + [n0, n0 + n1)
+    // Every epilogue thread reaches the named barrier below whether or not
+    // its bounded wait succeeded; a failure anywhere skips the write-out.
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
+    float2* sout = reinterpret_cast<float2*>(stage_base);  // [npairs], stages idle after the last MMA
     const bool ok = mbar_wait(bar_acc, 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok) {
       atomicExch(err, 1);
+      atomicExch(epi_failed, 1);
     } else {
       const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
       const int ncols = n0 + n1;
@@ -780,9 +791,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mv[4 * v + 2] = t.z;
             mv[4 * v + 3] = t.w;
           }
-          store_pairs16(stack, stack_pitch, f, mv, re, im, scale, accumulate);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int32_t v = mv[j];
+            if (v != -1) {
+              const bool rev = v < -1;
+              sout[rev ? -v - 2 : v] = make_float2(re[j] * scale, (rev ? -im[j] : im[j]) * scale);
+            }
+          }
         }
       }
+    }
+    asm volatile("bar.sync 1, %0;" ::"n"(kTcThreads - 64) : "memory");
+    if (*epi_failed == 0) {
+      // pairs [0, npairs) as float4 pairs; an odd count writes one padding
+      // element of the row (bin_pitch is a multiple of 4)
+      const float4* src4 = reinterpret_cast<const float4*>(sout);
+      float4* dst4 = reinterpret_cast<float4*>(binmajor + (int64_t)f * bin_pitch);
+      for (int i = threadIdx.x - 64; i < (npairs + 1) / 2; i += kTcThreads - 64) dst4[i] = src4[i];
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -790,6 +816,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// Bin-major rows -> the [pair][bin] stack: stack[p][f] (+)= binmajor[f][p],
+// through 32 x 32 shared-memory tiles so both sides move in 256-byte runs.
+__global__ void __launch_bounds__(256)
+    k_xc_binmajor_to_stack(const float2* __restrict__ binmajor, int64_t bin_pitch, int64_t npairs, int nspec,
+                           float2* __restrict__ stack, int64_t stack_pitch, int accumulate) {
+  __shared__ float2 tile[32][33];
+  const int64_t p0 = (int64_t)blockIdx.x * 32;
+  const int f0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = ty; k < 32; k += 8) {
+    const int f = f0 + k;
+    const int64_t p = p0 + tx;
+    if (f < nspec && p < npairs) tile[k][tx] = __ldcs(binmajor + (int64_t)f * bin_pitch + p);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t p = p0 + k;
+    const int f = f0 + tx;
+    if (p < npairs && f < nspec) {
+      float2 v = tile[tx][k];
+      float2* d = stack + p * stack_pitch + f;
+      if (accumulate) {
+        const float2 o = *d;
+        v.x += o.x;
+        v.y += o.y;
+      }
+      *d = v;
+    }
   }
 }
 
@@ -802,6 +861,13 @@ static bool whole_bin_plan(const XcTensorPlan* tp) {
   if (C <= kTcM) return t.size() == 1 && t[0].a0 == 0 && t[0].b0 == 0 && t[0].am == C && t[0].bn == C;
   return t.size() == 2 && t[0].a0 == 0 && t[0].b0 == 0 && t[0].am == kTcM && t[0].bn == C && t[1].a0 == kTcM &&
          t[1].b0 == kTcM && t[1].am == C - kTcM && t[1].bn == C - kTcM;
+}
+
+bool xc_gemm_accumulate_is_cheap(const fxc_pairplan* plan) {
+  // the whole-bin contraction accumulates in its coalesced transpose; the
+  // tiled one in scattered 8-byte read-modify-writes
+  return plan->tensor && whole_bin_plan(plan->tensor) &&
+         plan->npairs * (int64_t)sizeof(float2) <= (int64_t)kBinStages * kBinStageBytes && !getenv("FXC_GEMM_TILED");
 }
 
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
@@ -843,11 +909,20 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
                                    ctx->stream));
     return FXC_OK;
   }
-  if (whole_bin_plan(tp) && !getenv("FXC_GEMM_TILED")) {
+  if (xc_gemm_accumulate_is_cheap(plan)) {
+    // bin-major rows in context scratch, then transposed into the stack
+    const int64_t bin_pitch = round_up(plan->npairs, 4);
+    FXC_TRY(ctx->scratch5.reserve(sizeof(float2) * (size_t)bin_pitch * (size_t)nspec));
+    float2* binmajor = reinterpret_cast<float2*>(ctx->scratch5.ptr);
     FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin, kBinSmemBytes));
     k_xc_tc_gemm_bin<<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
-        packed, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, stack, stack_pitch,
-        accumulate, ctx->d_err);
+        packed, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, binmajor, bin_pitch,
+        (int)plan->npairs, ctx->d_err);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    const dim3 tg((unsigned)((plan->npairs + 31) / 32), (unsigned)((nspec + 31) / 32));
+    k_xc_binmajor_to_stack<<<tg, 256, 0, ctx->stream>>>(binmajor, bin_pitch, plan->npairs, nspec, stack,
+                                                         stack_pitch, accumulate);
     count_launch();
     FXC_LAUNCH_CHECK();
     return FXC_OK;

@@ -113,6 +113,41 @@ def test_stack_matches_oracle_with_mask_and_ragged_tiles(ctx, torch_cuda, method
     assert np.all(d_stack.cpu().numpy()[:, nspec:] == 0)
 
 
+@pytest.mark.parametrize("nchan", [150, 192, 96])
+def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, monkeypatch):
+    """Up to 192 channels one CTA contracts a whole bin and writes it as a
+    bin-major row that a transpose moves into the stack. An odd number of
+    pairs, autocorrelations, reversed (conjugated) pairs and a shuffled pair
+    order; same stack as the FP64 oracle and as the tiled contraction."""
+    torch = torch_cuda
+    from fastxc_gb300.core import PairPlan
+
+    rng = np.random.default_rng(17)
+    nwin, nspec = 40, 257
+    spec = make_spec(rng, nwin, nchan, nspec)
+    iu, ju = np.triu_indices(nchan)
+    keep = rng.random(iu.size) < 0.3
+    src, rec = iu[keep].astype(np.int32), ju[keep].astype(np.int32)
+    if src.size % 2 == 0:
+        src, rec = src[:-1], rec[:-1]
+    flip = rng.random(src.size) < 0.3
+    src, rec = np.where(flip, rec, src).astype(np.int32), np.where(flip, src, rec).astype(np.int32)
+    perm = rng.permutation(src.size)
+    src, rec = src[perm], rec[perm]
+    plan = PairPlan(ctx, src, rec, nchan)
+    d_spec = torch.from_numpy(spec).cuda()
+    a = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+    b = torch.zeros_like(a)
+    ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, a, nspec, 1)
+    monkeypatch.setenv("FXC_GEMM_TILED", "1")
+    ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, b, nspec, 1)
+    monkeypatch.delenv("FXC_GEMM_TILED")
+    ctx.synchronize()
+    ref = xo.xc_stack(spec, src, rec, 0.5)
+    assert rel_l2(a.cpu().numpy(), ref) < 2e-5
+    assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+
+
 def test_packed_resident_path_equals_tensor_stack(ctx, torch_cuda):
     """fxc_xc_pack + fxc_xc_stack_packed (spectra kept in packed form) gives
     bit-identical stacks to fxc_xc_stack(FXC_XC_TENSOR), for two pair plans
