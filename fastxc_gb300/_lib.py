@@ -62,6 +62,8 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_version": (_int, []),
     "fxc_launch_count": (_i64, []),
     "fxc_launch_count_reset": (None, []),
+    "fxc_ctx_kernel_timing": (_int, [_vp, _int]),
+    "fxc_ctx_kernel_time": (_int, [_vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(_i64)]),
     "fxc_ctx_create": (_int, [_int, _vp, C.POINTER(_vp)]),
     "fxc_ctx_destroy": (_int, [_vp]),
     "fxc_ctx_set_stream": (_int, [_vp, _vp]),

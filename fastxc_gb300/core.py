@@ -54,6 +54,17 @@ class Context:
     def synchronize(self) -> None:
         lib().fxc_ctx_synchronize(self.handle)
 
+    def kernel_timing(self, enable: bool) -> None:
+        """Bracket the dominant kernels' launches with CUDA events (or stop)."""
+        lib().fxc_ctx_kernel_timing(self.handle, int(bool(enable)))
+
+    def kernel_time(self, kernel: str) -> tuple[float, int]:
+        """(summed ms, launches) of `kernel` since the last query."""
+        ms = C.c_double()
+        n = C.c_int64()
+        lib().fxc_ctx_kernel_time(self.handle, kernel.encode(), C.byref(ms), C.byref(n))
+        return ms.value, n.value
+
     def close(self) -> None:
         if self._h:
             lib().fxc_ctx_destroy(self._h)

@@ -138,10 +138,57 @@ int fxc_ctx_create(int device, void* stream, fxc_ctx** out) {
   return FXC_OK;
 }
 
+static void ktime_drop(fxc_ctx* ctx) {
+  for (auto& r : ctx->ktimes) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+  }
+  ctx->ktimes.clear();
+}
+
+int fxc_ctx_kernel_timing(fxc_ctx* ctx, int enable) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  if (!enable) {
+    cudaStreamSynchronize(ctx->stream);
+    ktime_drop(ctx);
+  }
+  ctx->ktime_on = enable != 0;
+  return FXC_OK;
+}
+
+int fxc_ctx_kernel_time(fxc_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(kernel && total_ms && launches, "null argument");
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  double sum = 0.0;
+  int64_t n = 0;
+  std::vector<KernelTimeRec> keep;
+  for (auto& r : ctx->ktimes) {
+    if (r.name == kernel) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, r.start, r.stop) == cudaSuccess) {
+        sum += ms;
+        ++n;
+      }
+      cudaEventDestroy(r.start);
+      cudaEventDestroy(r.stop);
+    } else {
+      keep.push_back(r);
+    }
+  }
+  ctx->ktimes.swap(keep);
+  *total_ms = sum;
+  *launches = n;
+  return FXC_OK;
+}
+
 int fxc_ctx_destroy(fxc_ctx* ctx) {
   if (!ctx) return FXC_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  ktime_drop(ctx);
   ctx->scratch.release();
   ctx->scratch2.release();
   ctx->scratch3.release();

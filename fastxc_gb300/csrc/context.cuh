@@ -1,6 +1,9 @@
 // Context object behind the opaque fxc_ctx handle.
 #pragma once
 
+#include <string>
+#include <vector>
+
 #include "fxc_common.cuh"
 
 namespace fxc {
@@ -19,6 +22,13 @@ int ctx_check_device_error(fxc_ctx* ctx);
 
 }  // namespace fxc
 
+namespace fxc {
+struct KernelTimeRec {
+  std::string name;
+  cudaEvent_t start, stop;
+};
+}  // namespace fxc
+
 struct fxc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -30,4 +40,40 @@ struct fxc_ctx {
   fxc::Scratch scratch5;  // bin-major stack rows of the whole-bin tensor-core contraction
   int* d_err = nullptr;   // device error word: set by kernels whose bounded waits time out
   cudaStream_t copy_stream = nullptr;  // host<->device copies of the host-buffer entry points
+  bool ktime_on = false;               // fxc_ctx_kernel_timing
+  std::vector<fxc::KernelTimeRec> ktimes;
 };
+
+namespace fxc {
+// Brackets one launch with events on the context stream while kernel timing
+// is enabled (a no-op otherwise): construct before the launch, stop() after.
+struct KernelTimer {
+  fxc_ctx* ctx;
+  const char* name;
+  cudaEvent_t start = nullptr;
+  KernelTimer(fxc_ctx* c, const char* n) : ctx(c), name(n) {
+    if (ctx->ktime_on && cudaEventCreate(&start) == cudaSuccess) {
+      if (cudaEventRecord(start, ctx->stream) != cudaSuccess) {
+        cudaEventDestroy(start);
+        start = nullptr;
+      }
+    } else {
+      start = nullptr;
+    }
+  }
+  void stop() {
+    if (!start) return;
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) == cudaSuccess && cudaEventRecord(e, ctx->stream) == cudaSuccess) {
+      ctx->ktimes.push_back(KernelTimeRec{name, start, e});
+    } else {
+      if (e) cudaEventDestroy(e);
+      cudaEventDestroy(start);
+    }
+    start = nullptr;
+  }
+  ~KernelTimer() {
+    if (start) cudaEventDestroy(start);
+  }
+};
+}  // namespace fxc

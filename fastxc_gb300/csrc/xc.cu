@@ -684,19 +684,21 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   // copy -- the bound of this call -- hides most of the compute:
   //   plain   each chunk is stacked into the running sum (the plain kernel's
   //           read-modify-write is coalesced along the bins);
-  //   tensor  each chunk is packed as it lands; a group of up to
-  //           kGroupChunks chunks is contracted and accumulated into the
-  //           running stack (the whole-bin contraction accumulates in its
-  //           coalesced transpose; the tiled one writes a partial stack that
-  //           a coalesced add folds in). The last chunk is a group of its
-  //           own, so what follows the last copy is one chunk's contraction,
-  //           the finalize and the last NCF block's copy back.
+  //   tensor  each chunk is packed as it lands and contracted into the
+  //           running stack: chunk by chunk for the whole-bin contraction
+  //           (it accumulates in its coalesced transpose), in groups of up
+  //           to four chunks for the tiled one (a partial stack that a
+  //           coalesced add folds in). The last chunk is a group of its own,
+  //           so what follows the last copy is one chunk's contraction, the
+  //           finalize and the last NCF block's copy back.
   const int nspec = shape->nspec;
   const int64_t wchunk = 64;  // windows per chunk (two 32-window K-blocks)
   const int kRing = 3;
-  const int64_t kGroupChunks = 4;
   const int64_t nchunks = (nwin + wchunk - 1) / wchunk;
   const bool tensor = method == FXC_XC_TENSOR;
+  // a contraction whose accumulate is cheap runs per chunk; otherwise per
+  // group of chunks, to spread the partial-stack add
+  const int64_t kGroupChunks = tensor && xc_gemm_accumulate_is_cheap(plan) ? 1 : 4;
   const size_t row_bytes = sizeof(float2) * (size_t)nchan * (size_t)spec_pitch;  // one window
   const size_t chunk_bytes = row_bytes * (size_t)wchunk;
   const size_t mask_bytes = h_mask ? (size_t)nwin * (size_t)nchan : 0;

@@ -762,6 +762,27 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
     float2* sout = reinterpret_cast<float2*>(stage_base);  // [npairs], stages idle after the last MMA
+    const int ncols = n0 + n1;
+    const int row = q * 32 + lane;
+    const TcTile t1 = two ? tiles[1] : t0;
+    // the pair map of a 16-column chunk (-1 where the row has no pair); the
+    // next chunk's map is in flight while the current one is scattered, and
+    // the first one while the MMAs run
+    auto load_map = [&](int cc, int4 (&m)[4]) {
+      const bool in1 = cc >= n0;
+      const TcTile& tt = in1 ? t1 : t0;
+      if (cc < ncols && row < tt.am) {
+        const int4* m4 = reinterpret_cast<const int4*>(maps + tt.map_offset + (int64_t)row * (in1 ? n1 : n0) +
+                                                       (in1 ? cc - n0 : cc));
+#pragma unroll
+        for (int v = 0; v < 4; ++v) m[v] = __ldg(m4 + v);
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) m[v] = make_int4(-1, -1, -1, -1);
+      }
+    };
+    int4 mcur[4], mnext[4];
+    load_map(16 * half, mcur);
     const bool ok = mbar_wait(bar_acc, 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok) {
@@ -769,37 +790,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       atomicExch(epi_failed, 1);
     } else {
       const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-      const int ncols = n0 + n1;
       for (int cc = 16 * half; cc < ncols; cc += 32) {
+        load_map(cc + 32, mnext);
         const bool in1 = cc >= n0;  // warp-uniform
         const int c0 = in1 ? cc - n0 : cc;
-        const TcTile& tt = in1 ? tiles[1] : t0;
-        const int n = in1 ? n1 : n0;
         float re[16], im[16];
         tmem_ld16(lane_base + (in1 ? c_re1 : c_re0) + (uint32_t)c0, re);
         tmem_ld16(lane_base + (in1 ? c_im1 : c_im0) + (uint32_t)c0, im);
         tmem_ld_wait();
-        const int row = q * 32 + lane;
-        if (row < tt.am) {
-          const int4* m4 = reinterpret_cast<const int4*>(maps + tt.map_offset + (int64_t)row * n + c0);
-          int32_t mv[16];
+        const int32_t* mv = reinterpret_cast<const int32_t*>(mcur);
 #pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            const int4 t = __ldg(m4 + v);
-            mv[4 * v] = t.x;
-            mv[4 * v + 1] = t.y;
-            mv[4 * v + 2] = t.z;
-            mv[4 * v + 3] = t.w;
-          }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int32_t v = mv[j];
-            if (v != -1) {
-              const bool rev = v < -1;
-              sout[rev ? -v - 2 : v] = make_float2(re[j] * scale, (rev ? -im[j] : im[j]) * scale);
-            }
+        for (int j = 0; j < 16; ++j) {
+          const int32_t v = mv[j];
+          if (v != -1) {
+            const bool rev = v < -1;
+            sout[rev ? -v - 2 : v] = make_float2(re[j] * scale, (rev ? -im[j] : im[j]) * scale);
           }
         }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) mcur[v] = mnext[v];
       }
     }
     asm volatile("bar.sync 1, %0;" ::"n"(kTcThreads - 64) : "memory");
@@ -915,9 +924,11 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
     FXC_TRY(ctx->scratch5.reserve(sizeof(float2) * (size_t)bin_pitch * (size_t)nspec));
     float2* binmajor = reinterpret_cast<float2*>(ctx->scratch5.ptr);
     FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin, kBinSmemBytes));
+    KernelTimer kt(ctx, "k_xc_tc_gemm_bin");
     k_xc_tc_gemm_bin<<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
         packed, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, binmajor, bin_pitch,
         (int)plan->npairs, ctx->d_err);
+    kt.stop();
     count_launch();
     FXC_LAUNCH_CHECK();
     const dim3 tg((unsigned)((plan->npairs + 31) / 32), (unsigned)((nspec + 31) / 32));
@@ -929,9 +940,11 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
   }
   FXC_TRY(set_smem_limit(k_xc_tc_gemm, kTcSmemBytes));
   dim3 gg((unsigned)tp->ntiles, (unsigned)nspec);
+  KernelTimer kt(ctx, "k_xc_tc_gemm");
   k_xc_tc_gemm<<<gg, kTcThreads, kTcSmemBytes, ctx->stream>>>(
       packed, nkb, tp->cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, accumulate,
       ctx->d_err);
+  kt.stop();
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;

@@ -60,6 +60,16 @@ int fxc_version(void);
 int64_t fxc_launch_count(void);
 void fxc_launch_count_reset(void);
 
+/* Per-kernel device timing (a measurement aid with no counterpart in the
+ * reference). While enabled on a context, the library brackets the launches
+ * of its dominant kernels (currently the tensor-core contraction,
+ * "k_xc_tc_gemm_bin" / "k_xc_tc_gemm") with CUDA events on the context
+ * stream. fxc_ctx_kernel_time synchronises that stream, returns the summed
+ * event time and launch count of the named kernel since the last query and
+ * forgets them. Disabling drops every pending record. */
+int fxc_ctx_kernel_timing(fxc_ctx *ctx, int enable);
+int fxc_ctx_kernel_time(fxc_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches);
+
 /* Create a context bound to `device`. `stream` is a cudaStream_t (NULL = the
  * legacy default stream). The context owns its scratch buffers and FFT
  * tables. */

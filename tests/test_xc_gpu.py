@@ -200,15 +200,19 @@ def test_empty_pair_list(ctx, torch_cuda):
     ctx.synchronize()
 
 
-@pytest.mark.parametrize("nwin,method,masked",
-                         [(4, 0, False), (150, 0, True), (150, 1, True), (200, 1, False), (400, 1, True)])
-def test_host_entry_matches_oracle_and_device_entry(ctx, torch_cuda, nwin, method, masked):
+@pytest.mark.parametrize("nwin,method,masked,tiled",
+                         [(4, 0, False, False), (150, 0, True, False), (150, 1, True, False),
+                          (200, 1, False, False), (400, 1, True, False), (400, 1, True, True)])
+def test_host_entry_matches_oracle_and_device_entry(ctx, torch_cuda, nwin, method, masked, tiled, monkeypatch):
     """The host-buffer entry streams windows in 64-window chunks through a
     ring of device buffers (ragged last chunk, gap mask) and stacks them as
-    they land -- chunk by chunk (plain), or in groups of up to four chunks
-    folded into the running stack (tensor; 400 windows make groups of 4, 2
-    and 1 chunks): same NCFs as the FP64 oracle, and as the device entry up
-    to the FP32 summation order."""
+    they land: chunk by chunk (plain, and the whole-bin tensor contraction),
+    or in groups of up to four chunks whose partial stacks are added to the
+    running one (the tiled tensor contraction; 400 windows make groups of 4,
+    2 and 1 chunks). Same NCFs as the FP64 oracle, and as the device entry
+    up to the FP32 summation order."""
+    if tiled:
+        monkeypatch.setenv("FXC_GEMM_TILED", "1")
     rng = np.random.default_rng(5)
     nsta, nspec = 4, 1001
     spec = make_spec(rng, nwin, 3 * nsta, nspec)
@@ -264,3 +268,27 @@ def test_20hz_long_transform(ctx, torch_cuda, method):
     got, _ = run_xc(ctx, torch_cuda, spec, src, rec, shape, 1.0 / nwin, method=method)
     ref = xo.xc_run(spec, src, rec, 1.0 / nwin, xo.finalize_shape(nspec, nwin, 0.05, 200.0))
     assert per_row_rel_l2(got, ref).max() < NCF_RTOL
+
+
+def test_kernel_timing_counts_contraction_launches(ctx, torch_cuda):
+    """fxc_ctx_kernel_timing brackets each contraction launch with events;
+    the query returns their count and summed time once, then forgets them."""
+    torch = torch_cuda
+    from fastxc_gb300.core import PairPlan
+
+    rng = np.random.default_rng(8)
+    nwin, nchan, nspec = 40, 24, 301
+    spec = make_spec(rng, nwin, nchan, nspec)
+    src, rec = station_pairs(8)
+    plan = PairPlan(ctx, src, rec, nchan)
+    d_spec = torch.from_numpy(spec).cuda()
+    d_stack = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+    ctx.kernel_timing(True)
+    for _ in range(3):
+        ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 1.0, d_stack, nspec, 1)
+    ms, n = ctx.kernel_time("k_xc_tc_gemm_bin")
+    assert n == 3 and ms > 0.0
+    assert ctx.kernel_time("k_xc_tc_gemm_bin") == (0.0, 0)
+    ctx.kernel_timing(False)
+    ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 1.0, d_stack, nspec, 1)
+    assert ctx.kernel_time("k_xc_tc_gemm_bin") == (0.0, 0)
