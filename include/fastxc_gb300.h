@@ -244,6 +244,20 @@ int fxc_xc_run_host(fxc_ctx *ctx, const fxc_pairplan *plan, const float *h_spec,
                     int32_t nchan, int64_t spec_pitch, const uint8_t *h_mask, float scale,
                     const fxc_xc_shape *shape, float *h_ncf, int method);
 
+/* ---- ENZ -> RTZ rotation of nine-component NCFs ------------------------- */
+
+/* The 9 x 9 float32 matrix of build_rotate_matrix
+ * (fastxc/operators/rotation/python_rotate.py:33-95), row-major: rows R-R,
+ * R-T, R-Z, T-R, T-T, T-Z, Z-R, Z-T, Z-Z; columns E-E, E-N, E-Z, N-E, N-N,
+ * N-Z, Z-E, Z-N, Z-Z. Host function (no device work). */
+int fxc_rotate_matrix(double azimuth_deg, double back_azimuth_deg, float *out81);
+
+/* d_rtz[p][r][t] = sum_c d_mats[p][r][c] * d_enz[p][c][t] for npairs pairs
+ * of nine traces ([npairs][9][pitch] float32, npts samples used) --
+ * rotate_enz_to_rtz (python_rotate.py:98-105) batched over pairs. */
+int fxc_rotate_enz_rtz(fxc_ctx *ctx, const float *d_enz, int64_t npairs, int32_t npts, int64_t pitch,
+                       const float *d_mats, float *d_rtz);
+
 /* ---- stacking: linear stack, PWS, TF-PWS -------------------------------- */
 
 /* Cross-timestamp linear stack (_linear_stack_group,

@@ -18,7 +18,14 @@ copied):  python tests/golden/make_golden.py
                         records;
   formats_golden.json   a stepack batch written by fastxc_gb300.formats as
                         parsed by the reference's fastxc/tools/extract_stepack.py,
-                        and a SAC header encoded by fastxc/io/sac_binary.py.
+                        and a SAC header encoded by fastxc/io/sac_binary.py;
+  operators_golden.json / operators_rtz.npz
+                        the reference's SourcePack materializer
+                        (fastxc/operators/sourcepack/builder.py), linear stack
+                        (fastxc/operators/stacking/linear_stack.py) and ENZ->RTZ
+                        rotation (fastxc/operators/rotation/python_rotate.py)
+                        run in sequence on the seeded workspace of
+                        operators_case.py; absolute paths become {ROOT}.
 """
 
 from __future__ import annotations
@@ -276,5 +283,77 @@ def formats_case():
     return chans, spec
 
 
+def ref_packages():
+    """The reference's Python sub-packages, loaded without the top-level
+    package __init__ (which pulls in the inventory and pandas)."""
+    import importlib
+    import types
+
+    sys.path.insert(0, str(REF_ROOT))
+    for name in ("fastxc", "fastxc.operators", "fastxc.inventory"):
+        if name not in sys.modules:
+            m = types.ModuleType(name)
+            m.__path__ = [str(REF_ROOT / name.replace(".", "/"))]
+            sys.modules[name] = m
+    return (importlib.import_module("fastxc.operators.sourcepack.builder"),
+            importlib.import_module("fastxc.operators.stacking.linear_stack"),
+            importlib.import_module("fastxc.operators.rotation.python_rotate"))
+
+
+def operators_golden() -> None:
+    import hashlib
+    import tempfile
+
+    sys.path.insert(0, str(HERE))
+    import operators_case as oc
+
+    builder, linear, rotate = ref_packages()
+    out: dict = {}
+    with tempfile.TemporaryDirectory() as td:
+        root = Path(td).resolve()
+        ncf = oc.make_xc_workspace(root)
+        res = builder.build_sourcepack(ncf, root / "sourcepack")
+        out["materializer"] = {
+            "result": [res.record_count, res.source_count, res.bytes_indexed],
+            "files": {p.relative_to(root).as_posix(): oc.normalize(p.read_text(), root)
+                      for p in sorted((root / "sourcepack").rglob("*")) if p.is_file()},
+        }
+        indexes = sorted((root / "sourcepack").glob("*/sourcepack_index.tsv"))
+        lres = linear.linear_stack_sourcepack_indexes(indexes, root / "stack")
+        ldir = root / "stack" / "linearstack_sourcepack" / "STACK"
+        out["linear"] = {
+            "results": [[oc.normalize(str(r.input_path), root), oc.normalize(str(r.output_path), root),
+                         r.segment_count, r.sample_count] for r in lres],
+            "index": oc.normalize((ldir / "sourcepack_index.tsv").read_text(), root),
+            "success": oc.normalize((ldir / "_SUCCESS").read_text(), root),
+            "pack_sha256": hashlib.sha256((ldir / "linearstack.pack").read_bytes()).hexdigest(),
+        }
+        rres = rotate.rotate_linearstack_sourcepack(root)
+        rdir = root / "stack" / "rtz_linearstack_sourcepack" / "STACK"
+        raw = (rdir / "rtz_linearstack.pack").read_bytes()
+        rec = 632 + 4 * oc.NPTS
+        headers = [raw[k:k + 632].hex() for k in range(0, len(raw), rec)]
+        data = np.stack([np.frombuffer(raw[k + 632:k + rec], "<f4") for k in range(0, len(raw), rec)])
+        out["rotate"] = {
+            "pairs": len(rres),
+            "index": oc.normalize((rdir / "sourcepack_index.tsv").read_text(), root),
+            "success": oc.normalize((rdir / "_SUCCESS").read_text(), root),
+            "headers": headers,
+        }
+        # the rotation matrices of a few geometries, for the CPU pin
+        out["matrices"] = {f"{az}_{baz}": rotate.build_rotate_matrix(az, baz).tolist()
+                           for az, baz in ((0.0, 180.0), (37.5, 219.25), (90.0, 270.0), (301.1, 120.7))}
+        out["rudoe"] = [list(rotate.distkm_az_baz_rudoe(*g)) for g in
+                        ((101.0, 31.0, 101.9, 31.4), (100.6, 30.2, 101.0, 31.0), (0.0, 0.0, 10.0, 0.0),
+                         (-70.5, -33.4, 151.2, -33.9), (10.0, 90.0, 20.0, 45.0))]
+        np.savez_compressed(HERE / "operators_rtz.npz", data=data)
+    (HERE / "operators_golden.json").write_text(json.dumps(out, indent=1))
+    print("operator goldens written to", HERE)
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "operators":
+        operators_golden()
+        raise SystemExit(0)
     main()
+    operators_golden()
