@@ -59,6 +59,8 @@ static std::string clean_field(const std::string& s) {
   return o;
 }
 
+std::string tsv_clean(const std::string& s) { return clean_field(s); }
+
 void Progress::init(const char* p, const char* task_name, size_t tot, const char* unit_name) {
   path = (p && strcmp(p, "NONE") != 0) ? p : "";
   task = task_name;

@@ -163,5 +163,7 @@ SacHeader ncf_header(const Task& t, const Channel& src, const Channel& rec, floa
                      float cc_len, const TimeInfo* ti, bool have_time);
 
 int mkdir_p(const std::string& path);
+// TSV field text: tabs, CR and LF become spaces (the xcpack and progress TSVs)
+std::string tsv_clean(const std::string& s);
 
 }  // namespace fxcio

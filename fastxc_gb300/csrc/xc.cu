@@ -529,6 +529,30 @@ __global__ void __launch_bounds__(256) k_xc_stack_add(float4* __restrict__ dst, 
   }
 }
 
+// dst[dst_rows[r]][c] (+)= src[src_rows[r]][c] for c < ncols float2 columns:
+// folds one day's stack rows into the cross-day stack rows of their
+// (path, component) groups
+__global__ void __launch_bounds__(256)
+    k_xc_rows_accumulate(const float2* __restrict__ src, int64_t src_pitch, const int64_t* __restrict__ src_rows,
+                         const int64_t* __restrict__ dst_rows, int64_t nrows, float2* __restrict__ dst,
+                         int64_t dst_pitch, int ncols, int assign) {
+  for (int64_t r = blockIdx.y; r < nrows; r += gridDim.y) {
+    const float2* s = src + src_rows[r] * src_pitch;
+    float2* d = dst + dst_rows[r] * dst_pitch;
+    for (int c = blockIdx.x * 256 + threadIdx.x; c < ncols; c += gridDim.x * 256) {
+      const float2 a = __ldcs(s + c);
+      if (assign) {
+        d[c] = a;
+      } else {
+        float2 b = d[c];
+        b.x += a.x;
+        b.y += a.y;
+        d[c] = b;
+      }
+    }
+  }
+}
+
 int xc_stack_add_launch(fxc_ctx* ctx, float2* dst, const float2* src, int64_t n) {
   if (n <= 0) return FXC_OK;
   FXC_CHECK_ARG(n % 2 == 0, "stack add length %lld is odd", (long long)n);
@@ -668,6 +692,43 @@ int fxc_xc_run(fxc_ctx* ctx, const fxc_pairplan* plan, const float* d_spec, int6
   FXC_TRY(fxc_xc_stack(ctx, plan, d_spec, nwin, nchan, shape->nspec, spec_pitch, d_mask, scale,
                        stack, pitch, method));
   return fxc_xc_finalize(ctx, stack, plan->npairs, pitch, shape, d_ncf);
+}
+
+int fxc_xc_rows_accumulate(fxc_ctx* ctx, const float* d_src, int64_t src_rows, int64_t src_pitch,
+                           const int64_t* h_src_idx, const int64_t* h_dst_idx, int64_t nrows, float* d_dst,
+                           int64_t dst_rows, int64_t dst_pitch, int32_t ncols, int32_t assign) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(nrows >= 0 && ncols >= 0 && src_pitch >= ncols && dst_pitch >= ncols, "invalid shape");
+  if (nrows == 0 || ncols == 0) return FXC_OK;
+  FXC_CHECK_ARG(d_src && h_src_idx && h_dst_idx && d_dst, "null pointer");
+  // both index lists address their buffers; destination rows are distinct
+  // within one call (the kernel adds without atomics)
+  std::vector<int64_t> sorted(h_dst_idx, h_dst_idx + nrows);
+  std::sort(sorted.begin(), sorted.end());
+  FXC_CHECK_ARG(sorted.front() >= 0 && sorted.back() < dst_rows, "destination row outside [0, %lld)",
+                (long long)dst_rows);
+  FXC_CHECK_ARG(std::adjacent_find(sorted.begin(), sorted.end()) == sorted.end(),
+                "destination rows repeat within one call");
+  for (int64_t r = 0; r < nrows; ++r)
+    FXC_CHECK_ARG(h_src_idx[r] >= 0 && h_src_idx[r] < src_rows, "source row %lld outside [0, %lld)",
+                  (long long)h_src_idx[r], (long long)src_rows);
+  const size_t bytes = sizeof(int64_t) * (size_t)nrows;
+  const size_t off = (bytes + 255) & ~size_t(255);
+  FXC_TRY(ctx->scratch2.reserve(off + bytes));
+  int64_t* d_si = reinterpret_cast<int64_t*>(ctx->scratch2.ptr);
+  int64_t* d_di = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(ctx->scratch2.ptr) + off);
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_si, h_src_idx, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_di, h_dst_idx, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  const dim3 g((unsigned)std::min<int64_t>((ncols + 255) / 256, 64), (unsigned)std::min<int64_t>(nrows, 65535));
+  k_xc_rows_accumulate<<<g, 256, 0, ctx->stream>>>(reinterpret_cast<const float2*>(d_src), src_pitch, d_si, d_di,
+                                                   nrows, reinterpret_cast<float2*>(d_dst), dst_pitch, ncols,
+                                                   assign != 0);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  // the index staging is reused by the next call on this context
+  FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return FXC_OK;
 }
 
 int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec, int64_t nwin,

@@ -258,6 +258,20 @@ int fxc_rotate_matrix(double azimuth_deg, double back_azimuth_deg, float *out81)
 int fxc_rotate_enz_rtz(fxc_ctx *ctx, const float *d_enz, int64_t npairs, int32_t npts, int64_t pitch,
                        const float *d_mats, float *d_rtz);
 
+/* Cross-day fold of complex stack rows (no counterpart in the reference,
+ * whose linear stack averages finished per-day NCF files):
+ * d_dst[h_dst_idx[r]][c] += d_src[h_src_idx[r]][c] (or = with assign != 0,
+ * for rows that start a group) for r < nrows and c < ncols complex columns;
+ * pitches in complex elements; destination rows distinct within a call and
+ * < dst_rows, source rows < src_rows. One call per timestamp builds the sum
+ * over timestamps of per-timestamp stacks, from which one finalize gives
+ * the mean of the per-timestamp NCFs that _linear_stack_group
+ * (fastxc/operators/stacking/linear_stack.py:228-247) computes, because the
+ * finalize is linear. Synchronises the context stream. */
+int fxc_xc_rows_accumulate(fxc_ctx *ctx, const float *d_src, int64_t src_rows, int64_t src_pitch,
+                           const int64_t *h_src_idx, const int64_t *h_dst_idx, int64_t nrows, float *d_dst,
+                           int64_t dst_rows, int64_t dst_pitch, int32_t ncols, int32_t assign);
+
 /* ---- stacking: linear stack, PWS, TF-PWS -------------------------------- */
 
 /* Cross-timestamp linear stack (_linear_stack_group,
