@@ -322,8 +322,75 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> di
                         "workload": f"{tp} pairs x {ntr} traces -> {ng} groups of 10, {n} lags, 0.05-5 Hz band"}
         del t, lin, d_g, d_w, d_l, o
         torch.cuda.empty_cache()
+        out["batching"] = batching_run(torch, dev, ctx, stream)
     finally:
         ctx.close()
+    return out
+
+
+def batching_run(torch, dev, ctx, stream) -> dict:
+    """One day of the batching configuration: 500 stations x 3 components at
+    seeded positions in a 400 x 400 km square, component pairs of the station
+    pairs within 150 km, 24 one-hour windows, each station covering a
+    contiguous run of U(10%, 100%) of the day's windows at a random offset
+    (the rest masked). The pairs run in blocks of 65 536 (stack + NCFs of one
+    block resident); the method is autotuned on the first block."""
+    from fastxc_gb300._lib import FXC_XC_TENSOR
+    from fastxc_gb300.core import Context, PairPlan, xc_shape
+
+    rng = np.random.default_rng(4)
+    nsta, nstep, nspec, blk = 500, 24, 18523, 65536
+    nchan = 3 * nsta
+    pos = rng.uniform(0.0, 400.0, (nsta, 2))
+    dist = np.hypot(pos[:, None, 0] - pos[None, :, 0], pos[:, None, 1] - pos[None, :, 1])
+    si, sj = np.nonzero(np.triu(dist <= 150.0, 1))
+    a, b = np.meshgrid(np.arange(3), np.arange(3), indexing="ij")
+    src = (3 * si[:, None] + a.reshape(1, -1)).reshape(-1).astype(np.int32)
+    rec = (3 * sj[:, None] + b.reshape(1, -1)).reshape(-1).astype(np.int32)
+    npairs = src.size
+    cover = rng.uniform(0.1, 1.0, nsta)
+    mask = np.zeros((nstep, nchan), np.uint8)
+    for k in range(nsta):
+        n = max(1, int(round(cover[k] * nstep)))
+        o = int(rng.integers(0, nstep - n + 1))
+        mask[o:o + n, 3 * k:3 * k + 3] = 1
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    spec = torch.randn((nstep, nchan, nspec), generator=g, device=dev, dtype=torch.complex64)
+    d_mask = torch.from_numpy(mask).to(dev)
+    shape = xc_shape(nspec, nstep, 0.1, 100.0)
+    pitch = (nspec + 3) // 4 * 4
+    plans = [PairPlan(ctx, src[i:i + blk], rec[i:i + blk], nchan) for i in range(0, npairs, blk)]
+    method, ms_plain, ms_tensor = ctx.xc_autotune(plans[0], spec, nstep, nchan, nspec, nspec)
+    packed = None
+    if method == FXC_XC_TENSOR:
+        packed = torch.empty((Context.xc_packed_bytes(nchan, nstep, nspec) // 16, 4), dtype=torch.int32, device=dev)
+    d_stack = torch.empty((min(blk, npairs), pitch), dtype=torch.complex64, device=dev)
+    d_ncf = torch.empty((min(blk, npairs), shape.cc_size), dtype=torch.float32, device=dev)
+    scale = 1.0 / nstep
+
+    def day():
+        if packed is not None:
+            ctx.xc_pack(spec, nstep, nchan, nspec, nspec, d_mask, packed)
+        for i, pl in enumerate(plans):
+            n = min(blk, npairs - i * blk)
+            if packed is not None:
+                ctx.xc_stack_packed(pl, packed, nstep, nspec, scale, d_stack, pitch)
+            else:
+                ctx.xc_stack(pl, spec, nstep, nchan, nspec, nspec, d_mask, scale, d_stack, pitch, method)
+            ctx.xc_finalize(d_stack, n, pitch, shape, d_ncf)
+
+    ms = _timed(torch, stream, day, reps=2, warm=1)
+    covered = int(sum(int(np.minimum(mask[:, s], mask[:, r]).sum()) for s, r in zip(src[::9] , rec[::9]))) * 9
+    out = {"pair_windows_per_s": npairs * nstep / (ms / 1e3), "ms_per_day": ms, "pairs": int(npairs),
+           "station_pairs": int(si.size), "channels": nchan, "windows": nstep, "nspec": nspec,
+           "method": "tensor" if method == FXC_XC_TENSOR else "plain",
+           "autotune_sample_ms": {"plain": ms_plain, "tensor": ms_tensor},
+           "covered_pair_windows": covered,
+           "workload": "500 sta x 3 comp, pairs within 150 km of a 400 km square, 24 windows of 3600 s, "
+                       "coverage U(10%,100%) per station-day, blocks of 65536 pairs (stack + finalize)"}
+    del spec, d_mask, packed, d_stack, d_ncf, plans
+    torch.cuda.empty_cache()
     return out
 
 
