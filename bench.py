@@ -323,9 +323,40 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> di
         del t, lin, d_g, d_w, d_l, o
         torch.cuda.empty_cache()
         out["batching"] = batching_run(torch, dev, ctx, stream)
+        out["plain_small"] = small_run(torch, dev, ctx)
     finally:
         ctx.close()
     return out
+
+
+def small_run(torch, dev, ctx) -> dict:
+    """The small plain configuration end to end through the host-buffer
+    call (pinned spectra in, NCFs out): 4 stations x 3 components, one day
+    of 24 windows, nspec 18523, the 6 station pairs x 9 components."""
+    from fastxc_gb300.core import PairPlan, xc_shape
+    from fastxc_gb300.synthetic import cross_station_pairs
+
+    nsta, nstep, nspec = 4, 24, 18523
+    nchan = 3 * nsta
+    src, rec = cross_station_pairs(nsta)
+    rng = np.random.default_rng(1)
+    h = torch.empty((nstep, nchan, nspec), dtype=torch.complex64, pin_memory=True)
+    h.copy_(torch.from_numpy((rng.standard_normal((nstep, nchan, nspec)) +
+                              1j * rng.standard_normal((nstep, nchan, nspec))).astype(np.complex64)))
+    shape = xc_shape(nspec, nstep, 0.1, 100.0)
+    plan = PairPlan(ctx, src, rec, nchan)
+    o = torch.empty((src.size, shape.cc_size), dtype=torch.float32, pin_memory=True)
+    hs, ho = h.numpy(), o.numpy()
+    times = []
+    for i in range(6):
+        t0 = time.perf_counter()
+        ctx.xc_run_host(plan, hs, nstep, nchan, nspec, None, 1.0 / nstep, shape, ho, 0)
+        if i > 0:
+            times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.median(times)
+    return {"ms": ms, "pair_windows": int(src.size * nstep), "pair_windows_per_s": src.size * nstep / (ms / 1e3),
+            "method": "plain", "workload": f"{nsta} sta x 3 comp, 1 day = {nstep} windows, nspec {nspec}, "
+                                          f"{src.size} pairs, host buffers in and out (median of 5)"}
 
 
 def batching_run(torch, dev, ctx, stream) -> dict:

@@ -750,10 +750,12 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   //           (it accumulates in its coalesced transpose), in groups of up
   //           to four chunks for the tiled one (a partial stack that a
   //           coalesced add folds in). The last chunk is a group of its own,
-  //           so what follows the last copy is one chunk's contraction, the
-  //           finalize and the last NCF block's copy back.
+  //           so what follows the last copy is one chunk's contraction (the
+  //           plain kernel's when it has at most 16 windows), the finalize
+  //           and the last NCF block's copy back.
   const int nspec = shape->nspec;
   const int64_t wchunk = 64;  // windows per chunk (two 32-window K-blocks)
+  const int64_t kShortTailWindows = 16;
   const int kRing = 3;
   const int64_t nchunks = (nwin + wchunk - 1) / wchunk;
   const bool tensor = method == FXC_XC_TENSOR;
@@ -833,7 +835,14 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
     cuda_ok(cudaStreamWaitEvent(ctx->stream, landed[r], 0));
     if (rc != FXC_OK) break;
     const float2* spec = reinterpret_cast<const float2*>(slot);
-    if (tensor) {
+    // a short last chunk (the remainder of nwin / 64) costs the contraction
+    // mostly its fixed per-bin work; the plain kernel stacks it for less
+    const bool short_tail = tensor && c > 0 && c == nchunks - 1 && nw <= kShortTailWindows;
+    if (short_tail) {
+      rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,
+                           scale, stack, pitch, FXC_XC_PLAIN, 1);
+      cuda_ok(cudaEventRecord(used[r], ctx->stream));
+    } else if (tensor) {
       // pack into the group's operand layout; the slot is free again once
       // packed (the GEMM reads the packed copy)
       const int64_t g0 = group_first[(size_t)c];
