@@ -157,25 +157,74 @@ __global__ void __launch_bounds__(kStT)
   fft_twiddles_to_smem<kStT>(a.p, stw);
   for (int t = threadIdx.x; t < n; t += kStT) acc[t] = make_float2(0.f, 0.f);
   const float invn = 1.0f / (float)n;
-  for (int g = 0; g < ng; ++g) {
-    const float* x = groups + (goff + g) * n;
-    const float wg = weights[goff + g];
-    __syncthreads();
-    for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
-    __syncthreads();
-    any_forward<kStT>(buf, a, stw);  // R2C into an N-point row (odd N: full spectrum)
-    analytic_mask(buf, a);
-    __syncthreads();
-    any_inverse<kStT>(buf, a, stw);  // C2C inverse, unnormalised, natural order
-    for (int t = threadIdx.x; t < n; t += kStT) {
-      // cudaNormalizeComplex: z / nfft, modulus floored at 1e-7
-      const float2 z = buf[t];
-      const float re = z.x * invn, im = z.y * invn;
-      float mod = sqrtf(re * re + im * im);
-      mod = (mod > 1e-7f) ? mod : 1e-7f;
-      // cudaWeightedMeanBatch
-      acc[t].x += (re / mod) * wg;
-      acc[t].y += (im / mod) * wg;
+  __shared__ float2 dc;
+  if (n & 1) {
+    // Odd N (every NCF: N = 2 half_cc + 1). The masked inverse z/N of the
+    // reference is x - mean(x) + i H(x): its real part needs no transform,
+    // and the Hilbert transform H is real-to-real, so two groups share one
+    // forward transform of x1 + i x2 and one inverse of -i sign(k) Z(k),
+    // which returns N (H(x1) + i H(x2)). One transform per group instead of
+    // two; the group rows are read again (from L2) for the real parts.
+    const int half = (n + 1) / 2;
+    for (int g = 0; g < ng; g += 2) {
+      const bool two = g + 1 < ng;
+      const float* x1 = groups + (goff + g) * n;
+      const float* x2 = two ? x1 + n : x1;
+      const float w1 = weights[goff + g];
+      const float w2 = two ? weights[goff + g + 1] : 0.f;
+      __syncthreads();
+      for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x1[t], two ? x2[t] : 0.f);
+      __syncthreads();
+      any_forward<kStT>(buf, a, stw);
+      for (int k = threadIdx.x; k < n; k += kStT) {
+        const int pos = any_pos(a, k);
+        const float2 z = buf[pos];
+        if (k == 0) dc = z;  // (sum x1, sum x2)
+        // -i z for 0 < k < N/2, +i z above, 0 at DC
+        buf[pos] = k == 0 ? make_float2(0.f, 0.f) : (k < half ? mul_mi(z) : mul_pi(z));
+      }
+      __syncthreads();
+      any_inverse<kStT>(buf, a, stw);
+      const float m1 = dc.x * invn, m2 = dc.y * invn;
+      for (int t = threadIdx.x; t < n; t += kStT) {
+        const float2 h = buf[t];
+        // cudaNormalizeComplex (modulus floored at 1e-7) + cudaWeightedMeanBatch
+        float re = x1[t] - m1, im = h.x * invn;
+        float mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+        float2 ac = acc[t];
+        ac.x += (re / mod) * w1;
+        ac.y += (im / mod) * w1;
+        if (two) {
+          re = x2[t] - m2;
+          im = h.y * invn;
+          mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+          ac.x += (re / mod) * w2;
+          ac.y += (im / mod) * w2;
+        }
+        acc[t] = ac;
+      }
+    }
+  } else {
+    for (int g = 0; g < ng; ++g) {
+      const float* x = groups + (goff + g) * n;
+      const float wg = weights[goff + g];
+      __syncthreads();
+      for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
+      __syncthreads();
+      any_forward<kStT>(buf, a, stw);  // R2C into an N-point row (full spectrum)
+      analytic_mask(buf, a);
+      __syncthreads();
+      any_inverse<kStT>(buf, a, stw);  // C2C inverse, unnormalised, natural order
+      for (int t = threadIdx.x; t < n; t += kStT) {
+        // cudaNormalizeComplex: z / nfft, modulus floored at 1e-7
+        const float2 z = buf[t];
+        const float re = z.x * invn, im = z.y * invn;
+        float mod = sqrtf(re * re + im * im);
+        mod = (mod > 1e-7f) ? mod : 1e-7f;
+        // cudaWeightedMeanBatch
+        acc[t].x += (re / mod) * wg;
+        acc[t].y += (im / mod) * wg;
+      }
     }
   }
   __syncthreads();

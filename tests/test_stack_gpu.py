@@ -91,6 +91,23 @@ def test_tfpws_matches_oracle(ctx, torch_cuda, band, power):
     assert err.max() < 1e-5
 
 
+@pytest.mark.parametrize("n,ngroups", [(2000, 7), (2001, 1), (2001, 2)])
+def test_pws_group_parity_and_even_length(ctx, torch_cuda, n, ngroups):
+    """Odd N pairs the groups two per transform (one group left alone when
+    their count is odd, a single group on its own); even N keeps one
+    transform pair per group."""
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    tr = ncf_traces(3, ngroups, n, seed=9)
+    g, w, lin, goff, gcnt = _prestacked(ctx, torch, tr, 1, stack.MODE_PWS)
+    out = torch.empty((3, n), dtype=torch.float32, device="cuda")
+    stack.pws(ctx, g, w, goff, gcnt, lin, n, out, 1.0)
+    got = out.cpu().numpy()
+    ref = np.stack([sto.pws(tr[p], 1, 1.0) for p in range(3)])
+    assert rel(got, ref).max() < 1e-5
+
+
 @pytest.mark.parametrize("n", [4001, 1009, 3937])
 def test_pws_prime_lengths_bluestein(ctx, torch_cuda, n):
     """NCF lengths with a prime factor above 31 (4001 = lag 200 s at 10 Hz,
