@@ -20,7 +20,8 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 12, 16, 60, 64, 1001, 2001, 4096, 18000, 18144, 18522, 19200])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 12, 16, 60, 64, 124, 323, 646, 1001, 2001, 4096, 18000, 18144,
+                               18522, 19200])
 @pytest.mark.parametrize("inverse", [False, True])
 def test_c2c(ctx, torch_cuda, n, inverse):
     torch = torch_cuda
