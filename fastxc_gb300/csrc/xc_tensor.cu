@@ -184,16 +184,12 @@ constexpr int kPackF = 16;
 constexpr int kPackC = 16;
 constexpr size_t kPackSmem = sizeof(float2) * kTcKb * kPackC * (kPackF + 1);
 
-__device__ __forceinline__ uint16_t bf16_bits_rn(float x) {
-  // round-to-nearest-even float -> bf16 (inputs are finite: the spectra are
-  // sanitised by the producing stage)
-  uint32_t u = __float_as_uint(x);
-  u += 0x7fffu + ((u >> 16) & 1u);
-  return (uint16_t)(u >> 16);
-}
-
-__device__ __forceinline__ float bf16_bits_to_float(uint16_t b) {
-  return __uint_as_float((uint32_t)b << 16);
+// Two floats -> packed bf16x2 (lo in bits 0-15), rounded to nearest even
+// (the spectra are finite: the producing stage sanitises them).
+__device__ __forceinline__ uint32_t bf16x2_rn(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
 }
 
 __global__ void __launch_bounds__(256)
@@ -232,23 +228,16 @@ __global__ void __launch_bounds__(256)
     uint32_t w_rh[4], w_rl[4], w_ih[4], w_il[4];
 #pragma unroll
     for (int e2 = 0; e2 < 4; ++e2) {
-      uint32_t rh = 0, rl = 0, ih = 0, il = 0;
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const float2 v = psm[((kc * 8 + e2 * 2 + h) * kPackC + row) * (kPackF + 1) + f];
-        const uint16_t a = bf16_bits_rn(v.x);
-        const uint16_t b = bf16_bits_rn(v.x - bf16_bits_to_float(a));
-        const uint16_t c = bf16_bits_rn(v.y);
-        const uint16_t d = bf16_bits_rn(v.y - bf16_bits_to_float(c));
-        rh |= (uint32_t)a << (16 * h);
-        rl |= (uint32_t)b << (16 * h);
-        ih |= (uint32_t)c << (16 * h);
-        il |= (uint32_t)d << (16 * h);
-      }
+      // windows 2 e2 (low half) and 2 e2 + 1 (high half): hi = bf16(x),
+      // lo = bf16(x - hi)
+      const float2 v0 = psm[((kc * 8 + e2 * 2) * kPackC + row) * (kPackF + 1) + f];
+      const float2 v1 = psm[((kc * 8 + e2 * 2 + 1) * kPackC + row) * (kPackF + 1) + f];
+      const uint32_t rh = bf16x2_rn(v0.x, v1.x);
+      const uint32_t ih = bf16x2_rn(v0.y, v1.y);
       w_rh[e2] = rh;
-      w_rl[e2] = rl;
       w_ih[e2] = ih;
-      w_il[e2] = il;
+      w_rl[e2] = bf16x2_rn(v0.x - __uint_as_float(rh << 16), v1.x - __uint_as_float(rh & 0xffff0000u));
+      w_il[e2] = bf16x2_rn(v0.y - __uint_as_float(ih << 16), v1.y - __uint_as_float(ih & 0xffff0000u));
     }
     const int64_t fo = f0 + f;
     // chunk index of (f, plane, kb, kc) -> rows [0, cpad)

@@ -148,6 +148,41 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
 
 
+def _bf16_rne(x):
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def test_pack_bits_match_numpy_restatement(ctx, torch_cuda):
+    """The bf16 hi/lo planes of fxc_xc_pack, bit for bit: per bin, plane
+    (Re-hi, Re-lo, Im-hi, Im-lo), 32-window block, 8-window chunk, channel
+    row padded to 8, 8 windows; hi = RNE bf16(x), lo = RNE bf16(x - hi);
+    masked, missing and padding entries are zero."""
+    torch = torch_cuda
+    from fastxc_gb300.core import Context
+
+    rng = np.random.default_rng(12)
+    nwin, nchan, nspec = 45, 13, 37
+    spec = make_spec(rng, nwin, nchan, nspec)
+    mask = (rng.random((nwin, nchan)) > 0.2).astype(np.uint8)
+    nb = Context.xc_packed_bytes(nchan, nwin, nspec)
+    d_packed = torch.zeros((nb // 16, 4), dtype=torch.int32, device="cuda")
+    ctx.xc_pack(torch.from_numpy(spec).cuda(), nwin, nchan, nspec, nspec, torch.from_numpy(mask).cuda(), d_packed)
+    ctx.synchronize()
+    nkb, cpad = (nwin + 31) // 32, (nchan + 7) // 8 * 8
+    got = d_packed.cpu().numpy().view(np.uint16).reshape(nspec, 4, nkb, 4, cpad, 8)
+    v = np.zeros((nkb * 32, cpad, nspec), np.complex64)
+    v[:nwin, :nchan] = np.where(mask[:, :, None] != 0, spec, np.complex64(0))  # +0.0 where masked
+    v = v.reshape(nkb, 4, 8, cpad, nspec).transpose(4, 0, 1, 3, 2)  # [f][kb][kc][row][e]
+    planes = []
+    for part in (v.real, v.imag):
+        hi = _bf16_rne(part)
+        lo = _bf16_rne(part - (hi.astype(np.uint32) << 16).view(np.float32))
+        planes += [hi, lo]
+    want = np.stack(planes, axis=1)  # [f][plane][kb][kc][row][e]
+    assert np.array_equal(got, want)
+
+
 def test_packed_resident_path_equals_tensor_stack(ctx, torch_cuda):
     """fxc_xc_pack + fxc_xc_stack_packed (spectra kept in packed form) gives
     bit-identical stacks to fxc_xc_stack(FXC_XC_TENSOR), for two pair plans
