@@ -563,9 +563,10 @@ def main():
         kern_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
         fin_ms = statistics.mean(e[2].elapsed_time(e[3]) for e in evs)
         ncf_snapshot = d_ncf[:16].float().cpu().numpy().copy()
+        gemm_ms = gemm_total / gemm_n if gemm_n else None
         results[name] = {"total_ms": total_ms, "ms_per_step": total_ms / args.steps, "pack_ms": pack_ms,
                          "stack_ms": kern_ms, "finalize_ms": fin_ms, "launches": launches, "ncf16": ncf_snapshot,
-                         "gemm_ms": gemm_total / gemm_n if gemm_n else None}
+                         "gemm_ms": gemm_ms}
 
     # parity sample: 16 pairs over all windows against the FP64 oracle
     from oracle import xc_oracle as xo
@@ -606,8 +607,8 @@ def main():
                 sum_n += (min(256, nchan - b0) + 15) // 16 * 16
         issued = float(nspec) * nkb * 24 * 2 * 128 * 16 * sum_n
         # the contraction kernel's own launches, timed with CUDA events on
-        # the context stream (the stack stage also holds the bin-major ->
-        # [pair][bin] transpose of the whole-bin kernel)
+        # the context stream around each launch (fxc_ctx_kernel_timing); the
+        # stack stage also holds the bin-major -> [pair][bin] transpose
         kms = hr["gemm_ms"] if hr.get("gemm_ms") else hr["stack_ms"]
         achieved = issued / (kms / 1e3) / 1e12
         peak = peaks.get("bf16_tflops_sustained", 1700.0)

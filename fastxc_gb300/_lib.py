@@ -87,6 +87,7 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_xc_pack": (_int, [_vp, _vp, _i64, _i32, _i32, _i64, _vp, _vp]),
     "fxc_xc_stack_packed": (_int, [_vp, _vp, _vp, _i64, _i32, _f32, _vp, _i64]),
     "fxc_xc_finalize": (_int, [_vp, _vp, _i64, _i64, C.POINTER(XcShape), _vp]),
+    "fxc_xc_stack_finalize_packed": (_int, [_vp, _vp, _vp, _i64, _i32, _f32, C.POINTER(XcShape), _vp]),
     "fxc_xc_run": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
     "fxc_xc_run_host": (_int, [_vp, _vp, _vp, _i64, _i32, _i64, _vp, _f32, C.POINTER(XcShape), _vp, _int]),
     "fxc_xc_rows_accumulate": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _i64, _i32, _i32]),

@@ -122,6 +122,10 @@ class Context:
         lib().fxc_xc_stack_packed(self.handle, plan.handle, _ptr(d_packed), nwin, nspec, float(scale),
                                   _ptr(d_stack), stack_pitch)
 
+    def xc_stack_finalize_packed(self, plan: "PairPlan", d_packed, nwin, nspec, scale, shape: XcShape, d_ncf):
+        lib().fxc_xc_stack_finalize_packed(self.handle, plan.handle, _ptr(d_packed), nwin, nspec, float(scale),
+                                           C.byref(shape), _ptr(d_ncf))
+
     def xc_finalize(self, d_stack, npairs, stack_pitch, shape: XcShape, d_ncf):
         lib().fxc_xc_finalize(self.handle, _ptr(d_stack), npairs, stack_pitch, C.byref(shape),
                               _ptr(d_ncf))

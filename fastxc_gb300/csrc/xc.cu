@@ -686,6 +686,17 @@ int fxc_xc_run(fxc_ctx* ctx, const fxc_pairplan* plan, const float* d_spec, int6
   FXC_TRY(ctx_enter(ctx));
   FXC_CHECK_ARG(plan != nullptr && shape != nullptr, "null plan or shape");
   if (plan->npairs == 0) return FXC_OK;
+  if (method == FXC_XC_TENSOR && plan->tensor) {
+    // pack, then contraction + finalize without a [pair][bin] stack
+    FXC_CHECK_ARG(nchan == plan->nchan && nwin >= 0 && spec_pitch >= shape->nspec && d_spec && d_ncf,
+                  "invalid arguments");
+    const int64_t chunks = xc_packed_chunks(nchan, nwin, shape->nspec);
+    if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
+    uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
+    FXC_TRY(xc_pack_launch(ctx, reinterpret_cast<const float2*>(d_spec), nwin, nchan, shape->nspec, spec_pitch,
+                           d_mask, packed));
+    return fxc_xc_stack_finalize_packed(ctx, plan, packed, nwin, shape->nspec, scale, shape, d_ncf);
+  }
   const int64_t pitch = xc_stack_pitch(shape->nspec);
   FXC_TRY(ctx->scratch.reserve(sizeof(float2) * (size_t)pitch * (size_t)plan->npairs));
   float* stack = reinterpret_cast<float*>(ctx->scratch.ptr);

@@ -68,5 +68,8 @@ bool xc_gemm_accumulate_is_cheap(const fxc_pairplan* plan);
 int xc_stack_add_launch(fxc_ctx* ctx, float2* dst, const float2* src, int64_t n);
 int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_t stack_pitch,
                        const fxc_xc_shape* s, float* ncf);
+// Contraction of packed operands + finalize, the stack in context scratch.
+int xc_gemm_finalize_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
+                            int nspec, float scale, const fxc_xc_shape* s, float* ncf);
 
 }  // namespace fxc

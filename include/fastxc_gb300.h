@@ -221,6 +221,12 @@ int fxc_xc_pack(fxc_ctx *ctx, const float *d_spec, int64_t nwin, int32_t nchan, 
                 int64_t spec_pitch, const uint8_t *d_mask, void *d_packed);
 int fxc_xc_stack_packed(fxc_ctx *ctx, const fxc_pairplan *plan, const void *d_packed, int64_t nwin,
                         int32_t nspec, float scale, float *d_stack, int64_t stack_pitch);
+/* fxc_xc_stack_packed + fxc_xc_finalize in one call, the stack in context
+ * scratch (accumulateStepXc2DKernel loop + finalize_xc_batch,
+ * native/xc/worker/async_workers.cu:66-83, executor.cu:6-55): d_ncf is
+ * [npairs][cc_size]. */
+int fxc_xc_stack_finalize_packed(fxc_ctx *ctx, const fxc_pairplan *plan, const void *d_packed, int64_t nwin,
+                                 int32_t nspec, float scale, const fxc_xc_shape *shape, float *d_ncf);
 
 /* ncf[p, j] = C2R(stack[p] * (-1)^f)[nfft/2 - half_cc + j] / (nfft * dt),
  * j < cc_size. d_ncf is [npairs][cc_size] float. Replaces

@@ -148,6 +148,42 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
 
 
+@pytest.mark.parametrize("env", [{}, {"FXC_GEMM_TILED": "1"}, {"FXC_FINALIZE": "pruned"}])
+def test_stack_finalize_packed_equals_stack_then_finalize(ctx, torch_cuda, env, monkeypatch):
+    """fxc_xc_stack_finalize_packed gives the same NCF bits as
+    fxc_xc_stack_packed + fxc_xc_finalize, for the whole-bin and the tiled
+    contraction and the output-pruned finalize, and so does fxc_xc_run."""
+    torch = torch_cuda
+    from fastxc_gb300.core import Context, PairPlan
+
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    rng = np.random.default_rng(14)
+    nwin, nsta, nspec = 40, 5, 1001
+    nchan = 3 * nsta
+    spec = make_spec(rng, nwin, nchan, nspec)
+    src, rec = station_pairs(nsta, auto=True)
+    plan = PairPlan(ctx, src, rec, nchan)
+    shape = ctx_shape(nspec, nwin, 0.1, 20.0)
+    d_spec = torch.from_numpy(spec).cuda()
+    nb = Context.xc_packed_bytes(nchan, nwin, nspec)
+    d_packed = torch.zeros((nb // 16, 4), dtype=torch.int32, device="cuda")
+    ctx.xc_pack(d_spec, nwin, nchan, nspec, nspec, None, d_packed)
+    pitch = (nspec + 3) // 4 * 4
+    d_stack = torch.zeros((src.size, pitch), dtype=torch.complex64, device="cuda")
+    a = torch.zeros((src.size, shape.cc_size), dtype=torch.float32, device="cuda")
+    b = torch.zeros_like(a)
+    c = torch.zeros_like(a)
+    ctx.xc_stack_packed(plan, d_packed, nwin, nspec, 0.25, d_stack, pitch)
+    ctx.xc_finalize(d_stack, src.size, pitch, shape, a)
+    ctx.xc_stack_finalize_packed(plan, d_packed, nwin, nspec, 0.25, shape, b)
+    ctx.xc_run(plan, d_spec, nwin, nchan, nspec, None, 0.25, shape, c, 1)
+    ctx.synchronize()
+    assert torch.equal(a, b) and torch.equal(a, c)
+    ref = xo.xc_run(spec, src, rec, 0.25, xo.finalize_shape(nspec, nwin, 0.1, 20.0))
+    assert per_row_rel_l2(b.cpu().numpy(), ref).max() < NCF_RTOL
+
+
 def _bf16_rne(x):
     u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
     return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
