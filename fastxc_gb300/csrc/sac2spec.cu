@@ -27,8 +27,10 @@
 //                   C2R, then either the output transform or the time row
 //   k_s2s_output    [RAM divide] zero-pad, R2C(output_nfft), x dt,
 //                   sanitize, optional phase-only
-// Boxcar smoothing keeps the reference's window and divisor; the running
-// sums are FP32 with Kahan compensation (FP64 is kept for the detrend sums).
+// Boxcar smoothing keeps the reference's window and divisor. The reference's
+// FP64 sums and products (demean, detrend, normalisations) run as FP32 with
+// Kahan-compensated sums and two-float constants (F2c below): GB300's FP64
+// pipe is a small fraction of its FP32 rate.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -79,6 +81,32 @@ __device__ __forceinline__ double block_sum_f64(double v, double* sred) {
   return t;
 }
 
+// GB300 runs FP64 at a small fraction of its FP32 rate, so per-sample work
+// stays in FP32. A double constant c becomes the unevaluated sum hi + lo of
+// two floats; x * c = fma(x, hi, x * lo) is within an ulp of the float of
+// the double product. Sums over a row are Kahan-compensated FP32 per thread
+// with only the 1024-way block reduction in double.
+struct F2c {
+  float hi, lo;
+};
+__device__ __forceinline__ F2c f2c(double c) {
+  F2c r;
+  r.hi = (float)c;
+  r.lo = (float)(c - (double)r.hi);
+  return r;
+}
+__device__ __forceinline__ float mul_f2c(float x, F2c c) { return fmaf(x, c.hi, x * c.lo); }
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 __device__ __forceinline__ bool finite2(float2 v) { return isfinite(v.x) && isfinite(v.y); }
 __device__ __forceinline__ float2 sanitize2(float2 v) {
   return finite2(v) ? v : make_float2(0.f, 0.f);
@@ -94,7 +122,7 @@ __device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, St
   const int c0 = threadIdx.x * per;
   if (c0 >= n) return;
   const int c1 = min(n, c0 + per);
-  const double inv = 1.0 / (double)win;
+  const F2c inv = f2c(1.0 / (double)win);
   const int half = win / 2;
   float s = 0.f, comp = 0.f;
   auto kadd = [&](float v) {
@@ -106,7 +134,7 @@ __device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, St
   int lo = max(0, c0 - half), hi = min(n - 1, c0 - half + win - 1);
   for (int j = lo; j <= hi; ++j) kadd(ABS ? fabsf(src[j]) : src[j]);
   for (int c = c0; c < c1; ++c) {
-    store(c, (float)((double)s * inv));
+    store(c, mul_f2c(s, inv));
     const int out = c - half;      // leaves the window
     const int in = c - half + win;  // enters the window
     if (out >= 0 && out < n) kadd(-(ABS ? fabsf(src[out]) : src[out]));
@@ -122,7 +150,9 @@ __device__ __forceinline__ float ram_divide(float x, const float* __restrict__ w
   float s = 0.f;
   for (int c = 0; c < num_ch; ++c) s += w[(row0 + c) * pitch + i];
   if (!isfinite(s) || s < kMinValF) s = kMinValF;
-  float y = ((double)s < kMinValD) ? 0.f : x / s;
+  // (double)s < MINVAL in double is s < (float)MINVAL for a float s (no
+  // float lies in [1e-30, (float)1e-30)), and never true after the clamp
+  float y = (s < kMinValF) ? 0.f : x / s;
   if (!isfinite(y)) y = 0.f;
   return fminf(fmaxf(y, -kMaxVal), kMaxVal);
 }
@@ -208,7 +238,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
   const int seg = d.seg;
   fft_twiddles_to_smem<kS2sT>(pf, stw);
   // load + NaN/Inf -> 0 (isnan2DKernel); samples past the series are zero
-  double s1 = 0.0;
+  Kahan s1;
   for (int i = threadIdx.x; i < 2 * Mf; i += kS2sT) {
     float v = 0.f;
     if (i < seg && start + i < series_len) {
@@ -216,20 +246,20 @@ __global__ void __launch_bounds__(kS2sT, 1)
       if (!isfinite(v)) v = 0.f;
     }
     xs[i] = v;
-    if (i < seg) s1 += (double)v;
+    if (i < seg) s1.add(v);
   }
-  // demean (rdc2DKernel): x -= sum/width in double
-  const double mean = block_sum_f64(s1, sred) / (double)seg;
-  double s2 = 0.0, si = 0.0;
+  // demean (rdc2DKernel): x -= sum/width
+  const F2c mean = f2c(block_sum_f64(s1.value(), sred) / (double)seg);
+  Kahan s2, si;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    const float v = (float)((double)xs[i] - mean);
+    const float v = (xs[i] - mean.hi) - mean.lo;
     xs[i] = v;
-    s2 += (double)v;
-    si += (double)v * (double)i;
+    s2.add(v);
+    si.add(v * (float)i);
   }
-  // detrend (rtr2DKernel): closed-form least squares in double
-  const double y2 = block_sum_f64(s2, sred);
-  const double y1 = block_sum_f64(si, sred);
+  // detrend (rtr2DKernel): closed-form least squares
+  const double y2 = block_sum_f64(s2.value(), sred);
+  const double y1 = block_sum_f64(si.value(), sred);
   const double a12 = 0.5 * seg * (seg - 1);
   const double a11 = a12 * (2 * seg - 1) / 3.0;
   const double a22 = seg;
@@ -237,15 +267,15 @@ __global__ void __launch_bounds__(kS2sT, 1)
   const double ca = (a22 * y1 - a12 * y2) / det;
   const double cb = (a11 * y2 - a12 * y1) / det;
   const int tap = d.taper;
-  const double pi = 3.14159265358979323846;
+  const float caf = (float)ca, cbf = (float)cb, itap = 1.0f / (float)tap;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    float v = (float)((double)xs[i] - (ca * i + cb));
-    // timetaper2DKernel (float factor computed in double)
+    const float v = xs[i] - fmaf(caf, (float)i, cbf);
+    // timetaper2DKernel: 0.5 (1 - cos(pi i / tap)) at both ends
     float fac = 1.0f;
     if (i < tap)
-      fac = (float)(0.5 * (1.0 - cos(pi * i / tap)));
+      fac = 0.5f * (1.0f - cospif((float)i * itap));
     else if (i >= seg - tap)
-      fac = (float)(0.5 * (1.0 - cos(pi * (seg - i) / tap)));
+      fac = 0.5f * (1.0f - cospif((float)(seg - i) * itap));
     xs[i] = v * fac;
   }
   __syncthreads();
@@ -259,10 +289,10 @@ __global__ void __launch_bounds__(kS2sT, 1)
   });
   __syncthreads();
   fft_dit<kS2sT>(sbuf, pf, stw, true);
-  const double inrm = inv_norm(2 * Mf, dt);
+  const F2c inrm = f2c(inv_norm(2 * Mf, dt));
   float* xo = xout + (int64_t)r * seg;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    float v = (float)((double)xs[i] * inrm);
+    float v = mul_f2c(xs[i], inrm);
     if (mode == 1) v = (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f);
     xs[i] = v;
     xo[i] = v;
@@ -302,10 +332,10 @@ __global__ void __launch_bounds__(kS2sT, 1)
   });
   __syncthreads();
   fft_dit<kS2sT>(sbuf, pf, stw, true);
-  const double inrm = inv_norm(2 * Mf, dt);
+  const F2c inrm = f2c(inv_norm(2 * Mf, dt));
   float* xo = xb + (int64_t)r * seg;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    const float v = (float)((double)xs[i] * inrm);
+    const float v = mul_f2c(xs[i], inrm);
     xs[i] = v;
     xo[i] = v;
   }
@@ -376,19 +406,13 @@ __global__ void __launch_bounds__(kS2sT, 1)
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ float spec_taper_factor(int col, int width, const S2sDev& d) {
-  // specTaper2DKernel, np = 1 (factor in double)
+  // specTaper2DKernel, np = 1: cosine ramps up over [i1, i2), down over
+  // [i3, i4)
   const int i1 = d.f_idx1, i2 = d.f_idx2, i3 = d.f_idx3;
   const int i4 = d.f_idx4 < width ? d.f_idx4 : width;
-  const double pi = 3.14159265358979323846;
   if (col < i1) return 0.f;
-  if (col >= i1 && col < i2) {
-    const double dom = pi / (double)(i2 - i1);
-    return (float)((1.0 - cos(dom * (col - i1))) / 2.0);
-  }
-  if (col >= i3 && col < i4) {
-    const double dom = pi / (double)(i4 - i3);
-    return (float)((1.0 + cos(dom * (col - i3))) / 2.0);
-  }
+  if (col >= i1 && col < i2) return 0.5f * (1.0f - cospif((float)(col - i1) / (float)(i2 - i1)));
+  if (col >= i3 && col < i4) return 0.5f * (1.0f + cospif((float)(col - i3) / (float)(i4 - i3)));
   if (col >= i4 && col < width) return 0.f;
   return 1.f;
 }
@@ -447,10 +471,12 @@ __global__ void __launch_bounds__(kS2sT, 1)
     for (int c = 0; c < d.num_ch; ++c) s += Ain[(row0 + c) * fpitch + k];
     if (!isfinite(s) || s < kMinValF) s = kMinValF;  // clampmin2DKernel
     float2 X = Xr[k];
-    if ((double)s < kMinValD) X = make_float2(0.f, 0.f);  // cdiv2DKernel
+    if (s < kMinValF) X = make_float2(0.f, 0.f);  // cdiv2DKernel's double compare, as in ram_divide
     else X = make_float2(X.x / s, X.y / s);
+    // (float)((double)x * f) of two floats is the correctly rounded float
+    // product: the double product is exact
     const float f = spec_taper_factor(k, fw, d);
-    X = make_float2((float)((double)X.x * f), (float)((double)X.y * f));
+    X = make_float2(X.x * f, X.y * f);
     return sanitize2(X);
   };
   for (int k = threadIdx.x; k < Ms; k += kS2sT) {
@@ -465,9 +491,9 @@ __global__ void __launch_bounds__(kS2sT, 1)
   __syncthreads();
   fft_dit<kS2sT>(sbuf, ps, stw, true);
   const int seg = d.seg;
-  const double inrm = inv_norm(seg, d.delta);
+  const F2c inrm = f2c(inv_norm(seg, d.delta));
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    float v = (float)((double)xs[i] * inrm);
+    float v = mul_f2c(xs[i], inrm);
     if (to_time && time_mode == 1) v = (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f);
     xs[i] = v;
   }
