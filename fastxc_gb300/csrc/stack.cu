@@ -47,6 +47,7 @@ constexpr int kStBluestein = 16384;  // longest Bluestein length (any other trac
 // samples (kLsT apart, coalesced) so kLsV independent FP64 chains and loads
 // are in flight per trace.
 constexpr int kLsT = 256, kLsV = 4;
+
 __global__ void __launch_bounds__(kLsT)
     k_linear_stack(const float* __restrict__ traces, const int64_t* __restrict__ offs,
                    const int32_t* __restrict__ counts, int n, float* __restrict__ out) {
@@ -322,6 +323,14 @@ __device__ __forceinline__ float gauss_factor(int c, int f, int n, double scale)
   return (float)exp(-2.0 * pi * pi * (double)cc * (double)cc * scale / ((double)f * (double)f));
 }
 
+// The factors of every (frequency, shift) once per call: they do not depend
+// on the pair, and FP64 exp per CTA would load GB300's slow FP64 pipe.
+__global__ void k_tfpws_gauss(float* __restrict__ gtab, int n, int nfreq) {
+  const int64_t total = (int64_t)nfreq * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+    gtab[i] = gauss_factor((int)(i % n), (int)(i / n), n, 0.1);
+}
+
 // One CTA per (frequency f, pair): voices of every group and of the linear
 // stack at f, the time-frequency weight, the weighted stack voice summed
 // over time -> bin f of the output spectrum (band blend applied).
@@ -329,7 +338,7 @@ __global__ void __launch_bounds__(kStT)
     k_tfpws_freq(const float2* __restrict__ Xg, const float2* __restrict__ Xl,
                  const float* __restrict__ weights, const int64_t* __restrict__ goffs,
                  const int32_t* __restrict__ gcounts, AnyPlan a, int f0, TfBand band, float power,
-                 float2* __restrict__ spec_out) {
+                 const float* __restrict__ gtab, float2* __restrict__ spec_out) {
   extern __shared__ float2 sm[];
   __shared__ float sred[kStT / 32];
   __shared__ float sredi[kStT / 32];
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(kStT)
   }
   fft_twiddles_to_smem<kStT>(a.p, stw);
   for (int c = threadIdx.x; c < n; c += kStT) {
-    gs[c] = gauss_factor(c, f, n, 0.1);
+    gs[c] = gtab[(int64_t)f * n + c];
     W[c] = make_float2(0.f, 0.f);
   }
   const int64_t goff = goffs[pair];
@@ -629,7 +638,9 @@ int fxc_tfpws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   const size_t o_xg = o_gcnt + al(n4);
   const size_t o_xl = o_xg + al(sizeof(float2) * (size_t)total_groups * n);
   const size_t o_sp = o_xl + al(sizeof(float2) * (size_t)npairs * n);
-  const size_t total = o_sp + al(sizeof(float2) * (size_t)npairs * n);
+  const int nfreq = n / 2 + 1;
+  const size_t o_gt = o_sp + al(sizeof(float2) * (size_t)npairs * n);
+  const size_t total = o_gt + al(sizeof(float) * (size_t)nfreq * n);
   FXC_TRY(ctx->scratch4.reserve(total));
   char* base = reinterpret_cast<char*>(ctx->scratch4.ptr);
   int64_t* d_goff = reinterpret_cast<int64_t*>(base);
@@ -637,6 +648,7 @@ int fxc_tfpws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   float2* Xg = reinterpret_cast<float2*>(base + o_xg);
   float2* Xl = reinterpret_cast<float2*>(base + o_xl);
   float2* spec = reinterpret_cast<float2*>(base + o_sp);
+  float* gtab = reinterpret_cast<float*>(base + o_gt);
   FXC_CUDA_TRY(cudaMemcpyAsync(d_goff, h_group_offsets, n8, cudaMemcpyHostToDevice, ctx->stream));
   FXC_CUDA_TRY(cudaMemcpyAsync(d_gcnt, h_group_counts, n4, cudaMemcpyHostToDevice, ctx->stream));
   const size_t sm1 = sizeof(float2) * ((size_t)any_buf_elems(a) + fft_tw_smem_elems(a.p));
@@ -653,14 +665,16 @@ int fxc_tfpws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   k_tfpws_init<<<1024, 256, 0, ctx->stream>>>(Xl, (int64_t)npairs * n, band_limited, spec);
   count_launch();
   FXC_LAUNCH_CHECK();
-  const int nfreq = n / 2 + 1;
+  k_tfpws_gauss<<<1024, 256, 0, ctx->stream>>>(gtab, n, nfreq);
+  count_launch();
+  FXC_LAUNCH_CHECK();
   const size_t sm2 = sizeof(float2) * ((size_t)any_buf_elems(a) + (size_t)n + fft_tw_smem_elems(a.p)) +
                      sizeof(float) * (size_t)((n + 1) & ~1);
   FXC_TRY(set_smem_limit(k_tfpws_freq, sm2));
   for (int f0 = 0; f0 < nfreq; f0 += 65535) {
     dim3 g((unsigned)std::min(65535, nfreq - f0), (unsigned)npairs);
     k_tfpws_freq<<<g, kStT, sm2, ctx->stream>>>(Xg, Xl, d_weights, d_goff, d_gcnt, a, f0, band, power,
-                                                spec);
+                                                gtab, spec);
     count_launch();
     FXC_LAUNCH_CHECK();
   }

@@ -58,8 +58,10 @@ def test_oracle_filter_design_matches_reference_python(name, delta, bands):
     assert len(ref) == len(got)
     for r, g in zip(ref, got):
         assert r.freq_low == pytest.approx(g.freq_low) and r.freq_high == pytest.approx(g.freq_high)
-        assert np.allclose(r.b, g.b, rtol=1e-15, atol=1e-18)
-        assert np.allclose(r.a, g.a, rtol=1e-15, atol=1e-18)
+        # scipy's butter on another platform (libm, BLAS) may differ in the
+        # last bits of the double coefficients
+        assert np.allclose(r.b, g.b, rtol=1e-12, atol=1e-18)
+        assert np.allclose(r.a, g.a, rtol=1e-12, atol=1e-18)
 
 
 @pytest.mark.parametrize("case", range(5))
