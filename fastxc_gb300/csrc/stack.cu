@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "context.cuh"
+#include "exact_sum.cuh"
 #include "fft.cuh"
 #include "fft_any.cuh"
 #include "fft_launch.cuh"
@@ -42,36 +43,16 @@ constexpr int kStBluestein = 16384;  // longest Bluestein length (any other trac
 // linear stack and prestack
 // ---------------------------------------------------------------------------
 
-// out[p, t] = float(sum_k double(tr[off_p + k, t]) / count_p), the sum in
-// trace order (as _linear_stack_group accumulates). Each thread owns kLsV
-// samples (kLsT apart, coalesced) so kLsV independent FP64 chains and loads
-// are in flight per trace.
-constexpr int kLsT = 256, kLsV = 4;
+// Cross-timestamp linear stack: exact int64 fixed-point column sums that
+// reproduce _linear_stack_group's FP64 accumulation bit for bit
+// (exact_sum.cuh). One sample column per thread, an 8-row register ring, one
+// window branch per 2 rows (the fastest of the shapes timed on GB300).
+constexpr int kLsT = 256, kLsV = 1;
 
 __global__ void __launch_bounds__(kLsT)
     k_linear_stack(const float* __restrict__ traces, const int64_t* __restrict__ offs,
                    const int32_t* __restrict__ counts, int n, float* __restrict__ out) {
-  const int p = blockIdx.y;
-  const int64_t off = offs[p];
-  const int cnt = counts[p];
-  const int t0 = blockIdx.x * (kLsT * kLsV) + threadIdx.x;
-  double acc[kLsV];
-#pragma unroll
-  for (int v = 0; v < kLsV; ++v) acc[v] = 0.0;
-  const float* base = traces + off * n;
-  for (int k = 0; k < cnt; ++k) {
-    const float* row = base + (int64_t)k * n;
-#pragma unroll
-    for (int v = 0; v < kLsV; ++v) {
-      const int t = t0 + v * kLsT;
-      if (t < n) acc[v] += (double)__ldg(row + t);
-    }
-  }
-#pragma unroll
-  for (int v = 0; v < kLsV; ++v) {
-    const int t = t0 + v * kLsT;
-    if (t < n) out[(int64_t)p * n + t] = cnt > 0 ? (float)(acc[v] / (double)cnt) : 0.f;
-  }
+  linear_stack_cta<kLsT, kLsV, 8, 2>(traces, offs, counts, n, out);
 }
 
 // Group rows of `substack` consecutive traces (B < 2 -> 1): mode 0 mean

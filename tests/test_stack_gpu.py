@@ -34,6 +34,53 @@ def test_linear_stack_matches_reference_golden(ctx, torch_cuda):
     assert np.array_equal(out.cpu().numpy()[0], d["stacked"])
 
 
+def _adversarial_traces(cnt, n, seed):
+    """Columns by t mod 10: noise; terms across 80 decades; one term 2^-30
+    of the rest; all -0; mixed signed zeros; subnormals; a NaN; +-inf;
+    exact cancellations; cnt-scaled large values."""
+    rng = np.random.default_rng(seed)
+    tr = (rng.standard_normal((cnt, n)) * 0.3).astype(np.float32)
+    kind = np.arange(n) % 10
+    wide = rng.standard_normal((cnt, n)) * 10.0 ** rng.integers(-40, 38, (cnt, n))
+    tr[:, kind == 1] = wide[:, kind == 1].astype(np.float32)
+    tr[cnt // 2, kind == 2] *= np.float32(2.0 ** -30)
+    tr[:, kind == 3] = -0.0
+    tr[:, kind == 4] = np.where(rng.random((cnt, (kind == 4).sum())) < 0.5, -0.0, 0.0)
+    sub = rng.integers(-5, 6, (cnt, (kind == 5).sum())) * 2.0 ** rng.integers(-149, -126, (cnt, (kind == 5).sum()))
+    tr[:, kind == 5] = sub.astype(np.float32)
+    tr[cnt - 1, kind == 6] = np.nan
+    tr[0, kind == 7] = np.inf
+    if cnt > 1:
+        tr[1, kind == 7] = -np.inf if cnt > 2 else np.inf
+    half = cnt // 2
+    tr[half:2 * half, kind == 8] = -tr[:half, kind == 8]
+    tr[:, kind == 9] = (rng.standard_normal((cnt, (kind == 9).sum())) * 3e37).astype(np.float32)
+    return tr
+
+
+@pytest.mark.parametrize("cnt", [1, 2, 7, 720])
+def test_linear_stack_bits_on_adversarial_columns(ctx, torch_cuda, cnt):
+    """The fixed-point sum gives the reference's FP64 sequence bit for bit,
+    and the columns it cannot prove exact take the FP64 loop."""
+    torch = torch_cuda
+    from fastxc_gb300 import stack
+
+    n = 1100  # two CTAs per pair, the second one partly past the trace end
+    trs = [_adversarial_traces(c, n, seed=c) for c in (cnt, 3)]
+    allt = np.concatenate(trs)
+    counts = [cnt, 3]
+    offs = [0, cnt]
+    out = torch.empty((2, n), dtype=torch.float32, device="cuda")
+    stack.linear_stack(ctx, torch.from_numpy(allt).cuda(), offs, counts, n, out)
+    ctx.synchronize()
+    got = out.cpu().numpy()
+    with np.errstate(all="ignore"):
+        ref = np.stack([sto.linear_stack(t) for t in trs])
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))
+
+
 def _prestacked(ctx, torch, tr, substack, mode):
     from fastxc_gb300 import stack
 
