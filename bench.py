@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stages", action="store_true", help="skip the sac2spec / stacking stage timings")
+    ap.add_argument("--stack-pairs", type=int, default=2304, help="pairs of the stacking stages; smaller values only for profiling runs")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -243,7 +244,7 @@ def _timed(torch, stream, fn, reps=3, warm=1):
     return e0.elapsed_time(e1) / reps
 
 
-def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> dict:
+def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack_pairs: int = 2304) -> dict:
     """The other stages of the path on their own configurations, timed with
     CUDA events on the launching stream (inputs resident, larger than L2):
       sac2spec: one day of 64 stations x 3 components at 10 Hz (192 rows x
@@ -281,7 +282,7 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> di
         del series, spec, resp
         torch.cuda.empty_cache()
         # --- linear stack + PWS (config 3) ----------------------------------
-        npairs, ntr, n = 2304, 720, 2001
+        npairs, ntr, n = stack_pairs, 720, 2001
         t = torch.randn((npairs * ntr, n), generator=g, device=dev, dtype=torch.float32)
         offs = np.arange(npairs, dtype=np.int64) * ntr
         cnts = np.full(npairs, ntr, np.int32)
@@ -290,7 +291,7 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> di
         nbytes = t.numel() * 4 + lin.numel() * 4
         out["linear_stack"] = {"traces_per_s": npairs * ntr / (ms / 1e3), "ms": ms, "bytes": nbytes,
                                "hbm_gbs": nbytes / (ms / 1e3) / 1e9, "hbm_frac": nbytes / (ms / 1e3) / 1e9 / hbm_gbs,
-                               "workload": f"{npairs} pairs x {ntr} traces x {n} lags (FP64 accumulation)"}
+                               "workload": f"{npairs} pairs x {ntr} traces x {n} lags (sums bit-identical to FP64 accumulation)"}
         res = {}
 
         def pws_once():
@@ -306,7 +307,7 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float) -> di
                       "workload": f"{npairs} pairs x {ntr} traces x {n} lags, substack 1 (prestack + PWS)"}
         res.clear()
         # --- TF-PWS (subset) ---------------------------------------------------
-        tp = 128
+        tp = min(128, npairs)
         d_g, d_w, d_l, goff, gcnt = stack.prestack(ctx, torch, t[: tp * ntr], offs[:tp], cnts[:tp], n, 10,
                                                    stack.MODE_TFPWS)
         o = torch.empty((tp, n), dtype=torch.float32, device=dev)
@@ -691,7 +692,8 @@ def main():
     torch.cuda.empty_cache()
     if not args.no_stages and world == 1:
         line["stages"] = stages_run(torch, dev, local, peaks.get("hbm_gbs", 6800.0),
-                                    152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12)
+                                    152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12,
+                                    args.stack_pairs)
     if args.serve_seconds > 0:
         # serving: a Poisson stream of correlation jobs against the engine
         line["serving"] = serving_run(args, local, rank)
