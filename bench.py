@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stages", action="store_true", help="skip the sac2spec / stacking stage timings")
     ap.add_argument("--stack-pairs", type=int, default=2304, help="pairs of the stacking stages; smaller values only for profiling runs")
+    ap.add_argument("--batch-block", type=int, default=0,
+                    help="pairs per block of the batching stage (0: all pairs of the day in one block)")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -244,7 +246,8 @@ def _timed(torch, stream, fn, reps=3, warm=1):
     return e0.elapsed_time(e1) / reps
 
 
-def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack_pairs: int = 2304) -> dict:
+def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack_pairs: int = 2304,
+               batch_block: int = 0) -> dict:
     """The other stages of the path on their own configurations, timed with
     CUDA events on the launching stream (inputs resident, larger than L2):
       sac2spec: one day of 64 stations x 3 components at 10 Hz (192 rows x
@@ -323,7 +326,7 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack
                         "workload": f"{tp} pairs x {ntr} traces -> {ng} groups of 10, {n} lags, 0.05-5 Hz band"}
         del t, lin, d_g, d_w, d_l, o
         torch.cuda.empty_cache()
-        out["batching"] = batching_run(torch, dev, ctx, stream)
+        out["batching"] = batching_run(torch, dev, ctx, stream, batch_block)
         out["plain_small"] = small_run(torch, dev, ctx)
     finally:
         ctx.close()
@@ -360,18 +363,19 @@ def small_run(torch, dev, ctx) -> dict:
                                           f"{src.size} pairs, host buffers in and out (median of 5)"}
 
 
-def batching_run(torch, dev, ctx, stream) -> dict:
+def batching_run(torch, dev, ctx, stream, block: int = 0) -> dict:
     """One day of the batching configuration: 500 stations x 3 components at
     seeded positions in a 400 x 400 km square, component pairs of the station
     pairs within 150 km, 24 one-hour windows, each station covering a
     contiguous run of U(10%, 100%) of the day's windows at a random offset
-    (the rest masked). The pairs run in blocks of 65 536 (stack + NCFs of one
-    block resident); the method is autotuned on the first block."""
+    (the rest masked). The pairs run in blocks of `block` pairs (0: all of
+    them, a 51 GB stack resident); the method is autotuned on the first
+    block."""
     from fastxc_gb300._lib import FXC_XC_TENSOR
     from fastxc_gb300.core import Context, PairPlan, xc_shape
 
     rng = np.random.default_rng(4)
-    nsta, nstep, nspec, blk = 500, 24, 18523, 65536
+    nsta, nstep, nspec = 500, 24, 18523
     nchan = 3 * nsta
     pos = rng.uniform(0.0, 400.0, (nsta, 2))
     dist = np.hypot(pos[:, None, 0] - pos[None, :, 0], pos[:, None, 1] - pos[None, :, 1])
@@ -380,6 +384,7 @@ def batching_run(torch, dev, ctx, stream) -> dict:
     src = (3 * si[:, None] + a.reshape(1, -1)).reshape(-1).astype(np.int32)
     rec = (3 * sj[:, None] + b.reshape(1, -1)).reshape(-1).astype(np.int32)
     npairs = src.size
+    blk = block if block > 0 else npairs
     cover = rng.uniform(0.1, 1.0, nsta)
     mask = np.zeros((nstep, nchan), np.uint8)
     for k in range(nsta):
@@ -413,14 +418,40 @@ def batching_run(torch, dev, ctx, stream) -> dict:
             ctx.xc_finalize(d_stack, n, pitch, shape, d_ncf)
 
     ms = _timed(torch, stream, day, reps=2, warm=1)
+    # where one day's time goes: the contraction kernels (CUDA events around
+    # each launch) and the whole stack / finalize calls
+    phase = {"pack": 0.0, "stack": 0.0, "finalize": 0.0}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(name, fn):
+        ev[0].record(stream)
+        fn()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        phase[name] += ev[0].elapsed_time(ev[1])
+
+    ctx.kernel_timing(True)
+    if packed is not None:
+        timed("pack", lambda: ctx.xc_pack(spec, nstep, nchan, nspec, nspec, d_mask, packed))
+    for i, pl in enumerate(plans):
+        n = min(blk, npairs - i * blk)
+        if packed is not None:
+            timed("stack", lambda: ctx.xc_stack_packed(pl, packed, nstep, nspec, scale, d_stack, pitch))
+        else:
+            timed("stack", lambda: ctx.xc_stack(pl, spec, nstep, nchan, nspec, nspec, d_mask, scale, d_stack,
+                                                pitch, method))
+        timed("finalize", lambda: ctx.xc_finalize(d_stack, n, pitch, shape, d_ncf))
+    gemm = {k: ctx.kernel_time(k)[0] for k in ("k_xc_tc_gemm", "k_xc_tc_gemm_bin")}
+    ctx.kernel_timing(False)
     covered = int(sum(int(np.minimum(mask[:, s], mask[:, r]).sum()) for s, r in zip(src[::9] , rec[::9]))) * 9
     out = {"pair_windows_per_s": npairs * nstep / (ms / 1e3), "ms_per_day": ms, "pairs": int(npairs),
            "station_pairs": int(si.size), "channels": nchan, "windows": nstep, "nspec": nspec,
            "method": "tensor" if method == FXC_XC_TENSOR else "plain",
            "autotune_sample_ms": {"plain": ms_plain, "tensor": ms_tensor},
            "covered_pair_windows": covered,
+           "phase_ms": {**phase, "contraction_kernels": sum(gemm.values())},
            "workload": "500 sta x 3 comp, pairs within 150 km of a 400 km square, 24 windows of 3600 s, "
-                       "coverage U(10%,100%) per station-day, blocks of 65536 pairs (stack + finalize)"}
+                       f"coverage U(10%,100%) per station-day, blocks of {blk} pairs (stack + finalize)"}
     del spec, d_mask, packed, d_stack, d_ncf, plans
     torch.cuda.empty_cache()
     return out
@@ -693,7 +724,7 @@ def main():
     if not args.no_stages and world == 1:
         line["stages"] = stages_run(torch, dev, local, peaks.get("hbm_gbs", 6800.0),
                                     152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12,
-                                    args.stack_pairs)
+                                    args.stack_pairs, args.batch_block)
     if args.serve_seconds > 0:
         # serving: a Poisson stream of correlation jobs against the engine
         line["serving"] = serving_run(args, local, rank)

@@ -56,6 +56,7 @@ constexpr int kTcABytes = kTcPlanes * kTcM * kTcKb * 2;     // 32 KB per stage
 constexpr int kTcBBytesMax = kTcPlanes * kTcNmax * kTcKb * 2;  // 64 KB per stage
 constexpr int kTcStageBytes = kTcABytes + kTcBBytesMax;
 constexpr size_t kTcSmemBytes = (size_t)kTcStages * kTcStageBytes + 256;
+constexpr int64_t kBinMajorCap = int64_t(2) << 30;  // bin-major scratch of one tiled pass (bytes)
 
 struct TcTile {
   int32_t a0, am;  // first src row, valid src rows (<= 128)
@@ -69,7 +70,8 @@ struct XcTensorPlan {
   int32_t cpad = 0;
   int64_t ntiles = 0;
   TcTile* d_tiles = nullptr;
-  int32_t* d_maps = nullptr;  // per tile [128][n]: p, -(p+2) for a reversed pair, -1 none
+  int32_t* d_maps = nullptr;  // per tile [128][n]: q, -(q+2) for a reversed pair, -1 none
+  int32_t* d_perm = nullptr;  // perm[q] = pair index p of bin-major slot q
   std::vector<TcTile> h_tiles;
 };
 
@@ -135,25 +137,51 @@ int xc_tensor_plan_init(fxc_ctx*, fxc_pairplan* plan) {
       }
     }
   }
+  // Bin-major slots: the pairs of tile 0 first, then tile 1, ...; within a
+  // tile column by column, rows in order. The contraction writes a tile's
+  // values into one contiguous run of a bin's row (the 32 rows of a warp at
+  // one column into consecutive slots), and the transpose puts slot q back
+  // at pair perm[q].
+  std::vector<int32_t> perm((size_t)plan->npairs, -1);
+  int64_t q = 0;
+  for (const TcTile& t : tiles)
+    for (int32_t c = 0; c < t.n; ++c)
+      for (int32_t r = 0; r < kTcM; ++r) {
+        int32_t& cell = maps[(size_t)t.map_offset + (size_t)r * t.n + c];
+        if (cell == -1) continue;
+        const int32_t pi = cell >= 0 ? cell : -cell - 2;
+        perm[(size_t)q] = pi;
+        cell = cell >= 0 ? (int32_t)q : (int32_t)(-(q + 2));
+        ++q;
+      }
+  if (q != plan->npairs) {
+    delete tp;
+    set_error("tensor tile plan places %lld of %lld pairs", (long long)q, (long long)plan->npairs);
+    return FXC_ERR_INVALID;
+  }
   tp->ntiles = (int64_t)tiles.size();
   tp->h_tiles = tiles;
   if (!tiles.empty()) {
     cudaError_t e1 = cudaMalloc(&tp->d_tiles, sizeof(TcTile) * tiles.size());
     cudaError_t e2 = cudaMalloc(&tp->d_maps, sizeof(int32_t) * maps.size());
-    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    cudaError_t e2b = cudaMalloc(&tp->d_perm, sizeof(int32_t) * perm.size());
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e2b != cudaSuccess) {
       (void)cudaGetLastError();
       if (tp->d_tiles) cudaFree(tp->d_tiles);
       if (tp->d_maps) cudaFree(tp->d_maps);
+      if (tp->d_perm) cudaFree(tp->d_perm);
       delete tp;
       set_error("cudaMalloc of tensor tile plan failed");
       return FXC_ERR_NOMEM;
     }
     cudaMemcpy(tp->d_tiles, tiles.data(), sizeof(TcTile) * tiles.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(tp->d_perm, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice);
     cudaError_t e3 =
         cudaMemcpy(tp->d_maps, maps.data(), sizeof(int32_t) * maps.size(), cudaMemcpyHostToDevice);
     if (e3 != cudaSuccess) {
       cudaFree(tp->d_tiles);
       cudaFree(tp->d_maps);
+      cudaFree(tp->d_perm);
       delete tp;
       set_error("upload of tensor tile plan failed: %s", cudaGetErrorString(e3));
       return FXC_ERR_CUDA;
@@ -167,6 +195,7 @@ void xc_tensor_plan_free(fxc_pairplan* plan) {
   if (!plan->tensor) return;
   if (plan->tensor->d_tiles) cudaFree(plan->tensor->d_tiles);
   if (plan->tensor->d_maps) cudaFree(plan->tensor->d_maps);
+  if (plan->tensor->d_perm) cudaFree(plan->tensor->d_perm);
   delete plan->tensor;
   plan->tensor = nullptr;
 }
@@ -294,36 +323,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   }
 }
 
-// Scatter 16 accumulator columns of one TMEM row to the stack: column j goes
-// to pair p = mv[j] (conjugated for -(p + 2), skipped for -1) at bin f. With
-// accumulate the 16 previous values are all loaded before any store -- the
-// pairs of a row are distinct, and issuing the loads together keeps one DRAM
-// round trip per call instead of one per pair.
-__device__ __forceinline__ void store_pairs16(float2* __restrict__ stack, int64_t stack_pitch, int64_t f,
-                                              const int32_t* mv, const float* re, const float* im, float scale,
-                                              int accumulate) {
-  int64_t off[16];
-  float2 o[16];
+// 16 accumulator columns of one TMEM row into a bin-major row: column j goes
+// to slot q = mv[j] (conjugated for -(q + 2), skipped for -1).
+__device__ __forceinline__ void store_slots16(float2* __restrict__ row, const int32_t* mv, const float* re,
+                                              const float* im, float scale) {
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     const int32_t v = mv[j];
+    if (v == -1) continue;
     const bool rev = v < -1;
-    off[j] = v == -1 ? -1 : (rev ? (int64_t)(-v - 2) : (int64_t)v) * stack_pitch + f;
-    o[j] = make_float2(re[j] * scale, (rev ? -im[j] : im[j]) * scale);
+    row[rev ? -v - 2 : v] = make_float2(re[j] * scale, (rev ? -im[j] : im[j]) * scale);
   }
-  if (accumulate) {
-    float2 prev[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) prev[j] = off[j] >= 0 ? __ldcg(stack + off[j]) : make_float2(0.f, 0.f);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      o[j].x += prev[j].x;
-      o[j].y += prev[j].y;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 16; ++j)
-    if (off[j] >= 0) stack[off[j]] = o[j];
 }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
@@ -385,11 +395,27 @@ __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Output: bin-major rows, binmajor[f * bin_pitch + q] for the plan's slots
+// q (each tile owns one contiguous run of slots, column-major, so the 32
+// rows of a warp store one column into consecutive slots).
+// Persistent: CTA c runs the (bin, tile) items c, c + G, c + 2G, ... of
+// total = nspec * ntiles, numbered bin-major, so the G CTAs at work at any
+// time hold consecutive items: the tiles of a few adjacent bins, whose
+// operand rows are shared in L2. TMEM, the
+// barriers and the operand ring live across items: the producer loads the
+// next item's K-blocks while the current item's epilogue runs, and the MMAs
+// of an item start once the epilogue of the previous one has drained the
+// accumulators (tmem_empty, one arrival per epilogue warp). Rows of a stage
+// past a tile's valid rows hold stale data; they only reach accumulator rows
+// (>= am) and columns (>= bn) that the epilogue never stores.
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_xc_tc_gemm(const uint4* __restrict__ packed, int nkb, int cpad,
-                 const TcTile* __restrict__ tiles, const int32_t* __restrict__ maps, int nspec,
-                 float scale, float2* __restrict__ stack, int64_t stack_pitch, int accumulate,
-                 int* __restrict__ err) {
+                 const TcTile* __restrict__ tiles, int ntiles, const int32_t* __restrict__ maps, int nspec,
+                 float scale, float2* __restrict__ binmajor, int64_t bin_pitch, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* stage_base = smem;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)kTcStages * kTcStageBytes);
@@ -397,38 +423,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t bar_full0 = smem_u32(bars + 0);
   const uint32_t bar_empty0 = smem_u32(bars + 2);
   const uint32_t bar_acc = smem_u32(bars + 4);
+  const uint32_t bar_tfree = smem_u32(bars + 5);
+  const uint32_t bar_drain = smem_u32(bars + 6);
 
-  const TcTile tile = tiles[blockIdx.x];
-  const int f = blockIdx.y;
+  const int64_t total = (int64_t)ntiles * nspec;
+  const int64_t G = gridDim.x;
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int n = tile.n;
-  const uint32_t b_plane_bytes = (uint32_t)n * kTcKb * 2;  // n rows x 64 B
   const uint32_t a_plane_bytes = (uint32_t)kTcM * kTcKb * 2;
 
-  // Zero the padding rows once (bulk copies never write them).
-  if (tile.am < kTcM || tile.bn < n) {
-    for (int s = 0; s < kTcStages; ++s) {
-      unsigned char* st = stage_base + (size_t)s * kTcStageBytes;
-      for (int pl = 0; pl < kTcPlanes; ++pl)
-        for (int kc = 0; kc < kTcKc; ++kc) {
-          uint4* a = reinterpret_cast<uint4*>(st + pl * a_plane_bytes + kc * kTcM * 16);
-          for (int r = tile.am + threadIdx.x; r < kTcM; r += kTcThreads) a[r] = make_uint4(0, 0, 0, 0);
-          uint4* b = reinterpret_cast<uint4*>(st + kTcABytes + pl * b_plane_bytes + kc * n * 16);
-          for (int r = tile.bn + threadIdx.x; r < n; r += kTcThreads) b[r] = make_uint4(0, 0, 0, 0);
-        }
-    }
-  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kTcStages; ++s) {
       mbar_init(bar_full0 + 8 * s, 1);
       mbar_init(bar_empty0 + 8 * s, 1);
     }
     mbar_init(bar_acc, 1);
+    mbar_init(bar_tfree, 8);
+    mbar_init(bar_drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // make the generic-proxy zero fill visible to the tensor core (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
                      smem_u32(tmem_slot))
@@ -439,90 +452,108 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  bool failed = false;
 
   if (warp == 0) {
     if (lane == 0) {
-      const int64_t plane_stride = (int64_t)nkb * kTcKc * cpad;  // in 16-byte chunks
-      const uint32_t tx = (uint32_t)kTcPlanes * kTcKc * (uint32_t)(tile.am + tile.bn) * 16u;
-      int issued = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % kTcStages;
-        const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
-        if (!mbar_wait(bar_empty0 + 8 * s, ph ^ 1u)) {
-          failed = true;
-          break;
-        }
-        const uint32_t full = bar_full0 + 8 * s;
-        mbar_expect_tx(full, tx);
-        const uint32_t st = smem_u32(stage_base + (size_t)s * kTcStageBytes);
-        for (int pl = 0; pl < kTcPlanes; ++pl) {
-          const int64_t pbase = (((int64_t)f * kTcPlanes + pl) * nkb + kb) * kTcKc * cpad;
-          for (int kc = 0; kc < kTcKc; ++kc) {
-            const uint4* srcA = packed + pbase + (int64_t)kc * cpad + tile.a0;
-            const uint4* srcB = packed + pbase + (int64_t)kc * cpad + tile.b0;
-            bulk_g2s(st + pl * a_plane_bytes + kc * kTcM * 16, srcA, (uint32_t)tile.am * 16u, full);
-            bulk_g2s(st + kTcABytes + pl * b_plane_bytes + kc * n * 16, srcB, (uint32_t)tile.bn * 16u,
-                     full);
+      int64_t q = 0;  // K-blocks issued
+      bool failed = false;
+      for (int64_t i = blockIdx.x; i < total && !failed; i += G) {
+        const int f = (int)(i / ntiles);
+        const TcTile tile = tiles[i % ntiles];
+        const uint32_t b_plane_bytes = (uint32_t)tile.n * kTcKb * 2;
+        const uint32_t tx = (uint32_t)kTcPlanes * kTcKc * (uint32_t)(tile.am + tile.bn) * 16u;
+        for (int kb = 0; kb < nkb; ++kb, ++q) {
+          const int s = (int)(q % kTcStages);
+          const uint32_t ph = (uint32_t)(q / kTcStages) & 1u;
+          if (!mbar_wait(bar_empty0 + 8 * s, ph ^ 1u)) {
+            failed = true;
+            break;
+          }
+          const uint32_t full = bar_full0 + 8 * s;
+          mbar_expect_tx(full, tx);
+          const uint32_t st = smem_u32(stage_base + (size_t)s * kTcStageBytes);
+          for (int pl = 0; pl < kTcPlanes; ++pl) {
+            const int64_t pbase = (((int64_t)f * kTcPlanes + pl) * nkb + kb) * kTcKc * cpad;
+            for (int kc = 0; kc < kTcKc; ++kc) {
+              const uint4* srcA = packed + pbase + (int64_t)kc * cpad + tile.a0;
+              const uint4* srcB = packed + pbase + (int64_t)kc * cpad + tile.b0;
+              bulk_g2s(st + pl * a_plane_bytes + kc * kTcM * 16, srcA, (uint32_t)tile.am * 16u, full);
+              bulk_g2s(st + kTcABytes + pl * b_plane_bytes + kc * tile.n * 16, srcB, (uint32_t)tile.bn * 16u,
+                       full);
+            }
           }
         }
-        ++issued;
       }
-      (void)plane_stride;
       if (failed) {
         atomicExch(err, 1);
-        // drain the copies already issued before leaving
-        for (int kb = 0; kb < issued; ++kb) (void)mbar_wait(bar_full0 + 8 * (kb % kTcStages),
-                                                            (uint32_t)(kb / kTcStages) & 1u);
+        // the copies of the last issued K-blocks may still be in flight
+        for (int64_t r = q - 1; r >= 0 && r >= q - kTcStages; --r)
+          (void)mbar_wait(bar_full0 + 8 * (int)(r % kTcStages), (uint32_t)(r / kTcStages) & 1u);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t id_pos = umma_idesc(kTcM, n, false);
-      const uint32_t id_neg = umma_idesc(kTcM, n, true);
       const uint32_t acc_re = tmem, acc_im = tmem + kTcAccImCol;
-      const uint32_t a_lbo = kTcM * 16, b_lbo = (uint32_t)n * 16, sbo = 128;
-      bool first = true;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % kTcStages;
-        const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
-        if (!mbar_wait(bar_full0 + 8 * s, ph)) {
+      int64_t q = 0;
+      bool failed = false;
+      for (int64_t i = blockIdx.x, li = 0; i < total && !failed; i += G, ++li) {
+        const TcTile tile = tiles[i % ntiles];
+        const int n = tile.n;
+        const uint32_t id_pos = umma_idesc(kTcM, n, false);
+        const uint32_t id_neg = umma_idesc(kTcM, n, true);
+        const uint32_t b_plane_bytes = (uint32_t)n * kTcKb * 2;
+        const uint32_t a_lbo = kTcM * 16, b_lbo = (uint32_t)n * 16, sbo = 128;
+        // the epilogue of the previous item has read the accumulators
+        if (li > 0 && !mbar_wait(bar_tfree, (uint32_t)(li - 1) & 1u)) {
           failed = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t st = smem_u32(stage_base + (size_t)s * kTcStageBytes);
-        const uint32_t sa = st, sb = st + kTcABytes;
-#pragma unroll
-        for (int ks = 0; ks < kTcKc / 2; ++ks) {
-          const uint32_t koff_a = ks * 2 * a_lbo, koff_b = ks * 2 * b_lbo;
-          uint64_t A[4], B[4];
-#pragma unroll
-          for (int pl = 0; pl < 4; ++pl) {
-            A[pl] = umma_desc(sa + pl * a_plane_bytes + koff_a, a_lbo, sbo);
-            B[pl] = umma_desc(sb + pl * b_plane_bytes + koff_b, b_lbo, sbo);
+        bool first = true;
+        for (int kb = 0; kb < nkb; ++kb, ++q) {
+          const int s = (int)(q % kTcStages);
+          const uint32_t ph = (uint32_t)(q / kTcStages) & 1u;
+          if (!mbar_wait(bar_full0 + 8 * s, ph)) {
+            failed = true;
+            break;
           }
-          const uint32_t acc = first ? 0u : 1u;
-          // Re += re.re + im.im (hi.hi, hi.lo, lo.hi)
-          umma_bf16(acc_re, A[0], B[0], id_pos, acc);
-          umma_bf16(acc_re, A[0], B[1], id_pos, 1);
-          umma_bf16(acc_re, A[1], B[0], id_pos, 1);
-          umma_bf16(acc_re, A[2], B[2], id_pos, 1);
-          umma_bf16(acc_re, A[2], B[3], id_pos, 1);
-          umma_bf16(acc_re, A[3], B[2], id_pos, 1);
-          // Im += re.im - im.re
-          umma_bf16(acc_im, A[0], B[2], id_pos, acc);
-          umma_bf16(acc_im, A[0], B[3], id_pos, 1);
-          umma_bf16(acc_im, A[1], B[2], id_pos, 1);
-          umma_bf16(acc_im, A[2], B[0], id_neg, 1);
-          umma_bf16(acc_im, A[2], B[1], id_neg, 1);
-          umma_bf16(acc_im, A[3], B[0], id_neg, 1);
-          first = false;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = smem_u32(stage_base + (size_t)s * kTcStageBytes);
+          const uint32_t sa = st, sb = st + kTcABytes;
+#pragma unroll
+          for (int ks = 0; ks < kTcKc / 2; ++ks) {
+            const uint32_t koff_a = ks * 2 * a_lbo, koff_b = ks * 2 * b_lbo;
+            uint64_t A[4], B[4];
+#pragma unroll
+            for (int pl = 0; pl < 4; ++pl) {
+              A[pl] = umma_desc(sa + pl * a_plane_bytes + koff_a, a_lbo, sbo);
+              B[pl] = umma_desc(sb + pl * b_plane_bytes + koff_b, b_lbo, sbo);
+            }
+            const uint32_t acc = first ? 0u : 1u;
+            // Re += re.re + im.im (hi.hi, hi.lo, lo.hi)
+            umma_bf16(acc_re, A[0], B[0], id_pos, acc);
+            umma_bf16(acc_re, A[0], B[1], id_pos, 1);
+            umma_bf16(acc_re, A[1], B[0], id_pos, 1);
+            umma_bf16(acc_re, A[2], B[2], id_pos, 1);
+            umma_bf16(acc_re, A[2], B[3], id_pos, 1);
+            umma_bf16(acc_re, A[3], B[2], id_pos, 1);
+            // Im += re.im - im.re
+            umma_bf16(acc_im, A[0], B[2], id_pos, acc);
+            umma_bf16(acc_im, A[0], B[3], id_pos, 1);
+            umma_bf16(acc_im, A[1], B[2], id_pos, 1);
+            umma_bf16(acc_im, A[2], B[0], id_neg, 1);
+            umma_bf16(acc_im, A[2], B[1], id_neg, 1);
+            umma_bf16(acc_im, A[3], B[0], id_neg, 1);
+            first = false;
+          }
+          umma_commit(bar_empty0 + 8 * s);  // stage free once these MMAs are done
         }
-        umma_commit(bar_empty0 + 8 * s);  // stage free once these MMAs are done
+        if (!failed) umma_commit(bar_acc);  // this item's accumulators are complete
       }
       if (failed) atomicExch(err, 1);
-      umma_commit(bar_acc);  // accumulators complete (or abandoned)
+      // every MMA issued has completed before TMEM is freed
+      umma_commit(bar_drain);
+      (void)mbar_wait(bar_drain, 0);
     }
   } else {
     // epilogue warps 2..9: TMEM lane quarter = warp % 4; the two warps of a
@@ -531,13 +562,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
     const int row = q * 32 + lane;  // src row within the tile
-    const bool ok = mbar_wait(bar_acc, 0);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!ok) {
-      atomicExch(err, 1);
-      failed = true;
-    } else {
-      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    for (int64_t i = blockIdx.x, li = 0; i < total; i += G, ++li) {
+      const int64_t f = i / ntiles;
+      const TcTile tile = tiles[i % ntiles];
+      const int n = tile.n;
       const int4* map4 = reinterpret_cast<const int4*>(maps + tile.map_offset + (int64_t)row * n);
       const bool row_ok = row < tile.am;
       int4 mcur[4], mnxt[4];
@@ -546,6 +575,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
         for (int k = 0; k < 4; ++k) mcur[k] = __ldg(map4 + c0 / 4 + k);
       }
+      if (!mbar_wait(bar_acc, (uint32_t)li & 1u)) {
+        atomicExch(err, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (; c0 < n; c0 += 32) {
         const int c1 = c0 + 32;
         if (row_ok && c1 < n) {
@@ -557,11 +591,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tmem_ld16(lane_base + kTcAccImCol + (uint32_t)c0, im);
         tmem_ld_wait();
         if (row_ok)  // padding columns (b >= bn) hold -1
-          store_pairs16(stack, stack_pitch, f, reinterpret_cast<const int32_t*>(mcur), re, im, scale,
-                        accumulate);
+          store_slots16(binmajor + f * bin_pitch, reinterpret_cast<const int32_t*>(mcur), re, im, scale);
 #pragma unroll
         for (int k = 0; k < 4; ++k) mcur[k] = mnxt[k];
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar_tfree);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -570,7 +606,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
   }
-  (void)nspec;
 }
 
 // ---------------------------------------------------------------------------
@@ -817,11 +852,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
-// Bin-major rows -> the [pair][bin] stack: stack[p][f] (+)= binmajor[f][p],
-// through 32 x 32 shared-memory tiles so both sides move in 256-byte runs.
+// Bin-major rows -> the [pair][bin] stack: stack[perm[q]][f] (+)=
+// binmajor[f][q], through 32 x 32 shared-memory tiles so both sides move in
+// 256-byte runs (each slot's 32 bins are one run of its pair row).
 __global__ void __launch_bounds__(256)
     k_xc_binmajor_to_stack(const float2* __restrict__ binmajor, int64_t bin_pitch, int64_t npairs, int nspec,
-                           float2* __restrict__ stack, int64_t stack_pitch, int accumulate) {
+                           const int32_t* __restrict__ perm, float2* __restrict__ stack, int64_t stack_pitch,
+                           int accumulate) {
   __shared__ float2 tile[32][33];
   const int64_t p0 = (int64_t)blockIdx.x * 32;
   const int f0 = blockIdx.y * 32;
@@ -835,11 +872,11 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
 #pragma unroll
   for (int k = ty; k < 32; k += 8) {
-    const int64_t p = p0 + k;
+    const int64_t q = p0 + k;
     const int f = f0 + tx;
-    if (p < npairs && f < nspec) {
+    if (q < npairs && f < nspec) {
       float2 v = tile[tx][k];
-      float2* d = stack + p * stack_pitch + f;
+      float2* d = stack + (int64_t)__ldg(perm + q) * stack_pitch + f;
       if (accumulate) {
         const float2 o = *d;
         v.x += o.x;
@@ -933,21 +970,39 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
     int64_t bin_pitch = 0;
     FXC_TRY(gemm_bin_rows(ctx, plan, packed, nkb, nspec, scale, &binmajor, &bin_pitch));
     const dim3 tg((unsigned)((plan->npairs + 31) / 32), (unsigned)((nspec + 31) / 32));
-    k_xc_binmajor_to_stack<<<tg, 256, 0, ctx->stream>>>(binmajor, bin_pitch, plan->npairs, nspec, stack,
-                                                         stack_pitch, accumulate);
+    k_xc_binmajor_to_stack<<<tg, 256, 0, ctx->stream>>>(binmajor, bin_pitch, plan->npairs, nspec, tp->d_perm,
+                                                         stack, stack_pitch, accumulate);
     count_launch();
     FXC_LAUNCH_CHECK();
     return FXC_OK;
   }
   FXC_TRY(set_smem_limit(k_xc_tc_gemm, kTcSmemBytes));
-  dim3 gg((unsigned)tp->ntiles, (unsigned)nspec);
-  KernelTimer kt(ctx, "k_xc_tc_gemm");
-  k_xc_tc_gemm<<<gg, kTcThreads, kTcSmemBytes, ctx->stream>>>(
-      packed, nkb, tp->cpad, tp->d_tiles, tp->d_maps, nspec, scale, stack, stack_pitch, accumulate,
-      ctx->d_err);
-  kt.stop();
-  count_launch();
-  FXC_LAUNCH_CHECK();
+  // one persistent CTA per SM (the operand ring fills the shared memory)
+  int nsm = 0;
+  FXC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+  // bin-major rows of at most kBinMajorCap bytes per pass, then transposed
+  const int64_t bin_pitch = round_up(plan->npairs, 4);
+  const int64_t fb = std::max<int64_t>(1, std::min<int64_t>(nspec, kBinMajorCap / (bin_pitch * 8)));
+  FXC_TRY(ctx->scratch5.reserve(sizeof(float2) * (size_t)bin_pitch * (size_t)fb));
+  float2* binmajor = reinterpret_cast<float2*>(ctx->scratch5.ptr);
+  const int64_t per_bin = (int64_t)kTcPlanes * nkb * kTcKc * tp->cpad;  // 16-byte chunks per bin
+  for (int64_t f0 = 0; f0 < nspec; f0 += fb) {
+    const int nb = (int)std::min<int64_t>(fb, nspec - f0);
+    const int64_t items = tp->ntiles * (int64_t)nb;
+    const unsigned grid = (unsigned)std::min<int64_t>(items, std::max(nsm, 1));
+    KernelTimer kt(ctx, "k_xc_tc_gemm");
+    k_xc_tc_gemm<<<grid, kTcThreads, kTcSmemBytes, ctx->stream>>>(
+        packed + f0 * per_bin, nkb, tp->cpad, tp->d_tiles, (int)tp->ntiles, tp->d_maps, nb, scale, binmajor,
+        bin_pitch, ctx->d_err);
+    kt.stop();
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    const dim3 tg((unsigned)((plan->npairs + 31) / 32), (unsigned)((nb + 31) / 32));
+    k_xc_binmajor_to_stack<<<tg, 256, 0, ctx->stream>>>(binmajor, bin_pitch, plan->npairs, nb, tp->d_perm,
+                                                         stack + f0, stack_pitch, accumulate);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+  }
   return FXC_OK;
 }
 

@@ -148,6 +148,34 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
 
 
+@pytest.mark.parametrize("nwin", [24, 70])
+def test_tiled_contraction_above_256_channels(ctx, torch_cuda, nwin):
+    """Above 192 channels the persistent tiled contraction runs (bin, tile)
+    items: several 256-column chunks per row block, pairs listed twice (an
+    extra tile layer), reversed pairs, a partial K-block, few bins per CTA
+    and many; same stack as the FP64 oracle."""
+    torch = torch_cuda
+    from fastxc_gb300.core import PairPlan
+
+    rng = np.random.default_rng(23)
+    nchan, nspec = 300, 129
+    spec = make_spec(rng, nwin, nchan, nspec)
+    iu, ju = np.triu_indices(nchan)
+    keep = rng.random(iu.size) < 0.05
+    src, rec = iu[keep].astype(np.int32), ju[keep].astype(np.int32)
+    dup = rng.choice(src.size, 500, replace=False)
+    src, rec = np.concatenate([src, src[dup]]), np.concatenate([rec, rec[dup]])
+    flip = rng.random(src.size) < 0.3
+    src, rec = np.where(flip, rec, src).astype(np.int32), np.where(flip, src, rec).astype(np.int32)
+    plan = PairPlan(ctx, src, rec, nchan)
+    d_spec = torch.from_numpy(spec).cuda()
+    got = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+    ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, got, nspec, 1)
+    ctx.synchronize()
+    ref = xo.xc_stack(spec, src, rec, 0.5)
+    assert rel_l2(got.cpu().numpy(), ref) < 2e-5
+
+
 @pytest.mark.parametrize("env", [{}, {"FXC_GEMM_TILED": "1"}, {"FXC_FINALIZE": "pruned"}])
 def test_stack_finalize_packed_equals_stack_then_finalize(ctx, torch_cuda, env, monkeypatch):
     """fxc_xc_stack_finalize_packed gives the same NCF bits as
