@@ -11,7 +11,9 @@
 //     with digit-reversed output, or its transpose, decimation in time with
 //     digit-reversed input), one barrier per stage;
 //   * radices 2, 4, 8 are hand-written; odd primes up to 31 use the
-//     symmetric real-coefficient DFT; twiddles come from a per-length table
+//     symmetric real-coefficient DFT; composites 6, 9, 10, 12, 14, 15 run
+//     as two small DFTs in registers (one pass over shared memory for two
+//     factors); twiddles come from a per-length table
 //     computed in double precision on the host and rounded once to float.
 // Inverse transforms are forward transforms on conjugated data (the
 // conjugation is folded into the first load and the last store).
@@ -32,8 +34,10 @@ struct FftPlan {
   const int* perm;           // perm[k] = point holding frequency k after fft_dif (n entries)
 };
 
-// Host side (fft_plan.cu)
-int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out);
+// Host side (fft_plan.cu). composites = false keeps to the prime radices
+// and 4, 8 (the row kernels of the stacking stages, whose shared dispatch
+// would otherwise carry the composite stages).
+int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out, bool composites = true);
 // Cached device table perm[k] = fft_digit_pos(k) for the plan's radix order.
 int fft_perm_table(const FftPlan& p, const int** out);
 // Plan whose twiddle and digit-reversal tables are supplied by the caller
@@ -133,6 +137,45 @@ __constant__ float kOddSin[158] = {
     -3.943558551e-01f, -2.012985201e-01f};
 // offsets: R3:0, R5:3, R7:8, R11:15, R13:26, R17:39, R19:56, R23:75, R29:98, R31:127
 
+// cos(2*pi*m/R), sin(2*pi*m/R) for m in [0,R), composite R in {6,9,10,12,14,15}
+__constant__ float kCompCos[66] = {
+    +1.000000000e+00f, +5.000000000e-01f, -5.000000000e-01f, -1.000000000e+00f,
+    -5.000000000e-01f, +5.000000000e-01f, +1.000000000e+00f, +7.660444431e-01f,
+    +1.736481777e-01f, -5.000000000e-01f, -9.396926208e-01f, -9.396926208e-01f,
+    -5.000000000e-01f, +1.736481777e-01f, +7.660444431e-01f, +1.000000000e+00f,
+    +8.090169944e-01f, +3.090169944e-01f, -3.090169944e-01f, -8.090169944e-01f,
+    -1.000000000e+00f, -8.090169944e-01f, -3.090169944e-01f, +3.090169944e-01f,
+    +8.090169944e-01f, +1.000000000e+00f, +8.660254038e-01f, +5.000000000e-01f,
+    +6.123233996e-17f, -5.000000000e-01f, -8.660254038e-01f, -1.000000000e+00f,
+    -8.660254038e-01f, -5.000000000e-01f, -1.836970199e-16f, +5.000000000e-01f,
+    +8.660254038e-01f, +1.000000000e+00f, +9.009688679e-01f, +6.234898019e-01f,
+    +2.225209340e-01f, -2.225209340e-01f, -6.234898019e-01f, -9.009688679e-01f,
+    -1.000000000e+00f, -9.009688679e-01f, -6.234898019e-01f, -2.225209340e-01f,
+    +2.225209340e-01f, +6.234898019e-01f, +9.009688679e-01f, +1.000000000e+00f,
+    +9.135454576e-01f, +6.691306064e-01f, +3.090169944e-01f, -1.045284633e-01f,
+    -5.000000000e-01f, -8.090169944e-01f, -9.781476007e-01f, -9.781476007e-01f,
+    -8.090169944e-01f, -5.000000000e-01f, -1.045284633e-01f, +3.090169944e-01f,
+    +6.691306064e-01f, +9.135454576e-01f};
+__constant__ float kCompSin[66] = {
+    +0.000000000e+00f, +8.660254038e-01f, +8.660254038e-01f, +1.224646799e-16f,
+    -8.660254038e-01f, -8.660254038e-01f, +0.000000000e+00f, +6.427876097e-01f,
+    +9.848077530e-01f, +8.660254038e-01f, +3.420201433e-01f, -3.420201433e-01f,
+    -8.660254038e-01f, -9.848077530e-01f, -6.427876097e-01f, +0.000000000e+00f,
+    +5.877852523e-01f, +9.510565163e-01f, +9.510565163e-01f, +5.877852523e-01f,
+    +1.224646799e-16f, -5.877852523e-01f, -9.510565163e-01f, -9.510565163e-01f,
+    -5.877852523e-01f, +0.000000000e+00f, +5.000000000e-01f, +8.660254038e-01f,
+    +1.000000000e+00f, +8.660254038e-01f, +5.000000000e-01f, +1.224646799e-16f,
+    -5.000000000e-01f, -8.660254038e-01f, -1.000000000e+00f, -8.660254038e-01f,
+    -5.000000000e-01f, +0.000000000e+00f, +4.338837391e-01f, +7.818314825e-01f,
+    +9.749279122e-01f, +9.749279122e-01f, +7.818314825e-01f, +4.338837391e-01f,
+    +1.224646799e-16f, -4.338837391e-01f, -7.818314825e-01f, -9.749279122e-01f,
+    -9.749279122e-01f, -7.818314825e-01f, -4.338837391e-01f, +0.000000000e+00f,
+    +4.067366431e-01f, +7.431448255e-01f, +9.510565163e-01f, +9.945218954e-01f,
+    +8.660254038e-01f, +5.877852523e-01f, +2.079116908e-01f, -2.079116908e-01f,
+    -5.877852523e-01f, -8.660254038e-01f, -9.945218954e-01f, -9.510565163e-01f,
+    -7.431448255e-01f, -4.067366431e-01f};
+// offsets: R6:0, R9:6, R10:15, R12:25, R14:37, R15:51
+
 template <int R>
 struct OddRadixOffset;
 template <> struct OddRadixOffset<3> { static constexpr int v = 0; };
@@ -219,6 +262,57 @@ __device__ __forceinline__ void dft_odd(float2 (&x)[R]) {
 }
 
 template <int R>
+struct CompRadixOffset;
+template <> struct CompRadixOffset<6> { static constexpr int v = 0; };
+template <> struct CompRadixOffset<9> { static constexpr int v = 6; };
+template <> struct CompRadixOffset<10> { static constexpr int v = 15; };
+template <> struct CompRadixOffset<12> { static constexpr int v = 25; };
+template <> struct CompRadixOffset<14> { static constexpr int v = 37; };
+template <> struct CompRadixOffset<15> { static constexpr int v = 51; };
+
+template <int R>
+__device__ __forceinline__ void dft_any(float2 (&x)[R]);
+
+// Composite R = R1 * R2 in registers (one shared-memory pass instead of
+// two): with n = R2 n1 + n2 and k = k1 + R1 k2,
+//   X[k] = sum_n2 W_R^(n2 k1) W_R2^(n2 k2) sum_n1 x[n] W_R1^(n1 k1),
+// i.e. R2 DFTs of length R1, the inner twiddles W_R^(n2 k1), then R1 DFTs
+// of length R2; natural order in and out.
+template <int R1, int R2>
+__device__ __forceinline__ void dft_comp(float2 (&x)[R1 * R2]) {
+  constexpr int R = R1 * R2;
+  constexpr int OFF = CompRadixOffset<R>::v;
+  float2 y[R];  // y[n2 * R1 + k1]
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) {
+    float2 a[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) a[n1] = x[R2 * n1 + n2];
+    dft_any<R1>(a);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) {
+      const int m = (n2 * k1) % R;
+      if (m == 0) {
+        y[n2 * R1 + k1] = a[k1];
+      } else {
+        // a * exp(-2 pi i m / R)
+        const float c = kCompCos[OFF + m], sn = kCompSin[OFF + m];
+        y[n2 * R1 + k1] = make_float2(fmaf(a[k1].x, c, a[k1].y * sn), fmaf(a[k1].y, c, -a[k1].x * sn));
+      }
+    }
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) {
+    float2 b[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) b[n2] = y[n2 * R1 + k1];
+    dft_any<R2>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) x[k1 + R1 * k2] = b[k2];
+  }
+}
+
+template <int R>
 __device__ __forceinline__ void dft_any(float2 (&x)[R]) {
   if constexpr (R == 2) {
     dft2(x);
@@ -226,6 +320,18 @@ __device__ __forceinline__ void dft_any(float2 (&x)[R]) {
     dft4(x);
   } else if constexpr (R == 8) {
     dft8(x);
+  } else if constexpr (R == 6) {
+    dft_comp<2, 3>(x);
+  } else if constexpr (R == 9) {
+    dft_comp<3, 3>(x);
+  } else if constexpr (R == 10) {
+    dft_comp<2, 5>(x);
+  } else if constexpr (R == 12) {
+    dft_comp<4, 3>(x);
+  } else if constexpr (R == 14) {
+    dft_comp<2, 7>(x);
+  } else if constexpr (R == 15) {
+    dft_comp<3, 5>(x);
   } else {
     dft_odd<R>(x);
   }
@@ -308,9 +414,20 @@ __device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float
   __syncthreads();
 }
 
-template <int T, bool DIT>
+template <int T, bool DIT, bool COMP = true>
 __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, const float2* stw,
                                               int R, int L, int tw_step, bool ci, bool co) {
+  if constexpr (COMP) {
+    switch (R) {
+      case 6: fft_stage_ip<6, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 9: fft_stage_ip<9, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 10: fft_stage_ip<10, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 12: fft_stage_ip<12, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 14: fft_stage_ip<14, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 15: fft_stage_ip<15, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      default: break;
+    }
+  }
   switch (R) {
     case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
     case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
@@ -332,7 +449,7 @@ __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, con
 // Natural-order input, digit-reversed output. All T threads must call it
 // after buf and the twiddle table stw (fft_twiddles_to_smem) are written and
 // the CTA synchronised; the result is visible to the CTA on return.
-template <int T>
+template <int T, bool COMP = true>
 __device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = p.n;
   int Rprod = 1;  // r_0 ... r_{s-1}
@@ -341,14 +458,14 @@ __device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool i
     L /= R;
     // block length B = L*R = n / Rprod; twiddle w_B^{tj} = w_n^{t j Rprod}
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, false>(buf, p, stw, R, L, tw_step, inverse && s == 0,
+    fft_run_stage<T, false, COMP>(buf, p, stw, R, L, tw_step, inverse && s == 0,
                             inverse && s == p.nstages - 1);
     Rprod *= R;
   }
 }
 
 // Digit-reversed input (the layout fft_dif produces), natural-order output.
-template <int T>
+template <int T, bool COMP = true>
 __device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = 1;
   int Rprod = p.n;
@@ -356,7 +473,7 @@ __device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool i
     const int R = p.radix[s];
     Rprod /= R;
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, true>(buf, p, stw, R, L, tw_step, inverse && s == p.nstages - 1,
+    fft_run_stage<T, true, COMP>(buf, p, stw, R, L, tw_step, inverse && s == p.nstages - 1,
                            inverse && s == 0);
     L *= R;
   }

@@ -45,10 +45,10 @@ __device__ void bluestein(float2* buf, const AnyPlan& a, const float2* stw, bool
     buf[j] = v;
   }
   __syncthreads();
-  fft_dif<T>(buf, a.p, stw, false);
+  fft_dif<T, false>(buf, a.p, stw, false);
   for (int j = threadIdx.x; j < m; j += T) buf[j] = cmul(buf[j], __ldg(a.khat + j));
   __syncthreads();
-  fft_dit<T>(buf, a.p, stw, true);
+  fft_dit<T, false>(buf, a.p, stw, true);
   for (int k = threadIdx.x; k < n; k += T) {
     const float2 y = cmul(buf[k], __ldg(a.chirp + k));
     buf[k] = inverse ? conjf2(y) : y;
@@ -63,7 +63,7 @@ __device__ __forceinline__ void any_forward(float2* buf, const AnyPlan& a, const
   if (a.chirp)
     bluestein<T>(buf, a, stw, false);
   else
-    fft_dif<T>(buf, a.p, stw, false);
+    fft_dif<T, false>(buf, a.p, stw, false);
 }
 
 // Unnormalised inverse from the any_forward layout to natural order.
@@ -72,10 +72,11 @@ __device__ __forceinline__ void any_inverse(float2* buf, const AnyPlan& a, const
   if (a.chirp)
     bluestein<T>(buf, a, stw, true);
   else
-    fft_dit<T>(buf, a.p, stw, true);
+    fft_dit<T, false>(buf, a.p, stw, true);
 }
 
-// Host: direct plan when n factors into the supported radices and
+// Host: plans without composite radices (the row kernels dispatch only the
+// prime radices and 2, 4, 8). Direct plan when n factors into them and
 // n <= direct_max, else Bluestein over the smallest 2-3-5-7-smooth m >= 2n-1
 // (m <= bluestein_max). Tables are cached per device and length.
 int any_plan(int n, int direct_max, int bluestein_max, AnyPlan* out);

@@ -4,6 +4,7 @@
 #include <complex>
 #include <cstdint>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -15,29 +16,58 @@ namespace fxc {
 
 static const int kOddRadices[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
 
-static bool factorize(int n, std::vector<int>* out) {
+// Stages of an n-point transform: radix-8 stages for the powers of two, the
+// leftover 2 or 4 folded with an odd prime into a composite radix (14, 10,
+// 6 or 12), 3s folded with 5s (15) or with each other (9), then the
+// remaining primes. Fewer stages mean fewer passes over shared memory and
+// fewer barriers; every radix stays small enough for one thread's registers.
+static bool factorize(int n, std::vector<int>* out, bool composites = true) {
   out->clear();
   if (n < 1) return false;
   int m = n;
-  // powers of two: as many radix-8 stages as possible, then one 4 or 2
   int twos = 0;
   while (m % 2 == 0) {
     m /= 2;
     ++twos;
   }
-  while (twos >= 3) {
-    out->push_back(8);
-    twos -= 3;
-  }
-  if (twos == 2) out->push_back(4);
-  if (twos == 1) out->push_back(2);
+  std::map<int, int> odd;  // prime -> multiplicity
   for (int r : kOddRadices) {
     while (m % r == 0) {
-      out->push_back(r);
+      ++odd[r];
       m /= r;
     }
   }
   if (m != 1) return false;
+  auto take = [&](int r) {
+    auto it = odd.find(r);
+    if (it == odd.end() || it->second == 0) return false;
+    --it->second;
+    return true;
+  };
+  for (; twos >= 3; twos -= 3) out->push_back(8);
+  if (!composites) {
+    if (twos == 2) out->push_back(4);
+    if (twos == 1) out->push_back(2);
+  } else if (twos == 1) {
+    if (take(7)) out->push_back(14);
+    else if (take(5)) out->push_back(10);
+    else if (take(3)) out->push_back(6);
+    else out->push_back(2);
+  } else if (twos == 2) {
+    if (take(3)) out->push_back(12);
+    else out->push_back(4);
+  }
+  while (composites && odd[3] >= 1 && odd[5] >= 1) {
+    --odd[3];
+    --odd[5];
+    out->push_back(15);
+  }
+  while (composites && odd[3] >= 2) {
+    odd[3] -= 2;
+    out->push_back(9);
+  }
+  for (int r : kOddRadices)
+    for (int k = 0; k < odd[r]; ++k) out->push_back(r);
   if ((int)out->size() > kFftMaxStages) return false;
   return true;
 }
@@ -47,9 +77,9 @@ bool fft_length_supported(int n) {
   return factorize(n, &f);
 }
 
-int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out) {
+int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out, bool composites) {
   std::vector<int> f;
-  if (!factorize(n, &f)) {
+  if (!factorize(n, &f, composites)) {
     set_error("FFT length %d has a prime factor above 31 (not supported by the in-CTA FFT)", n);
     return FXC_ERR_UNSUPPORTED;
   }
@@ -96,11 +126,13 @@ void fft_perm_values(const FftPlan& p, int* out) {
 
 int fft_perm_table(const FftPlan& p, const int** out) {
   static std::mutex mu;
-  static std::map<std::pair<int, int>, int*> cache;
+  // one table per device, length and radix sequence (composite radices make
+  // different digit orders for the same length)
+  static std::map<std::tuple<int, int, std::vector<int>>, int*> cache;
   int dev = 0;
   FXC_CUDA_TRY(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lock(mu);
-  auto key = std::make_pair(dev, p.n);
+  auto key = std::make_tuple(dev, p.n, std::vector<int>(p.radix, p.radix + p.nstages));
   auto it = cache.find(key);
   if (it != cache.end()) {
     *out = it->second;
@@ -220,7 +252,7 @@ int any_plan(int n, int direct_max, int bluestein_max, AnyPlan* out) {
   if (n <= direct_max && fft_length_supported(n)) {
     const float2* tw = nullptr;
     FXC_TRY(fft_twiddles(n, &tw));
-    FXC_TRY(fft_make_plan(n, tw, 1, &a.p));
+    FXC_TRY(fft_make_plan(n, tw, 1, &a.p, false));
     *out = a;
     return FXC_OK;
   }
@@ -233,7 +265,7 @@ int any_plan(int n, int direct_max, int bluestein_max, AnyPlan* out) {
   }
   const float2* tw = nullptr;
   FXC_TRY(fft_twiddles(m, &tw));
-  FXC_TRY(fft_make_plan(m, tw, 1, &a.p));
+  FXC_TRY(fft_make_plan(m, tw, 1, &a.p, false));
   static std::mutex mu;
   static std::map<std::pair<int, int>, std::pair<float2*, float2*>> cache;
   int dev = 0;
