@@ -35,7 +35,7 @@
 
 namespace fxc {
 
-constexpr int kStT = 64;           // threads per row transform CTA
+constexpr int kStT = 96;           // threads per row transform CTA
 constexpr int kStNmax = 8192;      // longest directly transformed trace
 constexpr int kStBluestein = 16384;  // longest Bluestein length (any other trace length)
 
@@ -121,21 +121,26 @@ __device__ __forceinline__ float weight_pow(float mag2, float power) {
 }
 
 // ---------------------------------------------------------------------------
-// PWS: one CTA per pair
+// PWS: one CTA per (pair, chunk of groups)
 // ---------------------------------------------------------------------------
 
+// CTA (pair p, chunk c) sums the weighted unit phasors of groups
+// [c * cg, (c + 1) * cg) of pair p into partial row (p, c); k_pws_combine
+// adds a pair's partial rows in chunk order. Chunks keep the grid many
+// waves deep (one CTA per pair left the last of 2.5 waves half empty).
 __global__ void __launch_bounds__(kStT)
     k_pws(const float* __restrict__ groups, const float* __restrict__ weights,
-          const int64_t* __restrict__ goffs, const int32_t* __restrict__ gcounts,
-          const float* __restrict__ linear, AnyPlan a, float power, float* __restrict__ out) {
+          const int64_t* __restrict__ goffs, const int32_t* __restrict__ gcounts, int cg, AnyPlan a,
+          float2* __restrict__ partial) {
   extern __shared__ float2 sm[];
   const int n = a.n;
   float2* buf = sm;
   float2* acc = sm + any_buf_elems(a);
   float2* stw = acc + n;
   const int pair = blockIdx.x;
-  const int64_t goff = goffs[pair];
-  const int ng = gcounts[pair];
+  const int g0 = blockIdx.y * cg;
+  const int64_t goff = goffs[pair] + g0;
+  const int ng = max(0, min(cg, gcounts[pair] - g0));
   fft_twiddles_to_smem<kStT>(a.p, stw);
   for (int t = threadIdx.x; t < n; t += kStT) acc[t] = make_float2(0.f, 0.f);
   const float invn = 1.0f / (float)n;
@@ -210,11 +215,23 @@ __global__ void __launch_bounds__(kStT)
     }
   }
   __syncthreads();
-  const float* lin = linear + (int64_t)pair * n;
-  float* o = out + (int64_t)pair * n;
-  for (int t = threadIdx.x; t < n; t += kStT) {
-    const float2 a = acc[t];
-    o[t] = lin[t] * weight_pow(a.x * a.x + a.y * a.y, power);
+  float2* o = partial + ((int64_t)pair * gridDim.y + blockIdx.y) * n;
+  for (int t = threadIdx.x; t < n; t += kStT) o[t] = acc[t];
+}
+
+// out[p] = lin[p] * |sum_c partial[p][c]|^power, chunks added in order.
+__global__ void k_pws_combine(const float2* __restrict__ partial, int nchunks, const float* __restrict__ linear,
+                              int n, int64_t total, float power, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = i / n, t = i - p * n;
+    const float2* row = partial + p * nchunks * n + t;
+    float2 s = row[0];
+    for (int c = 1; c < nchunks; ++c) {
+      const float2 v = row[(int64_t)c * n];
+      s.x += v.x;
+      s.y += v.y;
+    }
+    out[i] = linear[i] * weight_pow(s.x * s.x + s.y * s.y, power);
   }
 }
 
@@ -576,8 +593,26 @@ int fxc_pws_run(fxc_ctx* ctx, const float* d_groups, const float* d_weights,
   const size_t smem =
       sizeof(float2) * ((size_t)any_buf_elems(a) + (size_t)nsamples + fft_tw_smem_elems(a.p));
   FXC_TRY(set_smem_limit(k_pws, smem));
-  k_pws<<<(unsigned)npairs, kStT, smem, ctx->stream>>>(d_groups, d_weights, d_goff, d_gcnt, d_linear,
-                                                        a, power, d_out);
+  // chunks of an even number of groups, enough CTAs for ~8 waves of the
+  // resident ones (register-bound at about 6 per SM)
+  int ngmax = 1, nsm = 0;
+  for (int p = 0; p < npairs; ++p) ngmax = std::max(ngmax, (int)h_group_counts[p]);
+  FXC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int64_t want = std::max<int64_t>(1, (8LL * 6 * std::max(nsm, 1) + npairs - 1) / npairs);
+  int nchunks = (int)std::min<int64_t>(want, (ngmax + 1) / 2);
+  int cg = (ngmax + nchunks - 1) / nchunks;
+  cg += cg & 1;
+  nchunks = (ngmax + cg - 1) / cg;
+  FXC_CHECK_ARG(nchunks <= 65535, "too many group chunks");
+  FXC_TRY(ctx->scratch4.reserve(sizeof(float2) * (size_t)npairs * (size_t)nchunks * (size_t)nsamples));
+  float2* d_part = reinterpret_cast<float2*>(ctx->scratch4.ptr);
+  k_pws<<<dim3((unsigned)npairs, (unsigned)nchunks), kStT, smem, ctx->stream>>>(d_groups, d_weights, d_goff,
+                                                                               d_gcnt, cg, a, d_part);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  const int64_t total = (int64_t)npairs * nsamples;
+  k_pws_combine<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 32), 256, 0, ctx->stream>>>(
+      d_part, nchunks, d_linear, nsamples, total, power, d_out);
   count_launch();
   FXC_LAUNCH_CHECK();
   FXC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
