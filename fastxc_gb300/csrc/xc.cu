@@ -323,6 +323,49 @@ __global__ void __launch_bounds__(T, 1)
   (void)inv_norm_f;
 }
 
+// Finalize for nfft = N = 2M with M above the in-CTA limit and M/2 within
+// it (e.g. nfft 74 088 at 20 Hz): the C2R runs, as in k_xc_finalize, as the
+// M-point inverse of the folded spectrum Z (c2r_pre), x[2n] = Re z[n],
+// x[2n+1] = Im z[n]; z is pruned to the lags kept. With k = k1 + 2 k2 and
+// Q = M/2,
+//   z[n] = Y_0[n mod Q] + exp(2 pi i n / M) Y_1[n mod Q],
+//   Y_k1 = inverse DFT_Q of Z[k1 + 2 k2],
+// two Q-point transforms in shared memory per pair (against P transforms of
+// a full complex N-point split in k_xc_finalize_pruned: a quarter of the
+// transform work).
+template <int T>
+__global__ void __launch_bounds__(T, 1)
+    k_xc_finalize_half(const float2* __restrict__ stack, int64_t stack_pitch, FftPlan pq,
+                       const float2* __restrict__ twn, int M, int half_cc, int cc_size, double inv_norm,
+                       float* __restrict__ ncf) {
+  extern __shared__ float2 buf[];
+  const int Q = pq.n;
+  const int N = 2 * M;
+  // pq's twiddle table has stride N/Q = 4 over the N-point table, so stw
+  // also serves exp(-2 pi i m / N) for the twiddle of Y_1
+  float2* stw = buf + Q;
+  float* acc = reinterpret_cast<float*>(stw + fft_tw_smem_elems(pq));
+  fft_twiddles_to_smem<T>(pq, stw);
+  const float2* X = stack + (int64_t)blockIdx.x * stack_pitch;
+  for (int k1 = 0; k1 < 2; ++k1) {
+    __syncthreads();
+    for (int k2 = threadIdx.x; k2 < Q; k2 += T) buf[k2] = c2r_pre(X, M, k1 + 2 * k2, twn);
+    __syncthreads();
+    fft_dif<T>(buf, pq, stw, true);  // inverse DFT_Q, digit-reversed positions
+    for (int j = threadIdx.x; j < cc_size; j += T) {
+      int m = N - half_cc + j;
+      if (m >= N) m -= N;
+      const int n = m >> 1;
+      float2 v = buf[__ldg(pq.perm + (n >= Q ? n - Q : n))];
+      if (k1) v = cmul(v, conjf2(tw_lookup(stw, 2 * n)));  // exp(+2 pi i n / M)
+      const float x = (m & 1) ? v.y : v.x;
+      acc[j] = k1 ? acc[j] + x : x;
+    }
+  }
+  float* out = ncf + (int64_t)blockIdx.x * cc_size;
+  for (int j = threadIdx.x; j < cc_size; j += T) out[j] = (float)((double)acc[j] * inv_norm);
+}
+
 // Output-pruned finalize for any even nfft (also above the in-CTA FFT
 // limit, e.g. nfft 74 088 at 20 Hz): only the cc_size lags of the cut are
 // formed. With nfft = N = P*Q and k = k1 + P*k2,
@@ -363,13 +406,23 @@ __global__ void __launch_bounds__(T, 4)
     }
     __syncthreads();
     fft_dif<T>(buf, pq, stw, true);  // inverse DFT_Q, digit-reversed positions
+    // lag n = (N - half_cc + t) mod N of this thread's first t; from one t
+    // to the next (t += T) n mod Q advances by T mod Q and n k1 mod N by
+    // T k1 mod N, so no division is left in the loop
+    int n = N - half_cc + (int)threadIdx.x;
+    if (n >= N) n -= N;
+    int m = (int)(((long long)n * k1) % N);
+    int idx = n % Q;
+    const int dm = (int)(((long long)T * k1) % N);
+    const int di = T % Q;
     for (int t = threadIdx.x; t < cc_size; t += T) {
-      int n = N - half_cc + t;
-      if (n >= N) n -= N;
-      const float2 y = buf[__ldg(pq.perm + n % Q)];
-      const int m = (int)(((long long)n * k1) % N);
+      const float2 y = buf[__ldg(pq.perm + idx)];
       const float2 w = tw_lookup(stw, m);
       acc[t] += y.x * w.x + y.y * w.y;  // Re(y * conj(w)), w = exp(-2 pi i m / N)
+      m += dm;
+      if (m >= N) m -= N;
+      idx += di;
+      if (idx >= Q) idx -= Q;
     }
   }
   __syncthreads();
@@ -459,6 +512,21 @@ int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_
   FXC_CHECK_ARG(N % 2 == 0 && N >= 2, "nfft %d must be even", N);
   const int M = N / 2;
   FXC_CHECK_ARG(npairs <= 0x7fffffff, "too many pairs for one launch");
+  if (M > kFftLargeNmax && !xc_finalize_prefers_pruned(N) && M % 2 == 0 && M / 2 <= kFftLargeNmax &&
+      fft_length_supported(M / 2) && s->cc_size <= 16384) {
+    const float2* twn = nullptr;
+    FXC_TRY(fft_twiddles(N, &twn));
+    FftPlan pq;
+    FXC_TRY(fft_make_plan(M / 2, twn, 4, &pq));
+    const double inv_norm = 1.0 / (double)((float)N * s->dt);
+    const size_t smem = sizeof(float2) * ((size_t)(M / 2) + fft_tw_smem_elems(pq)) + sizeof(float) * (size_t)s->cc_size;
+    FXC_TRY(set_smem_limit(k_xc_finalize_half<kFftLargeT>, smem));
+    k_xc_finalize_half<kFftLargeT><<<(unsigned)npairs, kFftLargeT, smem, ctx->stream>>>(
+        stack, stack_pitch, pq, twn, M, s->half_cc, s->cc_size, inv_norm, ncf);
+    count_launch();
+    FXC_LAUNCH_CHECK();
+    return FXC_OK;
+  }
   if (M > kFftLargeNmax || xc_finalize_prefers_pruned(N))
     return xc_finalize_pruned_launch(ctx, stack, npairs, stack_pitch, s, ncf);
   const float2* twn = nullptr;
