@@ -237,15 +237,62 @@ __global__ void k_pws_combine(const float2* __restrict__ partial, int nchunks, c
 
 // Streaming PWS: one group (e.g. one day's NCF of every pair) per call.
 // acc[p] += w * unit analytic phasor of row p, lin[p] += w * row p; the
-// same per-sample arithmetic as k_pws, summed call by call.
+// same per-sample arithmetic as k_pws, summed call by call. Odd lengths
+// take rows two at a time through one forward and one inverse transform
+// (the Hilbert parts of both; the real parts are x - mean), as k_pws does.
 __global__ void __launch_bounds__(kStT)
-    k_pws_stream_add(const float* __restrict__ rows, int64_t rows_pitch, AnyPlan a, float w,
+    k_pws_stream_add(const float* __restrict__ rows, int64_t rows_pitch, int nrows, AnyPlan a, float w,
                      float2* __restrict__ acc, float* __restrict__ lin) {
   extern __shared__ float2 sm[];
   const int n = a.n;
   float2* buf = sm;
   float2* stw = sm + any_buf_elems(a);
   fft_twiddles_to_smem<kStT>(a.p, stw);
+  if (n & 1) {
+    __shared__ float2 dc;
+    const int64_t r1 = 2 * (int64_t)blockIdx.x;
+    const bool two = r1 + 1 < nrows;
+    const float* x1 = rows + r1 * rows_pitch;
+    const float* x2 = two ? x1 + rows_pitch : x1;
+    for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x1[t], two ? x2[t] : 0.f);
+    __syncthreads();
+    any_forward<kStT>(buf, a, stw);
+    const int half = (n + 1) / 2;
+    for (int k = threadIdx.x; k < n; k += kStT) {
+      const int pos = any_pos(a, k);
+      const float2 z = buf[pos];
+      if (k == 0) dc = z;  // (sum x1, sum x2)
+      // -i z for 0 < k < N/2, +i z above, 0 at DC
+      buf[pos] = k == 0 ? make_float2(0.f, 0.f) : (k < half ? mul_mi(z) : mul_pi(z));
+    }
+    __syncthreads();
+    any_inverse<kStT>(buf, a, stw);
+    const float invn = 1.0f / (float)n;
+    const float m1 = dc.x * invn, m2 = dc.y * invn;
+    float2* ac1 = acc + r1 * n;
+    float* li1 = lin + r1 * n;
+    for (int t = threadIdx.x; t < n; t += kStT) {
+      const float2 h = buf[t];
+      float re = x1[t] - m1, im = h.x * invn;
+      float mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+      float2 v = ac1[t];
+      v.x += (re / mod) * w;
+      v.y += (im / mod) * w;
+      ac1[t] = v;
+      li1[t] += x1[t] * w;
+      if (two) {
+        re = x2[t] - m2;
+        im = h.y * invn;
+        mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+        v = ac1[n + t];
+        v.x += (re / mod) * w;
+        v.y += (im / mod) * w;
+        ac1[n + t] = v;
+        li1[n + t] += x2[t] * w;
+      }
+    }
+    return;
+  }
   const float* x = rows + (int64_t)blockIdx.x * rows_pitch;
   for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
   __syncthreads();
@@ -550,8 +597,9 @@ int fxc_pws_stream_add(fxc_ctx* ctx, const float* d_rows, int64_t rows_pitch, in
   FXC_TRY(stack_plan(nsamples, &a));
   const size_t smem = sizeof(float2) * ((size_t)any_buf_elems(a) + fft_tw_smem_elems(a.p));
   FXC_TRY(set_smem_limit(k_pws_stream_add, smem));
-  k_pws_stream_add<<<(unsigned)npairs, kStT, smem, ctx->stream>>>(d_rows, rows_pitch, a, weight,
-                                                                  reinterpret_cast<float2*>(d_acc), d_lin);
+  const unsigned grid = (nsamples & 1) ? (unsigned)((npairs + 1) / 2) : (unsigned)npairs;
+  k_pws_stream_add<<<grid, kStT, smem, ctx->stream>>>(d_rows, rows_pitch, npairs, a, weight,
+                                                      reinterpret_cast<float2*>(d_acc), d_lin);
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;
