@@ -11,7 +11,7 @@
 //     with digit-reversed output, or its transpose, decimation in time with
 //     digit-reversed input), one barrier per stage;
 //   * radices 2, 4, 8 are hand-written; odd primes up to 31 use the
-//     symmetric real-coefficient DFT; composites 6, 9, 10, 12, 14, 15 run
+//     symmetric real-coefficient DFT; composites 6, 9, 10, 12, 14, 15, 21 run
 //     as two small DFTs in registers (one pass over shared memory for two
 //     factors); twiddles come from a per-length table
 //     computed in double precision on the host and rounded once to float.
@@ -137,8 +137,8 @@ __constant__ float kOddSin[158] = {
     -3.943558551e-01f, -2.012985201e-01f};
 // offsets: R3:0, R5:3, R7:8, R11:15, R13:26, R17:39, R19:56, R23:75, R29:98, R31:127
 
-// cos(2*pi*m/R), sin(2*pi*m/R) for m in [0,R), composite R in {6,9,10,12,14,15}
-__constant__ float kCompCos[66] = {
+// cos(2*pi*m/R), sin(2*pi*m/R) for m in [0,R), composite R in {6,9,10,12,14,15,21}
+__constant__ float kCompCos[87] = {
     +1.000000000e+00f, +5.000000000e-01f, -5.000000000e-01f, -1.000000000e+00f,
     -5.000000000e-01f, +5.000000000e-01f, +1.000000000e+00f, +7.660444431e-01f,
     +1.736481777e-01f, -5.000000000e-01f, -9.396926208e-01f, -9.396926208e-01f,
@@ -155,8 +155,10 @@ __constant__ float kCompCos[66] = {
     +9.135454576e-01f, +6.691306064e-01f, +3.090169944e-01f, -1.045284633e-01f,
     -5.000000000e-01f, -8.090169944e-01f, -9.781476007e-01f, -9.781476007e-01f,
     -8.090169944e-01f, -5.000000000e-01f, -1.045284633e-01f, +3.090169944e-01f,
-    +6.691306064e-01f, +9.135454576e-01f};
-__constant__ float kCompSin[66] = {
+    +6.691306064e-01f, +9.135454576e-01f,
+    +1.000000000e+00f, +9.555728058e-01f, +8.262387743e-01f, +6.234898019e-01f, +3.653410244e-01f, +7.473009359e-02f, -2.225209340e-01f, -5.000000000e-01f, -7.330518718e-01f, -9.009688679e-01f, -9.888308262e-01f, -9.888308262e-01f, -9.009688679e-01f, -7.330518718e-01f, -5.000000000e-01f, -2.225209340e-01f, +7.473009359e-02f, +3.653410244e-01f, +6.234898019e-01f, +8.262387743e-01f, +9.555728058e-01f
+};
+__constant__ float kCompSin[87] = {
     +0.000000000e+00f, +8.660254038e-01f, +8.660254038e-01f, +1.224646799e-16f,
     -8.660254038e-01f, -8.660254038e-01f, +0.000000000e+00f, +6.427876097e-01f,
     +9.848077530e-01f, +8.660254038e-01f, +3.420201433e-01f, -3.420201433e-01f,
@@ -173,8 +175,10 @@ __constant__ float kCompSin[66] = {
     +4.067366431e-01f, +7.431448255e-01f, +9.510565163e-01f, +9.945218954e-01f,
     +8.660254038e-01f, +5.877852523e-01f, +2.079116908e-01f, -2.079116908e-01f,
     -5.877852523e-01f, -8.660254038e-01f, -9.945218954e-01f, -9.510565163e-01f,
-    -7.431448255e-01f, -4.067366431e-01f};
-// offsets: R6:0, R9:6, R10:15, R12:25, R14:37, R15:51
+    -7.431448255e-01f, -4.067366431e-01f,
+    +0.000000000e+00f, +2.947551744e-01f, +5.633200581e-01f, +7.818314825e-01f, +9.308737486e-01f, +9.972037972e-01f, +9.749279122e-01f, +8.660254038e-01f, +6.801727378e-01f, +4.338837391e-01f, +1.490422662e-01f, -1.490422662e-01f, -4.338837391e-01f, -6.801727378e-01f, -8.660254038e-01f, -9.749279122e-01f, -9.972037972e-01f, -9.308737486e-01f, -7.818314825e-01f, -5.633200581e-01f, -2.947551744e-01f
+};
+// offsets: R6:0, R9:6, R10:15, R12:25, R14:37, R15:51, R21:66
 
 template <int R>
 struct OddRadixOffset;
@@ -269,6 +273,7 @@ template <> struct CompRadixOffset<10> { static constexpr int v = 15; };
 template <> struct CompRadixOffset<12> { static constexpr int v = 25; };
 template <> struct CompRadixOffset<14> { static constexpr int v = 37; };
 template <> struct CompRadixOffset<15> { static constexpr int v = 51; };
+template <> struct CompRadixOffset<21> { static constexpr int v = 66; };
 
 template <int R>
 __device__ __forceinline__ void dft_any(float2 (&x)[R]);
@@ -332,6 +337,8 @@ __device__ __forceinline__ void dft_any(float2 (&x)[R]) {
     dft_comp<2, 7>(x);
   } else if constexpr (R == 15) {
     dft_comp<3, 5>(x);
+  } else if constexpr (R == 21) {
+    dft_comp<3, 7>(x);
   } else {
     dft_odd<R>(x);
   }
@@ -425,6 +432,7 @@ __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, con
       case 12: fft_stage_ip<12, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
       case 14: fft_stage_ip<14, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
       case 15: fft_stage_ip<15, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 21: fft_stage_ip<21, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
       default: break;
     }
   }

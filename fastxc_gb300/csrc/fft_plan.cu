@@ -18,8 +18,8 @@ static const int kOddRadices[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
 
 // Stages of an n-point transform: radix-8 stages for the powers of two, the
 // leftover 2 or 4 folded with an odd prime into a composite radix (14, 10,
-// 6 or 12), 3s folded with 5s (15) or with each other (9), then the
-// remaining primes. Fewer stages mean fewer passes over shared memory and
+// 6 or 12), 3s folded with 5s (15), with 7s (21) or with each other (9),
+// then the remaining primes. Fewer stages mean fewer passes over shared memory and
 // fewer barriers; every radix stays small enough for one thread's registers.
 static bool factorize(int n, std::vector<int>* out, bool composites = true) {
   out->clear();
@@ -61,6 +61,11 @@ static bool factorize(int n, std::vector<int>* out, bool composites = true) {
     --odd[3];
     --odd[5];
     out->push_back(15);
+  }
+  while (composites && odd[3] >= 1 && odd[7] >= 1) {
+    --odd[3];
+    --odd[7];
+    out->push_back(21);
   }
   while (composites && odd[3] >= 2) {
     odd[3] -= 2;
