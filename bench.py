@@ -560,8 +560,10 @@ def main():
             torch.distributed.barrier()
 
     # up to 192 channels one CTA runs both triangle tiles of a bin
-    gemm_kernel = ("k_xc_tc_gemm_bin" if nchan <= 192 and not os.environ.get("FXC_GEMM_TILED")
-                   else "k_xc_tc_gemm")
+    # (above 128 channels or 96 windows; shorter contractions over fewer
+    # channels, and more than 192 channels, run the persistent tiled kernel)
+    gemm_kernel = ("k_xc_tc_gemm_bin" if nchan <= 192 and (nchan > 128 or (nwin + 31) // 32 > 3)
+                   and not os.environ.get("FXC_GEMM_TILED") else "k_xc_tc_gemm")
     results = {}
     sampler = ClockSampler(local)
     clocks = None

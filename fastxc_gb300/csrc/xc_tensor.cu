@@ -899,10 +899,21 @@ static bool whole_bin_plan(const XcTensorPlan* tp) {
 }
 
 bool xc_gemm_accumulate_is_cheap(const fxc_pairplan* plan) {
-  // the whole-bin contraction accumulates in its coalesced transpose; the
-  // tiled one in scattered 8-byte read-modify-writes
+  // both contractions write bin-major rows and accumulate in the coalesced
+  // transpose into the stack
+  return plan->tensor != nullptr;
+}
+
+// The whole-bin kernel (one CTA per bin, C <= 192) unless the contraction
+// is short (at most three K-blocks) over at most 128 channels: then the
+// persistent tiled kernel, which pays the per-CTA setup once per SM rather
+// than once per bin, is ahead (at 90 channels and 24 windows 0.038 ms
+// against 0.050 ms per 512 bins; at 192 channels the two tie for short
+// contractions and from 264 windows the whole-bin kernel leads).
+static bool use_whole_bin(const fxc_pairplan* plan, int nkb) {
   return plan->tensor && whole_bin_plan(plan->tensor) &&
-         plan->npairs * (int64_t)sizeof(float2) <= (int64_t)kBinStages * kBinStageBytes && !getenv("FXC_GEMM_TILED");
+         plan->npairs * (int64_t)sizeof(float2) <= (int64_t)kBinStages * kBinStageBytes &&
+         (nkb > 3 || plan->tensor->nchan > kTcM) && !getenv("FXC_GEMM_TILED");
 }
 
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {
@@ -964,7 +975,7 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
                                    ctx->stream));
     return FXC_OK;
   }
-  if (xc_gemm_accumulate_is_cheap(plan)) {
+  if (use_whole_bin(plan, nkb)) {
     // bin-major rows in context scratch, then transposed into the stack
     float2* binmajor = nullptr;
     int64_t bin_pitch = 0;

@@ -123,7 +123,7 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     from fastxc_gb300.core import PairPlan
 
     rng = np.random.default_rng(17)
-    nwin, nspec = 40, 257
+    nwin, nspec = 130, 257  # more than three 32-window K-blocks: whole-bin below 129 channels too
     spec = make_spec(rng, nwin, nchan, nspec)
     iu, ju = np.triu_indices(nchan)
     keep = rng.random(iu.size) < 0.3
@@ -376,7 +376,7 @@ def test_kernel_timing_counts_contraction_launches(ctx, torch_cuda):
     from fastxc_gb300.core import PairPlan
 
     rng = np.random.default_rng(8)
-    nwin, nchan, nspec = 40, 24, 301
+    nwin, nchan, nspec = 130, 24, 301  # more than three K-blocks: the whole-bin kernel
     spec = make_spec(rng, nwin, nchan, nspec)
     src, rec = station_pairs(8)
     plan = PairPlan(ctx, src, rec, nchan)
