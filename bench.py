@@ -711,9 +711,21 @@ def main():
         for _ in range(e2e_steps):
             ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
         el = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, device=dev)
+        # the floor: the same spectra copied over the host link in the
+        # pipeline's 64-window chunks, back to back, with nothing else running
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        with torch.cuda.stream(stream):
+            for w0 in range(0, nwin, 64):
+                spec[w0:w0 + 64].copy_(host_spec[w0:w0 + 64], non_blocking=True)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        copy_ms = c0.elapsed_time(c1)
         line["e2e"] = {"value": replicas.whole_job_rate(pw, world, el), "unit": "pair-windows/s",
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
-                       "ms_per_step": el * 1e3, "steps": e2e_steps}
+                       "ms_per_step": el * 1e3, "steps": e2e_steps,
+                       "h2d_copy_ms": copy_ms, "h2d_gbs": spec.numel() * 8 / (copy_ms / 1e3) / 1e9}
 
     # the step's buffers are released before the stage timings and the
     # serving stream (which uses its own HBM arenas)

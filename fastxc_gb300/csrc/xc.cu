@@ -581,22 +581,6 @@ int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
 
 int64_t xc_stack_pitch(int nspec) { return (int64_t)((nspec + 3) / 4) * 4; }
 
-// dst[i] += src[i] over n complex values, two per thread step (n even: the
-// stack pitch is a multiple of 4 bins)
-__global__ void __launch_bounds__(256) k_xc_stack_add(float4* __restrict__ dst, const float4* __restrict__ src,
-                                                      int64_t n4) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-    const float4 a = __ldcs(src + i);
-    float4 b = dst[i];
-    b.x += a.x;
-    b.y += a.y;
-    b.z += a.z;
-    b.w += a.w;
-    dst[i] = b;
-  }
-}
-
 // dst[dst_rows[r]][c] (+)= src[src_rows[r]][c] for c < ncols float2 columns:
 // folds one day's stack rows into the cross-day stack rows of their
 // (path, component) groups
@@ -619,18 +603,6 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
-}
-
-int xc_stack_add_launch(fxc_ctx* ctx, float2* dst, const float2* src, int64_t n) {
-  if (n <= 0) return FXC_OK;
-  FXC_CHECK_ARG(n % 2 == 0, "stack add length %lld is odd", (long long)n);
-  const int64_t n4 = n / 2;
-  const int64_t blocks = std::min<int64_t>((n4 + 255) / 256, (int64_t)ctx->num_sms * 8);
-  k_xc_stack_add<<<(unsigned)blocks, 256, 0, ctx->stream>>>(reinterpret_cast<float4*>(dst),
-                                                            reinterpret_cast<const float4*>(src), n4);
-  count_launch();
-  FXC_LAUNCH_CHECK();
-  return FXC_OK;
 }
 
 }  // namespace fxc
@@ -838,9 +810,6 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   const int kRing = 3;
   const int64_t nchunks = (nwin + wchunk - 1) / wchunk;
   const bool tensor = method == FXC_XC_TENSOR;
-  // a contraction whose accumulate is cheap runs per chunk; otherwise per
-  // group of chunks, to spread the partial-stack add
-  const int64_t kGroupChunks = tensor && xc_gemm_accumulate_is_cheap(plan) ? 1 : 4;
   const size_t row_bytes = sizeof(float2) * (size_t)nchan * (size_t)spec_pitch;  // one window
   const size_t chunk_bytes = row_bytes * (size_t)wchunk;
   const size_t mask_bytes = h_mask ? (size_t)nwin * (size_t)nchan : 0;
@@ -850,28 +819,16 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t off_mask = al(chunk_bytes) * kRing;
   const size_t off_ncf = off_mask + al(mask_bytes);
-  const size_t off_part = off_ncf + al(ncf_bytes);
-  const bool use_partial = tensor && nchunks > 1 && !xc_gemm_accumulate_is_cheap(plan);
-  FXC_TRY(ctx->scratch2.reserve(off_part + (use_partial ? stack_bytes : 0)));
+  FXC_TRY(ctx->scratch2.reserve(off_ncf + al(ncf_bytes)));
   char* base = reinterpret_cast<char*>(ctx->scratch2.ptr);
   FXC_TRY(ctx->scratch.reserve(stack_bytes));
   float2* stack = reinterpret_cast<float2*>(ctx->scratch.ptr);
-  float2* partial = reinterpret_cast<float2*>(base + off_part);
-  // tensor groups: chunk c closes a group when it is the last or the
-  // next-to-last chunk, or the kGroupChunks-th of its group
-  std::vector<int64_t> group_first((size_t)std::max<int64_t>(nchunks, 1), 0);
   uint4* packed = nullptr;
   if (tensor) {
     FXC_CHECK_ARG(plan->tensor != nullptr, "pair plan has no tensor tiles");
-    int64_t first = 0, most = 0;
-    for (int64_t c = 0; c < nchunks; ++c) {
-      group_first[(size_t)c] = first;
-      if (c >= nchunks - 2 || c + 1 - first == kGroupChunks) {
-        most = std::max(most, std::min(nwin, (c + 1) * wchunk) - first * wchunk);
-        first = c + 1;
-      }
-    }
-    const int64_t chunks = xc_packed_chunks(nchan, most, nspec);  // the largest group's operands
+    // one chunk's operands: every chunk is packed and contracted on its own,
+    // the contraction accumulating into the stack through its transpose
+    const int64_t chunks = xc_packed_chunks(nchan, std::min(nwin, wchunk), nspec);
     if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
     packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
   }
@@ -922,28 +879,12 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
                            scale, stack, pitch, FXC_XC_PLAIN, 1);
       cuda_ok(cudaEventRecord(used[r], ctx->stream));
     } else if (tensor) {
-      // pack into the group's operand layout; the slot is free again once
-      // packed (the GEMM reads the packed copy)
-      const int64_t g0 = group_first[(size_t)c];
-      const bool closes = c == nchunks - 1 || group_first[(size_t)c + 1] == c + 1;
-      const int64_t gw0 = g0 * wchunk;
-      int64_t glast = c;  // the group's last chunk
-      while (glast < nchunks - 1 && group_first[(size_t)glast + 1] == g0) ++glast;
-      const int64_t gnw = std::min(nwin, (glast + 1) * wchunk) - gw0;
-      const int kb0 = (int)((w0 - gw0) / kTcKbWindows);
-      const int kb1 = (int)((w0 - gw0 + nw + kTcKbWindows - 1) / kTcKbWindows);
-      rc = xc_pack_launch(ctx, spec, gnw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)gw0 * nchan : nullptr,
-                          packed, kb0, kb1, w0 - gw0);
+      // pack the chunk (the slot is free again once packed: the GEMM reads
+      // the packed copy), then contract it into the stack
+      rc = xc_pack_launch(ctx, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,
+                          packed);
       cuda_ok(cudaEventRecord(used[r], ctx->stream));
-      if (rc == FXC_OK && closes) {
-        const bool first_group = g0 == 0;
-        if (first_group || !use_partial) {
-          rc = xc_gemm_launch(ctx, plan, packed, gnw, nspec, scale, stack, pitch, first_group ? 0 : 1);
-        } else {
-          rc = xc_gemm_launch(ctx, plan, packed, gnw, nspec, scale, partial, pitch);
-          if (rc == FXC_OK) rc = xc_stack_add_launch(ctx, stack, partial, plan->npairs * pitch);
-        }
-      }
+      if (rc == FXC_OK) rc = xc_gemm_launch(ctx, plan, packed, nw, nspec, scale, stack, pitch, c > 0 ? 1 : 0);
     } else {
       rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,
                            scale, stack, pitch, FXC_XC_PLAIN, c > 0);

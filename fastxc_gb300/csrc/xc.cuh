@@ -60,12 +60,6 @@ int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, in
 int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
                    int nspec, float scale, float2* stack, int64_t stack_pitch, int accumulate = 0);
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec);
-// True when xc_gemm_launch(accumulate=1) costs about the same as without it
-// (the whole-bin contraction); otherwise a partial stack plus
-// xc_stack_add_launch is cheaper.
-bool xc_gemm_accumulate_is_cheap(const fxc_pairplan* plan);
-// dst[i] += src[i] for n complex values on the context stream (n even)
-int xc_stack_add_launch(fxc_ctx* ctx, float2* dst, const float2* src, int64_t n);
 int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_t stack_pitch,
                        const fxc_xc_shape* s, float* ncf);
 // Contraction of packed operands + finalize, the stack in context scratch.

@@ -898,12 +898,6 @@ static bool whole_bin_plan(const XcTensorPlan* tp) {
          t[1].b0 == kTcM && t[1].am == C - kTcM && t[1].bn == C - kTcM;
 }
 
-bool xc_gemm_accumulate_is_cheap(const fxc_pairplan* plan) {
-  // both contractions write bin-major rows and accumulate in the coalesced
-  // transpose into the stack
-  return plan->tensor != nullptr;
-}
-
 // The whole-bin kernel (one CTA per bin, C <= 192) unless the contraction
 // is short (at most three K-blocks) over at most 128 channels: then the
 // persistent tiled kernel, which pays the per-CTA setup once per SM rather

@@ -243,9 +243,10 @@ int fxc_xc_run(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, int6
 /* Host-buffer variant of fxc_xc_run: copies h_spec ([nwin][nchan][spec_pitch]
  * complex) to the device, runs, copies the NCFs back to h_ncf
  * ([npairs][cc_size]) and synchronises. The windows travel in 64-window
- * chunks that are stacked as they land (FXC_XC_TENSOR: in groups of up to
- * four chunks, each group's partial stack added to the running one), so the
- * FP32 summation order differs from fxc_xc_run's at the chunk boundaries. */
+ * chunks that are stacked as they land (FXC_XC_TENSOR: each chunk packed and
+ * contracted, accumulated into the stack through the bin-major transpose),
+ * so the FP32 summation order differs from fxc_xc_run's at the chunk
+ * boundaries. */
 int fxc_xc_run_host(fxc_ctx *ctx, const fxc_pairplan *plan, const float *h_spec, int64_t nwin,
                     int32_t nchan, int64_t spec_pitch, const uint8_t *h_mask, float scale,
                     const fxc_xc_shape *shape, float *h_ncf, int method);
