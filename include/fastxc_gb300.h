@@ -93,7 +93,7 @@ int fxc_host_alloc(size_t bytes, void **out);
 int fxc_host_free(void *ptr);
 int fxc_memcpy(fxc_ctx *ctx, void *dst, const void *src, size_t bytes, int kind);
 
-/* ---- FFT (replaces every cuFFT plan of the reference, SURVEY table 2.4) --- */
+/* ---- FFT (replaces every cuFFT plan of the reference's hot path) --------- */
 
 /* Batched complex transform of length n, unnormalised (cuFFT convention:
  * forward exp(-2 pi i jk/n), inverse exp(+2 pi i jk/n)). Row r of the input

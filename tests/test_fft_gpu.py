@@ -1,6 +1,7 @@
 """The library's own FFT against numpy (FP64) for every length the hot path uses.
 
-Lengths (SURVEY 2.4 of the reference's cuFFT call sites): segment 36000,
+Lengths (those of the reference's cuFFT plans in sac2spec, xc and the
+stacking stages): segment 36000,
 filter 36288, output 37044 / 36750 / 38400, the half-lengths 18000, 18144,
 18522, NCF lengths 2001 (3*23*29) and 1001 (7*11*13), plus small edge cases.
 Tolerance: FP32 transforms, relative L2 error <= 2e-6 against FP64.

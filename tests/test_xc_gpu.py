@@ -1,7 +1,7 @@
 """xc_fast parity: library correlation + stack + finalize against the FP64 oracle.
 
 Tolerance: every NCF within relative L2 1e-5 of the FP64 restatement (the
-spec bound); the stacked spectra within 2e-6.
+bound the tensor path is held to); the stacked spectra within 2e-6.
 """
 
 import numpy as np
