@@ -247,7 +247,7 @@ def _timed(torch, stream, fn, reps=3, warm=1):
 
 
 def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack_pairs: int = 2304,
-               batch_block: int = 0) -> dict:
+               batch_block: int = 0, method_arg: str = "auto") -> dict:
     """The other stages of the path on their own configurations, timed with
     CUDA events on the launching stream (inputs resident, larger than L2):
       sac2spec: one day of 64 stations x 3 components at 10 Hz (192 rows x
@@ -326,7 +326,7 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack
                         "workload": f"{tp} pairs x {ntr} traces -> {ng} groups of 10, {n} lags, 0.05-5 Hz band"}
         del t, lin, d_g, d_w, d_l, o
         torch.cuda.empty_cache()
-        out["batching"] = batching_run(torch, dev, ctx, stream, batch_block)
+        out["batching"] = batching_run(torch, dev, ctx, stream, batch_block, method_arg)
         out["plain_small"] = small_run(torch, dev, ctx)
     finally:
         ctx.close()
@@ -363,15 +363,16 @@ def small_run(torch, dev, ctx) -> dict:
                                           f"{src.size} pairs, host buffers in and out (median of 5)"}
 
 
-def batching_run(torch, dev, ctx, stream, block: int = 0) -> dict:
+def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "auto") -> dict:
     """One day of the batching configuration: 500 stations x 3 components at
     seeded positions in a 400 x 400 km square, component pairs of the station
     pairs within 150 km, 24 one-hour windows, each station covering a
     contiguous run of U(10%, 100%) of the day's windows at a random offset
     (the rest masked). The pairs run in blocks of `block` pairs (0: all of
     them, a 51 GB stack resident); the method is autotuned on the first
-    block."""
-    from fastxc_gb300._lib import FXC_XC_TENSOR
+    block, unless method_arg names it (a profiler's per-launch overhead
+    would otherwise steer the autotuner)."""
+    from fastxc_gb300._lib import FXC_XC_PLAIN, FXC_XC_TENSOR
     from fastxc_gb300.core import Context, PairPlan, xc_shape
 
     rng = np.random.default_rng(4)
@@ -399,6 +400,8 @@ def batching_run(torch, dev, ctx, stream, block: int = 0) -> dict:
     pitch = (nspec + 3) // 4 * 4
     plans = [PairPlan(ctx, src[i:i + blk], rec[i:i + blk], nchan) for i in range(0, npairs, blk)]
     method, ms_plain, ms_tensor = ctx.xc_autotune(plans[0], spec, nstep, nchan, nspec, nspec)
+    if method_arg != "auto":
+        method = FXC_XC_TENSOR if method_arg == "tensor" else FXC_XC_PLAIN
     packed = None
     if method == FXC_XC_TENSOR:
         packed = torch.empty((Context.xc_packed_bytes(nchan, nstep, nspec) // 16, 4), dtype=torch.int32, device=dev)
@@ -738,7 +741,7 @@ def main():
     if not args.no_stages and world == 1:
         line["stages"] = stages_run(torch, dev, local, peaks.get("hbm_gbs", 6800.0),
                                     152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12,
-                                    args.stack_pairs, args.batch_block)
+                                    args.stack_pairs, args.batch_block, args.method)
     if args.serve_seconds > 0:
         # serving: a Poisson stream of correlation jobs against the engine
         line["serving"] = serving_run(args, local, rank)
