@@ -716,15 +716,18 @@ def main():
         el = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, device=dev)
         # the floor: the same spectra copied over the host link in the
         # pipeline's 64-window chunks, back to back, with nothing else running
-        c0 = torch.cuda.Event(enable_timing=True)
-        c1 = torch.cuda.Event(enable_timing=True)
-        c0.record(stream)
-        with torch.cuda.stream(stream):
-            for w0 in range(0, nwin, 64):
-                spec[w0:w0 + 64].copy_(host_spec[w0:w0 + 64], non_blocking=True)
-        c1.record(stream)
-        torch.cuda.synchronize()
-        copy_ms = c0.elapsed_time(c1)
+        # (the fastest of three: the host link's rate fluctuates on these boxes)
+        copy_ms = float("inf")
+        for _ in range(3):
+            c0 = torch.cuda.Event(enable_timing=True)
+            c1 = torch.cuda.Event(enable_timing=True)
+            c0.record(stream)
+            with torch.cuda.stream(stream):
+                for w0 in range(0, nwin, 64):
+                    spec[w0:w0 + 64].copy_(host_spec[w0:w0 + 64], non_blocking=True)
+            c1.record(stream)
+            torch.cuda.synchronize()
+            copy_ms = min(copy_ms, c0.elapsed_time(c1))
         line["e2e"] = {"value": replicas.whole_job_rate(pw, world, el), "unit": "pair-windows/s",
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps,
