@@ -43,13 +43,17 @@ __device__ __forceinline__ float2 r2c_post(const float2* Z, const int* __restric
 // so that the unnormalised inverse complex FFT of Z gives
 // z[m] = x[2m] + i x[2m+1] of the unnormalised real inverse. The imaginary
 // parts of the DC and Nyquist bins are ignored (cufftExecC2R / numpy irfft).
-__device__ __forceinline__ float2 c2r_pre_vals(float2 a, float2 b, int k,
-                                               const float2* __restrict__ twn) {
+// c2r_pre_w takes a = X[k], b = X[M-k] and the table value twn[k] as loaded.
+__device__ __forceinline__ float2 c2r_pre_w(float2 a, float2 b, float2 twk) {
   const float2 bc = conjf2(b);
   const float2 e = cadd(a, bc);
   const float2 d = csub(a, bc);
-  const float2 w = conjf2(__ldg(twn + k));
-  return cadd(e, mul_pi(cmul(w, d)));
+  return cadd(e, mul_pi(cmul(conjf2(twk), d)));
+}
+
+__device__ __forceinline__ float2 c2r_pre_vals(float2 a, float2 b, int k,
+                                               const float2* __restrict__ twn) {
+  return c2r_pre_w(a, b, __ldg(twn + k));
 }
 
 __device__ __forceinline__ float2 c2r_pre(const float2* __restrict__ X, int M, int k,

@@ -308,7 +308,32 @@ __global__ void __launch_bounds__(T, 1)
   float2* stw = buf + M;
   fft_twiddles_to_smem<T>(p, stw);
   const float2* X = stack + (int64_t)blockIdx.x * stack_pitch;
-  for (int k = threadIdx.x; k < M; k += T) buf[k] = c2r_pre(X, M, k, twn);
+  // the CTA holds its SM alone (the row fills shared memory), so the loads
+  // of four iterations are issued together rather than one trip at a time
+  constexpr int U = 4;
+  for (int k0 = threadIdx.x; k0 < M; k0 += U * T) {
+    float2 a[U], b[U], w[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = k0 + u * T;
+      if (k < M) {
+        a[u] = X[k];
+        b[u] = X[M - k];
+        w[u] = __ldg(twn + k);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = k0 + u * T;
+      if (k < M) {
+        if (k == 0) {
+          a[u].y = 0.f;
+          b[u].y = 0.f;
+        }
+        buf[k] = c2r_pre_w(a[u], b[u], w[u]);
+      }
+    }
+  }
   __syncthreads();
   fft_dif<T>(buf, p, stw, true);
   float* out = ncf + (int64_t)blockIdx.x * cc_size;
