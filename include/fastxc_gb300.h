@@ -284,7 +284,11 @@ int fxc_xc_rows_accumulate(fxc_ctx *ctx, const float *d_src, int64_t src_rows, i
 /* Cross-timestamp linear stack (_linear_stack_group,
  * fastxc/operators/stacking/linear_stack.py:228-247): out[p] = float(sum of
  * double(trace) / count) over traces [h_offsets[p], h_offsets[p]+h_counts[p])
- * of d_traces ([*][nsamples]). */
+ * of d_traces ([*][nsamples]). Bit-identical to the reference's sequential
+ * FP64 sum: the sum is formed exactly in int64 fixed point where that
+ * provably equals the FP64 sequence, and by the FP64 loop elsewhere (NaN,
+ * infinities, terms too small beside the largest). At most 65535 pairs per
+ * call (FXC_ERR_INVALID above). */
 int fxc_linear_stack(fxc_ctx *ctx, const float *d_traces, const int64_t *h_offsets,
                      const int32_t *h_counts, int32_t npairs, int32_t nsamples, float *d_out);
 
