@@ -132,3 +132,29 @@ def ncf_traces(npairs: int, ntraces: int, nsamples: int = 2001, delta: float = 0
         noise = rng.standard_normal((ntraces, nsamples))
         out[p] = (s[:, None] * sig[None, :] + noise).astype(np.float32)
     return out
+
+
+def station_series(arr: StationArray, npts: int, delta: float, seed: int = 0, band=(0.1, 2.0),
+                   source_amp: float = 3.0) -> np.ndarray:
+    """Time series of the plain configurations: per channel N(0,1) noise plus
+    a shared band-limited coherent source (4th-order zero-phase Butterworth
+    over ``band``, its upper edge held below 0.9 of the Nyquist frequency)
+    arriving at each station after its distance / 3 km/s delay, with a
+    seeded gain per channel. Returns float32 [nchan][npts]."""
+    from scipy.signal import butter, sosfiltfilt
+
+    band = (band[0], min(band[1], 0.45 / delta))
+    rng = np.random.default_rng(seed)
+    shifts = np.round(arr.delay_s / delta).astype(np.int64)
+    lead = int(shifts.max()) + 1
+    sos = butter(4, list(band), "bandpass", fs=1.0 / delta, output="sos")
+    src = sosfiltfilt(sos, rng.standard_normal(npts + lead))
+    gains = rng.uniform(0.5, 1.5, arr.nchan)
+    out = np.empty((arr.nchan, npts), np.float32)
+    for s in range(arr.nsta):
+        start = lead - int(shifts[s])
+        sig = src[start: start + npts]
+        for c in range(arr.ncomp):
+            ch = s * arr.ncomp + c
+            out[ch] = (rng.standard_normal(npts) + source_amp * gains[ch] * sig).astype(np.float32)
+    return out

@@ -1,7 +1,9 @@
 """Generates the golden fixtures in this directory from the reference itself.
 
 Run in a container where the reference tree exists (it is read there, never
-copied):  python tests/golden/make_golden.py
+copied):  python tests/golden/make_golden.py [reference root]
+The reference root is the argument, else $FXC_REFERENCE_ROOT, else the
+default of oracle/build_ref.py.
 
   filter_*.txt          fastxc/operators/filter_design.py:design_filter (the
                         reference's own Python, scipy butter) for the band
@@ -40,8 +42,10 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-REF_ROOT = Path("/root/reference")
 sys.path.insert(0, str(ROOT))
+from oracle.build_ref import reference_root  # noqa: E402
+
+REF_ROOT = reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
 
 FILTER_SETS = [
     ("filter_d0.1_0.1-2.txt", 0.1, "0.1/2"),
@@ -83,7 +87,7 @@ class RefResp(C.Structure):
 def ref_sac2spec_lib():
     from oracle import build_ref
 
-    libs = build_ref.build()
+    libs = build_ref.build(root=REF_ROOT)
     lib = C.CDLL(str(libs["sac2spec"]))
     lib.readButterworthFilters.restype = C.POINTER(RefButterworth)
     lib.readButterworthFilters.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
@@ -147,7 +151,7 @@ def main() -> None:
     # xc scheduler
     from oracle import build_ref
 
-    xlib = C.CDLL(str(build_ref.build()["xc"]))
+    xlib = C.CDLL(str(build_ref.build(root=REF_ROOT)["xc"]))
     xlib.ref_xc_tasks.restype = C.c_int
     cases = []
     rng = np.random.default_rng(0)
