@@ -59,8 +59,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-stages", action="store_true", help="skip the sac2spec / stacking stage timings")
     ap.add_argument("--stack-pairs", type=int, default=2304, help="pairs of the stacking stages; smaller values only for profiling runs")
-    ap.add_argument("--batch-block", type=int, default=0,
-                    help="pairs per block of the batching stage (0: all pairs of the day in one block)")
+    ap.add_argument("--batch-block", type=int, default=0, help="unused; kept for older command lines")
+    ap.add_argument("--batch-days", type=int, default=10, help="days of the batching stage")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -128,6 +128,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def cpu_model() -> str:
+    """CPU model name of the host (lscpu, else /proc/cpuinfo, else the
+    machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.machine()
+
+
 def cpu_baseline(seconds_target=15.0, threads=1):
     """FP64 oracle on a bounded sample: 16 stations (48 channels), whole days
     of 24 windows, all 9 x 120 component pairs; returns pair-windows/s."""
@@ -176,6 +197,7 @@ def run_reference(args):
         if i >= args.warmup:
             per_step.append(v)
     value = statistics.median(per_step)
+    gpu_ref = reference_kernels_gpu()
     line = {
         "impl": "reference",
         "metric": "pair-windows/s",
@@ -192,10 +214,107 @@ def run_reference(args):
         "config": {"workload": "xc linear stack, 64 sta x 3 comp x 30 days (sampled)", "nspec": NSPEC,
                    "pairs": 18144, "windows": NSTEP * NDAYS},
         "cpu_baseline": {"value": value, "unit": "pair-windows/s", "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": "pair-windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if gpu_ref is not None:
+        line["reference_kernels_gpu"] = gpu_ref
     print(json.dumps(line), flush=True)
+
+
+def reference_kernels_gpu() -> dict | None:
+    """The reference's own CUDA kernels (compiled from its sources with its
+    release flags) and cuFFT, in its host order, timed on this GPU with CUDA
+    events, inputs resident: one day of the precision configuration through
+    xc (24 accumulate launches + sign flip + C2R + 1/(N dt)), one day of 64
+    stations through sac2spec, PWS on 256 pairs and TF-PWS on 8 pairs of the
+    stacking configuration. None when no GPU or the kernels are not built."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return None
+        from oracle import ref_gpu
+    except Exception:
+        return None
+    if not ref_gpu.available():
+        return {"unavailable": "reference kernels not built (oracle/build_ref.py needs the reference tree)"}
+    from fastxc_gb300.synthetic import cross_station_pairs, spectra_device, station_array
+    from oracle import sac2spec_oracle as so
+    from oracle import stack_oracle as sto
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {"how": "reference kernel sources compiled by oracle/build_ref.py (-O3 --use_fast_math), cuFFT via torch "
+                  "(each transform's result is copied once into the reference's pitched buffer), host order restated "
+                  "in oracle/ref_gpu.py; CUDA events on the launching stream"}
+    # xc: one day (24 windows) of 64 stations x 3 components, 18 144 pairs
+    arr = station_array(NSTA, seed=0)
+    src, rec = cross_station_pairs(NSTA)
+    spec, _ = spectra_device(torch, NSTEP, arr, NSPEC, DT, seed=0, gap_frac=GAP_FRAC, device=dev)
+    nfft = 2 * (NSPEC - 1)
+    half = int(round(CC_LEN / DT))
+    m = ref_gpu.RefModule.get("xc")
+    d_src = torch.from_numpy(src.astype(np.int64)).to(dev)
+    d_rec = torch.from_numpy(rec.astype(np.int64)).to(dev)
+    stack = torch.zeros((src.size, NSPEC), dtype=torch.complex64, device=dev)
+    sign = torch.zeros(NSPEC, dtype=torch.int32, device=dev)
+    tim = torch.zeros((src.size, nfft), dtype=torch.float32, device=dev)
+    ms = _timed(torch, stream, lambda: ref_gpu.xc_launch(m, spec, d_src, d_rec, stack, sign, tim, NSTEP, arr.nchan,
+                                                         NSPEC, src.size, nfft, float(np.float32(DT)),
+                                                         1.0 / NSTEP), reps=3, warm=1)
+    out["xc_one_day"] = {"ms": ms, "pair_windows_per_s": src.size * NSTEP / (ms / 1e3), "pairs": int(src.size),
+                         "windows": NSTEP, "nspec": NSPEC, "cc_size": 2 * half + 1}
+    del spec, stack, tim
+    torch.cuda.empty_cache()
+    # sac2spec: one day of 64 stations x 3 components, RAM + whiten after
+    op = so.make_plan(86400, 3600, 3600, 100, 0.1, so.read_filter_file(
+        ROOT / "tests" / "golden" / "filter_d0.1_0.1-2.txt"), so.WHITEN_AFTER, so.NORM_RUNABS)
+    rows = 192 * op.nstep
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    x = torch.randn((rows, op.segment_pts), generator=g, device=dev, dtype=torch.float32)
+    resp = torch.from_numpy(op.responses).to(dev)
+    work = torch.empty_like(x)
+
+    def s2s_once():
+        work.copy_(x)
+        ref_gpu.sac2spec_rows_device(work, op, resp, 3)
+
+    ms = _timed(torch, stream, s2s_once, reps=2, warm=1)
+    out["sac2spec_one_day"] = {"ms": ms, "channel_windows_per_s": rows / (ms / 1e3), "rows": rows,
+                               "note": "includes one device copy of the windows (the reference's windowed H2D "
+                                       "lands them in its work buffer)"}
+    del x, work
+    torch.cuda.empty_cache()
+    # PWS (substack 1) on 256 pairs x 720 traces x 2001 lags; TF-PWS on 8 pairs
+    npairs, ntr, n = 256, 720, 2001
+    t = torch.randn((npairs * ntr, n), generator=g, device=dev, dtype=torch.float32)
+    w = torch.full((npairs * ntr,), 1.0 / ntr, dtype=torch.float32, device=dev)
+    lin = t.view(npairs, ntr, n).mean(dim=1)
+    ms = _timed(torch, stream, lambda: ref_gpu.pws_run_device(t, w, [ntr] * npairs, lin), reps=2, warm=1)
+    out["pws"] = {"ms": ms, "traces_per_s": npairs * ntr / (ms / 1e3), "pairs": npairs, "traces": ntr,
+                  "nsamples": n, "power": 1.0}
+    del t, w, lin
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(3)
+    tp = 8
+    pre = [sto.tfpws_prestack(rng.standard_normal((ntr, n)), 10) for _ in range(tp)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for gr, wt, li in pre:
+        ref_gpu.tfpws_run(gr.astype(np.float32), wt.astype(np.float32), li.astype(np.float32), 0.1,
+                          band=(0.05, 5.0, -1.0))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out["tfpws"] = {"ms": ms, "pairs_per_s": tp / (ms / 1e3), "pairs": tp, "groups": len(pre[0][1]),
+                    "wall_s": time.perf_counter() - t0,
+                    "note": "per pair as the reference (one pair per compute call), 64-frequency chunks"}
+    return out
 
 
 def serving_run(args, device: int, rank: int) -> dict:
@@ -233,6 +352,13 @@ def serving_run(args, device: int, rank: int) -> dict:
                         "10% PWS; win 3600 s; synthetic seeded spectra cached in HBM"}
 
 
+def _rel(got, ref) -> float:
+    """Largest per-row relative L2 error."""
+    got = np.asarray(got).reshape(-1, np.asarray(got).shape[-1])
+    ref = np.asarray(ref).reshape(-1, np.asarray(ref).shape[-1])
+    return float((np.linalg.norm(got - ref, axis=1) / np.maximum(np.linalg.norm(ref, axis=1), 1e-30)).max())
+
+
 def _timed(torch, stream, fn, reps=3, warm=1):
     for _ in range(warm):
         fn()
@@ -247,14 +373,16 @@ def _timed(torch, stream, fn, reps=3, warm=1):
 
 
 def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack_pairs: int = 2304,
-               batch_block: int = 0, method_arg: str = "auto") -> dict:
+               batch_block: int = 0, method_arg: str = "auto", batch_days: int = 10) -> dict:
     """The other stages of the path on their own configurations, timed with
     CUDA events on the launching stream (inputs resident, larger than L2):
       sac2spec: one day of 64 stations x 3 components at 10 Hz (192 rows x
         864 000 samples, 24 one-hour windows, RAM + whitening after);
       linear stack / PWS: 256 station pairs x 9 components, 720 NCF
         windows of 2001 lags each (13.3 GB), PWS power 2;
-      TF-PWS: 128 of those pairs, substacks of 10 (72 groups), 0.05-5 Hz."""
+      TF-PWS: all of those pairs, substacks of 10 (72 groups), 0.05-5 Hz;
+    each with its largest relative L2 error against the FP64 oracle on a
+    sample of its inputs."""
     from fastxc_gb300 import sac2spec as s2s
     from fastxc_gb300 import stack
     from fastxc_gb300.core import Context
@@ -281,7 +409,17 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack
                            "workload": f"{rows} rows x {npts} samples, {plan.nstep} windows of {plan.segment_pts}, "
                                        f"nspec {plan.nspec}, RAM + whiten after",
                            "algorithmic_bytes": alg, "hbm_frac": alg / (ms / 1e3) / 1e9 / hbm_gbs,
-                           "note": "algorithmic bytes = window read + spectrum write; FFT-bound, see DESIGN"}
+                           "note": "algorithmic bytes = window read + spectrum write; FFT-bound"}
+        from oracle import sac2spec_oracle as so
+
+        op = so.make_plan(86400, 3600, 3600, 100, 0.1, so.read_filter_file(
+            ROOT / "tests" / "golden" / "filter_d0.1_0.1-2.txt"), so.WHITEN_AFTER, so.NORM_RUNABS)
+        sample_steps = [0, 11]
+        wins = so.windows(series[:3].cpu().numpy().astype(np.float64), op, sample_steps)
+        ref = so.run_rows(wins, op, 3)
+        got = spec[sample_steps][:, :3].cpu().numpy()
+        out["sac2spec"]["rel_l2_vs_fp64"] = _rel(got.reshape(-1, plan.nspec), ref.reshape(-1, plan.nspec))
+        out["sac2spec"]["rel_l2_sample"] = "one station (3 channels) x windows 0 and 11, FP64 oracle"
         del series, spec, resp
         torch.cuda.empty_cache()
         # --- linear stack + PWS (config 3) ----------------------------------
@@ -303,30 +441,38 @@ def stages_run(torch, dev, local: int, hbm_gbs: float, fp32_tflops: float, stack
             res["g"] = d_g
 
         ms = _timed(torch, stream, pws_once, reps=2)
+        lin_pws = lin[:2].cpu().numpy()
         nbytes = t.numel() * 4 * 3 + lin.numel() * 4  # traces read, groups written and read, stack written
         out["pws"] = {"traces_per_s": npairs * ntr / (ms / 1e3), "ms": ms, "power": 2.0,
                       "hbm_gbs_algorithmic": nbytes / (ms / 1e3) / 1e9,
                       "hbm_frac": nbytes / (ms / 1e3) / 1e9 / hbm_gbs,
                       "workload": f"{npairs} pairs x {ntr} traces x {n} lags, substack 1 (prestack + PWS)"}
         res.clear()
-        # --- TF-PWS (subset) ---------------------------------------------------
-        tp = min(128, npairs)
-        d_g, d_w, d_l, goff, gcnt = stack.prestack(ctx, torch, t[: tp * ntr], offs[:tp], cnts[:tp], n, 10,
-                                                   stack.MODE_TFPWS)
-        o = torch.empty((tp, n), dtype=torch.float32, device=dev)
+        # --- TF-PWS: every pair ----------------------------------------------------
+        d_g, d_w, d_l, goff, gcnt = stack.prestack(ctx, torch, t, offs, cnts, n, 10, stack.MODE_TFPWS)
+        o = torch.empty((npairs, n), dtype=torch.float32, device=dev)
         ms = _timed(torch, stream, lambda: stack.tfpws(ctx, d_g, d_w, goff, gcnt, d_l, n, o, 0.1, band=(0.05, 5.0)),
                     reps=1, warm=1)
         ng = int(gcnt[0])
         # S-transform work: (G + 1) inverse transforms of n per (pair, frequency)
-        flops = tp * (ng + 1) * (n // 2 + 1) * 5.0 * n * np.log2(n)
-        out["tfpws"] = {"pairs_per_s": tp / (ms / 1e3), "ms": ms, "groups": ng, "pairs": tp,
+        flops = npairs * (ng + 1) * (n // 2 + 1) * 5.0 * n * np.log2(n)
+        out["tfpws"] = {"pairs_per_s": npairs / (ms / 1e3), "ms": ms, "groups": ng, "pairs": npairs,
                         "fft_flops": flops, "tflops": flops / (ms / 1e3) / 1e12,
                         "fp32_frac": flops / (ms / 1e3) / 1e12 / fp32_tflops,
-                        "extrapolated_2304_pairs_s": 2304 / (tp / (ms / 1e3)),
-                        "workload": f"{tp} pairs x {ntr} traces -> {ng} groups of 10, {n} lags, 0.05-5 Hz band"}
+                        "workload": f"{npairs} pairs x {ntr} traces -> {ng} groups of 10, {n} lags, 0.05-5 Hz band"}
+        # errors against the FP64 oracle on a sample of the stage inputs
+        from oracle import stack_oracle as sto
+
+        th = t[: 2 * ntr].cpu().numpy().reshape(2, ntr, n)
+        e_pws = [_rel(lin_pws[p], sto.pws(th[p], 1, 2.0)) for p in range(2)]
+        e_tf = _rel(o[0].cpu().numpy(), sto.tfpws(th[0], 10, 1.0, band=(0.05, 5.0), delta=0.1))
+        out["pws"]["rel_l2_vs_fp64"] = max(e_pws)
+        out["pws"]["rel_l2_sample"] = "2 pairs x 720 traces, FP64 oracle"
+        out["tfpws"]["rel_l2_vs_fp64"] = e_tf
+        out["tfpws"]["rel_l2_sample"] = "1 pair x 720 traces, FP64 oracle"
         del t, lin, d_g, d_w, d_l, o
         torch.cuda.empty_cache()
-        out["batching"] = batching_run(torch, dev, ctx, stream, batch_block, method_arg)
+        out["batching"] = batching_run(torch, dev, ctx, stream, batch_block, method_arg, batch_days)
         out["plain_small"] = small_run(torch, dev, ctx)
     finally:
         ctx.close()
@@ -363,99 +509,105 @@ def small_run(torch, dev, ctx) -> dict:
                                           f"{src.size} pairs, host buffers in and out (median of 5)"}
 
 
-def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "auto") -> dict:
-    """One day of the batching configuration: 500 stations x 3 components at
-    seeded positions in a 400 x 400 km square, component pairs of the station
-    pairs within 150 km, 24 one-hour windows, each station covering a
-    contiguous run of U(10%, 100%) of the day's windows at a random offset
-    (the rest masked). The pairs run in blocks of `block` pairs (0: all of
-    them, a 51 GB stack resident); the method is autotuned on the first
-    block, unless method_arg names it (a profiler's per-launch overhead
-    would otherwise steer the autotuner)."""
+def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "auto", days: int = 10) -> dict:
+    """The batching configuration: 500 stations x 3 components at seeded
+    positions in a 400 x 400 km square, split at random into a 3600-s and an
+    1800-s window group (the reference runs each group separately: their
+    spectra differ in length); per group the component pairs of its station
+    pairs within 150 km; `days` days, each station-day covering a contiguous
+    run of U(10%, 100%) of the day's windows at a random offset (the rest
+    masked), so window counts per pair are uneven. One step = every day of
+    both groups: per group-day the pack, one persistent contraction launch
+    (or the plain stack) and the finalize. The method is autotuned on each
+    group's first day unless method_arg names it. Rate = covered
+    pair-windows (windows that both stations of a pair hold) / time."""
+    from fastxc_gb300 import sac2spec as s2s
     from fastxc_gb300._lib import FXC_XC_PLAIN, FXC_XC_TENSOR
     from fastxc_gb300.core import Context, PairPlan, xc_shape
 
     rng = np.random.default_rng(4)
-    nsta, nstep, nspec = 500, 24, 18523
-    nchan = 3 * nsta
+    nsta = 500
     pos = rng.uniform(0.0, 400.0, (nsta, 2))
-    dist = np.hypot(pos[:, None, 0] - pos[None, :, 0], pos[:, None, 1] - pos[None, :, 1])
-    si, sj = np.nonzero(np.triu(dist <= 150.0, 1))
-    a, b = np.meshgrid(np.arange(3), np.arange(3), indexing="ij")
-    src = (3 * si[:, None] + a.reshape(1, -1)).reshape(-1).astype(np.int32)
-    rec = (3 * sj[:, None] + b.reshape(1, -1)).reshape(-1).astype(np.int32)
-    npairs = src.size
-    blk = block if block > 0 else npairs
-    cover = rng.uniform(0.1, 1.0, nsta)
-    mask = np.zeros((nstep, nchan), np.uint8)
-    for k in range(nsta):
-        n = max(1, int(round(cover[k] * nstep)))
-        o = int(rng.integers(0, nstep - n + 1))
-        mask[o:o + n, 3 * k:3 * k + 3] = 1
+    in_3600 = rng.random(nsta) < 0.5
+    F = s2s.read_filter_file(ROOT / "tests" / "golden" / "filter_d0.1_0.1-2.txt")
     g = torch.Generator(device=dev)
     g.manual_seed(11)
-    spec = torch.randn((nstep, nchan, nspec), generator=g, device=dev, dtype=torch.complex64)
-    d_mask = torch.from_numpy(mask).to(dev)
-    shape = xc_shape(nspec, nstep, 0.1, 100.0)
-    pitch = (nspec + 3) // 4 * 4
-    plans = [PairPlan(ctx, src[i:i + blk], rec[i:i + blk], nchan) for i in range(0, npairs, blk)]
-    method, ms_plain, ms_tensor = ctx.xc_autotune(plans[0], spec, nstep, nchan, nspec, nspec)
-    if method_arg != "auto":
-        method = FXC_XC_TENSOR if method_arg == "tensor" else FXC_XC_PLAIN
-    packed = None
-    if method == FXC_XC_TENSOR:
-        packed = torch.empty((Context.xc_packed_bytes(nchan, nstep, nspec) // 16, 4), dtype=torch.int32, device=dev)
-    d_stack = torch.empty((min(blk, npairs), pitch), dtype=torch.complex64, device=dev)
-    d_ncf = torch.empty((min(blk, npairs), shape.cc_size), dtype=torch.float32, device=dev)
-    scale = 1.0 / nstep
+    groups = []
+    for win, sel in ((3600, np.nonzero(in_3600)[0]), (1800, np.nonzero(~in_3600)[0])):
+        plan = s2s.plan(86400, win, win, 100, 0.1, F, s2s.WHITEN_AFTER, s2s.NORM_RUNABS)
+        nstep, nspec, n = int(plan.nstep), int(plan.nspec), sel.size
+        nchan = 3 * n
+        p = pos[sel]
+        dist = np.hypot(p[:, None, 0] - p[None, :, 0], p[:, None, 1] - p[None, :, 1])
+        si, sj = np.nonzero(np.triu(dist <= 150.0, 1))
+        a, b = np.meshgrid(np.arange(3), np.arange(3), indexing="ij")
+        src = (3 * si[:, None] + a.reshape(1, -1)).reshape(-1).astype(np.int32)
+        rec = (3 * sj[:, None] + b.reshape(1, -1)).reshape(-1).astype(np.int32)
+        # per station-day coverage: a contiguous run of U(10%, 100%) of the windows
+        cnt = np.maximum(1, np.round(rng.uniform(0.1, 1.0, (days, n)) * nstep).astype(np.int64))
+        off = (rng.random((days, n)) * (nstep - cnt + 1)).astype(np.int64)
+        w = np.arange(nstep)
+        sta_mask = ((w[None, :, None] >= off[:, None, :]) & (w[None, :, None] < (off + cnt)[:, None, :]))
+        mask = np.repeat(sta_mask, 3, axis=2).astype(np.uint8)  # [day][win][chan]
+        lo = np.maximum(off[:, si], off[:, sj])
+        hi = np.minimum(off[:, si] + cnt[:, si], off[:, sj] + cnt[:, sj])
+        covered = int(np.maximum(hi - lo, 0).sum()) * 9
+        spec = torch.randn((days, nstep, nchan, nspec), generator=g, device=dev, dtype=torch.complex64)
+        d_mask = torch.from_numpy(mask).to(dev)
+        shape = xc_shape(nspec, nstep, 0.1, 100.0)
+        pitch = (nspec + 3) // 4 * 4
+        pl = PairPlan(ctx, src, rec, nchan)
+        method, ms_plain, ms_tensor = ctx.xc_autotune(pl, spec[0], nstep, nchan, nspec, nspec)
+        if method_arg != "auto":
+            method = FXC_XC_TENSOR if method_arg == "tensor" else FXC_XC_PLAIN
+        packed = None
+        if method == FXC_XC_TENSOR:
+            packed = torch.empty((Context.xc_packed_bytes(nchan, nstep, nspec) // 16, 4), dtype=torch.int32,
+                                 device=dev)
+        groups.append(dict(win=win, nsta=n, nchan=nchan, nstep=nstep, nspec=nspec, src=src, rec=rec,
+                           station_pairs=int(si.size), covered=covered, spec=spec, mask=d_mask, shape=shape,
+                           pitch=pitch, plan=pl, method=method, autotune_ms={"plain": ms_plain, "tensor": ms_tensor},
+                           packed=packed,
+                           stack=torch.empty((src.size, pitch), dtype=torch.complex64, device=dev),
+                           ncf=torch.empty((src.size, shape.cc_size), dtype=torch.float32, device=dev)))
 
-    def day():
-        if packed is not None:
-            ctx.xc_pack(spec, nstep, nchan, nspec, nspec, d_mask, packed)
-        for i, pl in enumerate(plans):
-            n = min(blk, npairs - i * blk)
-            if packed is not None:
-                ctx.xc_stack_packed(pl, packed, nstep, nspec, scale, d_stack, pitch)
-            else:
-                ctx.xc_stack(pl, spec, nstep, nchan, nspec, nspec, d_mask, scale, d_stack, pitch, method)
-            ctx.xc_finalize(d_stack, n, pitch, shape, d_ncf)
-
-    ms = _timed(torch, stream, day, reps=2, warm=1)
-    # where one day's time goes: the contraction kernels (CUDA events around
-    # each launch) and the whole stack / finalize calls
-    phase = {"pack": 0.0, "stack": 0.0, "finalize": 0.0}
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-
-    def timed(name, fn):
-        ev[0].record(stream)
-        fn()
-        ev[1].record(stream)
-        torch.cuda.synchronize()
-        phase[name] += ev[0].elapsed_time(ev[1])
-
-    ctx.kernel_timing(True)
-    if packed is not None:
-        timed("pack", lambda: ctx.xc_pack(spec, nstep, nchan, nspec, nspec, d_mask, packed))
-    for i, pl in enumerate(plans):
-        n = min(blk, npairs - i * blk)
-        if packed is not None:
-            timed("stack", lambda: ctx.xc_stack_packed(pl, packed, nstep, nspec, scale, d_stack, pitch))
+    def group_day(gr, d):
+        scale = 1.0 / gr["nstep"]
+        sp, mk = gr["spec"][d], gr["mask"][d]
+        if gr["packed"] is not None:
+            ctx.xc_pack(sp, gr["nstep"], gr["nchan"], gr["nspec"], gr["nspec"], mk, gr["packed"])
+            ctx.xc_stack_packed(gr["plan"], gr["packed"], gr["nstep"], gr["nspec"], scale, gr["stack"], gr["pitch"])
         else:
-            timed("stack", lambda: ctx.xc_stack(pl, spec, nstep, nchan, nspec, nspec, d_mask, scale, d_stack,
-                                                pitch, method))
-        timed("finalize", lambda: ctx.xc_finalize(d_stack, n, pitch, shape, d_ncf))
-    gemm = {k: ctx.kernel_time(k)[0] for k in ("k_xc_tc_gemm", "k_xc_tc_gemm_bin")}
-    ctx.kernel_timing(False)
-    covered = int(sum(int(np.minimum(mask[:, s], mask[:, r]).sum()) for s, r in zip(src[::9] , rec[::9]))) * 9
-    out = {"pair_windows_per_s": npairs * nstep / (ms / 1e3), "ms_per_day": ms, "pairs": int(npairs),
-           "station_pairs": int(si.size), "channels": nchan, "windows": nstep, "nspec": nspec,
-           "method": "tensor" if method == FXC_XC_TENSOR else "plain",
-           "autotune_sample_ms": {"plain": ms_plain, "tensor": ms_tensor},
-           "covered_pair_windows": covered,
-           "phase_ms": {**phase, "contraction_kernels": sum(gemm.values())},
-           "workload": "500 sta x 3 comp, pairs within 150 km of a 400 km square, 24 windows of 3600 s, "
-                       f"coverage U(10%,100%) per station-day, blocks of {blk} pairs (stack + finalize)"}
-    del spec, d_mask, packed, d_stack, d_ncf, plans
+            ctx.xc_stack(gr["plan"], sp, gr["nstep"], gr["nchan"], gr["nspec"], gr["nspec"], mk, scale, gr["stack"],
+                         gr["pitch"], gr["method"])
+        ctx.xc_finalize(gr["stack"], gr["src"].size, gr["pitch"], gr["shape"], gr["ncf"])
+
+    def step():
+        for gr in groups:
+            for d in range(days):
+                group_day(gr, d)
+
+    ms = _timed(torch, stream, step, reps=2, warm=1)
+    per_group = []
+    for gr in groups:
+        gms = _timed(torch, stream, lambda: [group_day(gr, d) for d in range(days)], reps=1, warm=0)
+        per_group.append({"win_len_s": gr["win"], "stations": gr["nsta"], "station_pairs": gr["station_pairs"],
+                          "pairs": int(gr["src"].size), "windows_per_day": gr["nstep"], "nspec": gr["nspec"],
+                          "method": "tensor" if gr["method"] == FXC_XC_TENSOR else "plain",
+                          "autotune_sample_ms": gr["autotune_ms"], "ms_per_day": gms / days,
+                          "covered_pair_windows": gr["covered"],
+                          "nominal_pair_windows": int(gr["src"].size) * gr["nstep"] * days})
+    covered = sum(gr["covered"] for gr in groups)
+    nominal = sum(int(gr["src"].size) * gr["nstep"] * days for gr in groups)
+    out = {"pair_windows_per_s": covered / (ms / 1e3), "rate_basis": "covered pair-windows (both stations hold the window)",
+           "nominal_pair_windows_per_s": nominal / (ms / 1e3), "ms_per_step": ms, "days": days,
+           "covered_pair_windows": covered, "nominal_pair_windows": nominal, "groups": per_group,
+           "workload": f"500 sta x 3 comp in a 400 km square, split into 3600-s and 1800-s window groups, pairs "
+                       f"within 150 km per group, {days} days, coverage U(10%,100%) per station-day at a random "
+                       "offset; per group-day: pack + contraction (or plain stack) + finalize"}
+    for gr in groups:
+        gr.clear()
+    del groups
     torch.cuda.empty_cache()
     return out
 
@@ -605,6 +757,18 @@ def main():
                          "stack_ms": kern_ms, "finalize_ms": fin_ms, "launches": launches, "ncf16": ncf_snapshot,
                          "gemm_ms": gemm_ms}
 
+    # one day (the first 24 windows) through fxc_xc_run: the unit the
+    # reference's xc_fast processes per timestamp
+    one_day = {}
+    for name in results:
+        d_ncf1 = torch.empty((npairs, shape.cc_size), dtype=torch.float32, device=dev)
+        one_day[name] = _timed(torch, stream, lambda: ctx.xc_run(plan, spec[:NSTEP], NSTEP, nchan, nspec, None,
+                                                                  1.0 / NSTEP, shape, d_ncf1, methods[name]),
+                               reps=3, warm=1)
+        del d_ncf1
+    one_day_line = {k: {"ms": v, "pair_windows_per_s": npairs * NSTEP / (v / 1e3)} for k, v in one_day.items()}
+    one_day_line["workload"] = f"{npairs} pairs x {NSTEP} windows x nspec {nspec} (one day), fxc_xc_run"
+
     # parity sample: 16 pairs over all windows against the FP64 oracle
     from oracle import xc_oracle as xo
 
@@ -648,14 +812,24 @@ def main():
         # stack stage also holds the bin-major -> [pair][bin] transpose
         kms = hr["gemm_ms"] if hr.get("gemm_ms") else hr["stack_ms"]
         achieved = issued / (kms / 1e3) / 1e12
-        peak = peaks.get("bf16_tflops_sustained", 1700.0)
-        peak_src = ("measured sustained bf16 (cuBLAS, MEASURED_PEAKS.json)" if "bf16_tflops_sustained" in peaks
-                    else "fallback 1.7 PFLOP/s sustained")
+        # the burst peak applies when the sampled SM clock sat at its maximum
+        # with no power cap during the timed region, the sustained one otherwise
+        at_max = bool(clocks and clocks.get("sm_mhz") and clocks.get("sm_max_mhz")
+                      and clocks["sm_mhz"] >= 0.95 * clocks["sm_max_mhz"]
+                      and "sw_power_cap" not in (clocks.get("reasons") or []))
+        if at_max and "bf16_tflops" in peaks:
+            peak, peak_src = peaks["bf16_tflops"], "of measured burst bf16 (cuBLAS; clocks at max, no power cap)"
+        elif "bf16_tflops_sustained" in peaks:
+            peak, peak_src = peaks["bf16_tflops_sustained"], "of measured sustained bf16 (cuBLAS, power-capped clocks)"
+        else:
+            peak, peak_src = 1900.0, "of fallback 1.9 PFLOP/s burst"
+        useful_tf = useful_flop / (kms / 1e3) / 1e12
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                     "traffic": profile_traffic(gemm_kernel, wkey), "peak_source": peak_src, "kernel": gemm_kernel,
                     "algorithmic": "issued MMA flops = nspec x ceil(nwin/32) x 24 x (2 x 128 x 16 x n) summed over tiles "
                                    "(3 bf16 hi/lo products, Re and Im, upper-triangle tiles)",
-                    "useful_tflops": useful_flop / (kms / 1e3) / 1e12, "kernel_ms": kms,
+                    "useful_tflops": useful_tf, "useful_x3_frac": 3.0 * useful_tf / peak,
+                    "issued_over_useful_x3": issued / (3.0 * useful_flop), "kernel_ms": kms,
                     "stack_stage_ms": hr["stack_ms"], "pack_ms": hr["pack_ms"], "finalize_ms": hr["finalize_ms"]}
     else:
         kms = hr["stack_ms"]
@@ -687,9 +861,14 @@ def main():
                    "l2": f"inputs ({spec_bytes / 1e9:.1f} GB) larger than L2 (129 MB), no flush", "parallelism": f"replicas x{world}"},
         "rel_l2_vs_fp64": rel,
         "per_method": {k: {"pair_windows_per_s": pw / (v["ms_per_step"] / 1e3), "ms_per_step": v["ms_per_step"],
-                           "pack_ms": v["pack_ms"], "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"]}
+                           "pack_ms": v["pack_ms"], "stack_ms": v["stack_ms"], "finalize_ms": v["finalize_ms"],
+                           **({"stack_kernel_fp32_frac": useful_flop / (v["stack_ms"] / 1e3) / 1e12 /
+                               (152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12),
+                               "fp32_peak": "nominal FP32 (152 SMs x 128 lanes x 2 x max SM clock)"}
+                              if k == "plain" else {})}
                        for k, v in results.items()},
         "roofline": roofline,
+        "one_day": one_day_line,
         "autotune": autotune,
         "gpu_launches": hr["launches"],
         "clocks": clocks,
@@ -728,10 +907,19 @@ def main():
             c1.record(stream)
             torch.cuda.synchronize()
             copy_ms = min(copy_ms, c0.elapsed_time(c1))
+        # one more call with the phase record on (CUDA events on both streams)
+        ctx.kernel_timing(True)
+        ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
+        phases = ctx.host_phases()
+        ctx.kernel_timing(False)
         line["e2e"] = {"value": replicas.whole_job_rate(pw, world, el), "unit": "pair-windows/s",
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps,
-                       "h2d_copy_ms": copy_ms, "h2d_gbs": spec.numel() * 8 / (copy_ms / 1e3) / 1e9}
+                       "h2d_copy_ms": copy_ms, "h2d_gbs": spec.numel() * 8 / (copy_ms / 1e3) / 1e9,
+                       "over_copy_floor": el * 1e3 / copy_ms, "phase_ms": phases,
+                       "phase_note": "one extra call with CUDA events on the copy and compute streams: copy_busy = "
+                                     "sum of H2D copy durations, compute_busy = sum of per-chunk compute, "
+                                     "tail = time after the last H2D copy ends"}
 
     # the step's buffers are released before the stage timings and the
     # serving stream (which uses its own HBM arenas)
@@ -744,14 +932,16 @@ def main():
     if not args.no_stages and world == 1:
         line["stages"] = stages_run(torch, dev, local, peaks.get("hbm_gbs", 6800.0),
                                     152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12,
-                                    args.stack_pairs, args.batch_block, args.method)
+                                    args.stack_pairs, args.batch_block, args.method, args.batch_days)
     if args.serve_seconds > 0:
         # serving: a Poisson stream of correlation jobs against the engine
         line["serving"] = serving_run(args, local, rank)
 
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, sample = cpu_baseline(seconds_target=12.0, threads=1)
-        line["cpu_baseline"] = {"value": v, "unit": "pair-windows/s", "cores": 1, "kind": "port", "sample": sample}
+        cores = os.cpu_count() or 1
+        v, sample = cpu_baseline(seconds_target=12.0, threads=cores)
+        line["cpu_baseline"] = {"value": v, "unit": "pair-windows/s", "cores": cores, "kind": "port", "sample": sample,
+                                "cpu_model": cpu_model()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -22,6 +22,7 @@ FXC_ERR_NOMEM = -4
 FXC_ERR_IO = -5
 FXC_ERR_NODEVICE = -6
 FXC_ERR_TIMEOUT = -7
+FXC_ERR_NOTFOUND = -8
 
 FXC_XC_PLAIN = 0
 FXC_XC_TENSOR = 1
@@ -64,6 +65,7 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_launch_count_reset": (None, []),
     "fxc_ctx_kernel_timing": (_int, [_vp, _int]),
     "fxc_ctx_kernel_time": (_int, [_vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(_i64)]),
+    "fxc_ctx_host_phases": (_int, [_vp, C.POINTER(C.c_double), _i32]),
     "fxc_ctx_create": (_int, [_int, _vp, C.POINTER(_vp)]),
     "fxc_ctx_destroy": (_int, [_vp]),
     "fxc_ctx_set_stream": (_int, [_vp, _vp]),
@@ -239,4 +241,27 @@ _SIGNATURES.update({
     "fxc_server_fetch": (_int, [_vp, _i64, _vp, _vp]),
     "fxc_server_release": (_int, [_vp, _i64]),
     "fxc_server_stats": (_int, [_vp, C.POINTER(ServerStats)]),
+})
+
+
+class SourcePackTotals(C.Structure):
+    """fxc_sourcepack_totals."""
+
+    _fields_ = [("timestamps", C.c_int64), ("records", C.c_int64), ("sources", C.c_int64),
+                ("bytes_indexed", C.c_int64)]
+
+
+_SIGNATURES.update({
+    "fxc_sourcepack_build": (_int, [C.c_char_p, C.c_char_p, C.c_char_p, _int, C.c_char_p,
+                                    C.POINTER(SourcePackTotals), C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t]),
+    "fxc_sourcepack_async_start": (_int, [C.c_char_p, C.c_char_p, _int, C.c_char_p, C.c_double, C.POINTER(_vp)]),
+    "fxc_sourcepack_async_finish": (_int, [_vp, _int, C.c_char_p, C.POINTER(SourcePackTotals)]),
+})
+
+_SIGNATURES.update({
+    "fxc_xc_host_bytes": (_int, [_i64, _i64, _i32, _i64, C.POINTER(XcShape), _int, _int, C.POINTER(_i64)]),
+    "fxc_plan_xc_pairs": (_int, [_i64, _i64, _i32, _i64, C.POINTER(XcShape), _int, _int, _i64, C.POINTER(_i64),
+                                 C.POINTER(_i64)]),
+    "fxc_stack_batch_bytes": (_int, [_int, _i64, _i32, _i64, _i32, C.POINTER(_i64)]),
+    "fxc_plan_stack_traces": (_int, [_int, _i32, _i32, _i32, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
 })

@@ -7,6 +7,11 @@
 // Output (native/xc/pack_io/pack_writer.cu): <ncf>/xcpack/<ts>.iAAAAAA.jBBBBBB.wWWW.pPPP.{xcpack,tsv},
 // <ts>.done per timestamp, _SUCCESS at the end; exit code 0 / 1.
 //
+// Option of this build: --sourcepack <dir> writes each timestamp's SourcePack
+// index (<dir>/<ts>/{sourcepack_index.tsv,_SUCCESS}, the files the
+// reference's build_sourcepack makes afterwards) as soon as the timestamp's
+// records and .done marker are on disk.
+//
 // Environment: FASTXC_XC_METHOD=plain|tensor (default: autotuned per
 // timestamp shape with fxc_xc_autotune), FASTXC_XC_BLOCK=<files per block>
 // (default: the whole timestamp in one block), FASTXC_LOG_LEVEL.
@@ -27,11 +32,12 @@ static void usage() {
   fprintf(stderr,
           "Usage: xc_fast -I <stepack dir|tsv> -P <allowed_paths.tsv> -O <ncf dir> -C <cc length s>\n"
           "               [-G gpu_ids] [-M gpu_mem_mib] [-J lazy_write_depth]\n"
-          "               [--progress|--progress-file file] [--debug]\n");
+          "               [--progress|--progress-file file] [--sourcepack dir] [--debug]\n");
 }
 
 int main(int argc, char** argv) {
   const char *input = nullptr, *out_dir = nullptr, *paths_file = nullptr, *progress = nullptr;
+  const char* sourcepack_dir = nullptr;
   const char* gpus = "0";
   float cclen = 0.0f;
   if (argc <= 1) {
@@ -59,6 +65,7 @@ int main(int argc, char** argv) {
     else if (!strcmp(o, "-P")) paths_file = need(o);
     else if (!strcmp(o, "-J")) (void)need(o);
     else if (!strcmp(o, "--progress") || !strcmp(o, "--progress-file")) progress = need(o);
+    else if (!strcmp(o, "--sourcepack")) sourcepack_dir = need(o);
     else if (!strcmp(o, "--debug")) {
     } else {
       FXLOG_ERROR("argument_unknown", "option=\"%s\"", o);
@@ -180,6 +187,14 @@ int main(int argc, char** argv) {
     }
     if (failed) break;
     if (write_marker(root + "/" + ti.timestamp + ".done") != 0) {
+      failed = 1;
+      break;
+    }
+    if (sourcepack_dir &&
+        fxc_sourcepack_build(root.c_str(), sourcepack_dir, ti.timestamp.c_str(), 1, nullptr, nullptr, nullptr, 0,
+                             nullptr, 0) != FXC_OK) {
+      FXLOG_ERROR("sourcepack_index_failed", "timestamp=\"%s\" error=\"%s\"", ti.timestamp.c_str(),
+                  fxc_last_error());
       failed = 1;
       break;
     }

@@ -65,6 +65,13 @@ class Context:
         lib().fxc_ctx_kernel_time(self.handle, kernel.encode(), C.byref(ms), C.byref(n))
         return ms.value, n.value
 
+    def host_phases(self) -> dict:
+        """Phases (ms) of the last xc_run_host made while kernel timing was on."""
+        out = (C.c_double * 6)()
+        lib().fxc_ctx_host_phases(self.handle, out, 6)
+        keys = ("total", "copy_busy", "last_copy_end", "compute_busy", "tail_after_last_copy", "finalize_and_d2h")
+        return {k: (v if v >= 0 else None) for k, v in zip(keys, out)}
+
     def close(self) -> None:
         if self._h:
             lib().fxc_ctx_destroy(self._h)

@@ -42,6 +42,10 @@ struct fxc_ctx {
   cudaStream_t copy_stream = nullptr;  // host<->device copies of the host-buffer entry points
   bool ktime_on = false;               // fxc_ctx_kernel_timing
   std::vector<fxc::KernelTimeRec> ktimes;
+  // phases of the last fxc_xc_run_host while kernel timing is on (ms):
+  // total, copy-stream busy, last H2D copy end, compute busy, tail after the
+  // last H2D copy, finalize + D2H; -1 when not measured
+  double host_phase_ms[6] = {-1, -1, -1, -1, -1, -1};
 };
 
 namespace fxc {

@@ -807,6 +807,13 @@ int fxc_xc_rows_accumulate(fxc_ctx* ctx, const float* d_src, int64_t src_rows, i
   return FXC_OK;
 }
 
+int fxc_ctx_host_phases(fxc_ctx* ctx, double* out_ms, int32_t n) {
+  clear_error();
+  FXC_CHECK_ARG(ctx != nullptr && out_ms != nullptr && n >= 0, "null context or output");
+  for (int32_t i = 0; i < n; ++i) out_ms[i] = i < 6 ? ctx->host_phase_ms[i] : -1.0;
+  return FXC_OK;
+}
+
 int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec, int64_t nwin,
                     int32_t nchan, int64_t spec_pitch, const uint8_t* h_mask, float scale,
                     const fxc_xc_shape* shape, float* h_ncf, int method) {
@@ -877,6 +884,20 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
   };
   cuda_ok(cudaEventRecord(start_ev, ctx->stream));
   cuda_ok(cudaStreamWaitEvent(cs, start_ev, 0));
+  // phase record (kernel timing on): timing events around every H2D copy
+  // and every chunk's compute, read back once both streams are idle
+  const bool phases = ctx->ktime_on;
+  std::vector<cudaEvent_t> pev;
+  auto mark = [&](cudaStream_t st) -> int {
+    if (!phases) return -1;
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    cudaEventRecord(e, st);
+    pev.push_back(e);
+    return (int)pev.size() - 1;
+  };
+  std::vector<int> copy_b, copy_e, comp_b, comp_e;
+  const int ev_t0 = mark(ctx->stream);
   const uint8_t* d_mask = nullptr;
   if (h_mask) {
     cuda_ok(cudaMemcpyAsync(base + off_mask, h_mask, mask_bytes, cudaMemcpyHostToDevice, cs));
@@ -890,10 +911,13 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
     const int64_t w0 = c * wchunk, nw = std::min(wchunk, nwin - w0);
     char* slot = base + al(chunk_bytes) * r;
     if (c >= kRing) cuda_ok(cudaStreamWaitEvent(cs, used[r], 0));  // slot consumed
+    copy_b.push_back(mark(cs));
     cuda_ok(cudaMemcpyAsync(slot, reinterpret_cast<const char*>(h_spec) + row_bytes * (size_t)w0,
                             row_bytes * (size_t)nw, cudaMemcpyHostToDevice, cs));
+    copy_e.push_back(mark(cs));
     cuda_ok(cudaEventRecord(landed[r], cs));
     cuda_ok(cudaStreamWaitEvent(ctx->stream, landed[r], 0));
+    comp_b.push_back(mark(ctx->stream));
     if (rc != FXC_OK) break;
     const float2* spec = reinterpret_cast<const float2*>(slot);
     // a short last chunk (the remainder of nwin / 64) costs the contraction
@@ -915,7 +939,9 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
                            scale, stack, pitch, FXC_XC_PLAIN, c > 0);
       cuda_ok(cudaEventRecord(used[r], ctx->stream));
     }
+    comp_e.push_back(mark(ctx->stream));
   }
+  const int ev_fin0 = mark(ctx->stream);
   // finalize in pair blocks; each block's NCFs go back on the copy stream
   // while the next block is transformed
   float* d_ncf = reinterpret_cast<float*>(base + off_ncf);
@@ -932,8 +958,30 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
     cuda_ok(cudaMemcpyAsync(h_ncf + off, d_ncf + off, sizeof(float) * (size_t)np * (size_t)shape->cc_size,
                             cudaMemcpyDeviceToHost, cs));
   }
+  const int ev_end_cs = mark(cs);
   cudaStreamSynchronize(cs);
   cudaStreamSynchronize(ctx->stream);
+  if (phases) {
+    for (double& v : ctx->host_phase_ms) v = -1.0;
+    auto ms = [&](int a, int b) -> double {
+      float t = 0.f;
+      if (a < 0 || b < 0 || cudaEventElapsedTime(&t, pev[(size_t)a], pev[(size_t)b]) != cudaSuccess) return -1.0;
+      return (double)t;
+    };
+    double copy_busy = 0.0, comp_busy = 0.0;
+    for (size_t i = 0; i < copy_b.size() && i < copy_e.size(); ++i) copy_busy += std::max(0.0, ms(copy_b[i], copy_e[i]));
+    for (size_t i = 0; i < comp_b.size() && i < comp_e.size(); ++i) comp_busy += std::max(0.0, ms(comp_b[i], comp_e[i]));
+    const double total = ms(ev_t0, ev_end_cs);
+    const double last_copy = copy_e.empty() ? 0.0 : ms(ev_t0, copy_e.back());
+    ctx->host_phase_ms[0] = total;
+    ctx->host_phase_ms[1] = copy_busy;
+    ctx->host_phase_ms[2] = last_copy;
+    ctx->host_phase_ms[3] = comp_busy;
+    ctx->host_phase_ms[4] = total - last_copy;
+    ctx->host_phase_ms[5] = ms(ev_fin0, ev_end_cs);
+    (void)cudaGetLastError();
+  }
+  for (cudaEvent_t e : pev) cudaEventDestroy(e);
   cudaEventDestroy(start_ev);
   for (int r = 0; r < kRing; ++r) {
     cudaEventDestroy(landed[r]);

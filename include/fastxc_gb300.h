@@ -42,6 +42,7 @@ extern "C" {
 #define FXC_ERR_IO (-5)          /* file format or I/O error */
 #define FXC_ERR_NODEVICE (-6)    /* no CUDA device / driver */
 #define FXC_ERR_TIMEOUT (-7)     /* a kernel's bounded device-side wait gave up */
+#define FXC_ERR_NOTFOUND (-8)    /* an input file or folder does not exist */
 
 #define FXC_XC_PLAIN 0  /* FP32 CUDA-core per-pair product, register blocked */
 #define FXC_XC_TENSOR 1 /* BF16 hi/lo split tcgen05 contraction S(f)=Y^H Y */
@@ -69,6 +70,13 @@ void fxc_launch_count_reset(void);
  * forgets them. Disabling drops every pending record. */
 int fxc_ctx_kernel_timing(fxc_ctx *ctx, int enable);
 int fxc_ctx_kernel_time(fxc_ctx *ctx, const char *kernel, double *total_ms, int64_t *launches);
+/* Phases of the last fxc_xc_run_host on this context that ran while kernel
+ * timing was enabled, from CUDA events on its two streams (ms): [0] total,
+ * [1] copy stream busy with host-to-device copies, [2] end of the last
+ * host-to-device copy, [3] compute busy on the chunks, [4] tail after the
+ * last host-to-device copy, [5] finalize + device-to-host copies. Entries
+ * not measured are -1. Writes min(n, 6) values (the rest -1). */
+int fxc_ctx_host_phases(fxc_ctx *ctx, double *out_ms, int32_t n);
 
 /* Create a context bound to `device`. `stream` is a cudaStream_t (NULL = the
  * legacy default stream). The context owns its scratch buffers and FFT
@@ -415,6 +423,68 @@ int fxc_server_fetch(fxc_server *s, int64_t job_id, float *h_ncf, float *h_pws);
 int fxc_server_release(fxc_server *s, int64_t job_id);
 int fxc_server_stats(fxc_server *s, fxc_server_stats_t *out);
 
+/* ---- memory planners (host only, no GPU) ------------------------------------------ */
+
+/* Device bytes one fxc_xc_run_host call over npairs pairs reserves (chunk
+ * ring, mask, NCF staging, stacked spectra, pair tables; on the tensor path
+ * also one chunk's packed operands and the bin-major rows). No counterpart
+ * in the reference, whose own model is native/xc/memory/memory.cu:112-399. */
+int fxc_xc_host_bytes(int64_t npairs, int64_t nwin, int32_t nchan, int64_t spec_pitch, const fxc_xc_shape *shape,
+                      int method, int has_mask, int64_t *bytes);
+/* Largest pair count per fxc_xc_run_host call whose bytes fit budget_bytes
+ * (binary search over fxc_xc_host_bytes): the pair-block sizing of
+ * native/xc/memory/memory.cu:277-399 for this library's buffers.
+ * FXC_ERR_NOMEM when a single pair does not fit. */
+int fxc_plan_xc_pairs(int64_t npairs, int64_t nwin, int32_t nchan, int64_t spec_pitch, const fxc_xc_shape *shape,
+                      int method, int has_mask, int64_t budget_bytes, int64_t *pairs_per_call,
+                      int64_t *bytes_per_call);
+/* Device bytes of one stacking batch of ncf_pws (mode 0) / ncf_tfpws (mode 1):
+ * the executables' trace, group, weight, linear and output buffers plus the
+ * library scratch of fxc_pws_run / fxc_tfpws_run for the batch. */
+int fxc_stack_batch_bytes(int mode, int64_t ntraces, int32_t npairs, int64_t ngroups, int32_t nsamples,
+                          int64_t *bytes);
+/* Largest batch (in traces, whole pairs of traces_per_pair) whose bytes fit
+ * budget_bytes. Replaces select_tfpws_resident_chunk_plan
+ * (native/tfpws/include/tfpws_schedule.hpp:149-217): this library forms
+ * S-transform voices in shared memory, so its footprint depends on the pair
+ * batch, not on a frequency chunk. FXC_ERR_NOMEM when one pair does not fit. */
+int fxc_plan_stack_traces(int mode, int32_t nsamples, int32_t traces_per_pair, int32_t substack,
+                          int64_t budget_bytes, int64_t *max_traces, int64_t *bytes_per_batch);
+
+/* ---- SourcePack index over xcpack output (host only, no GPU) ------------------ */
+
+typedef struct fxc_sourcepack_totals {
+  int64_t timestamps, records, sources, bytes_indexed;
+} fxc_sourcepack_totals;
+typedef struct fxc_sourcepack_async fxc_sourcepack_async;
+
+/* Per-timestamp SourcePack indexes of an xc output (the xcpack folder, or
+ * the folder holding it): <out_dir>/<timestamp>/{sourcepack_index.tsv,
+ * _SUCCESS}. Replaces build_sourcepack (timestamp NULL: every timestamp of
+ * the TSVs, the workspace manifest and the .done markers; out_dir NULL:
+ * <xcpack>/../sourcepack) and build_sourcepack_timestamp (timestamp set:
+ * that timestamp from its own TSVs), fastxc/operators/sourcepack/
+ * builder.py:163-271. sort_within_source orders rows by path id, component
+ * slot, source key, receiver key, input order. progress_file (may be NULL)
+ * receives the two-line progress sidecar. The resolved output folder is
+ * written to out_path and the indexed timestamp folder names, one per line
+ * in index order, to names (each when its capacity is > 0; truncated to
+ * it). FXC_ERR_NOTFOUND for a missing folder or pack file, FXC_ERR_IO for a
+ * malformed TSV. */
+int fxc_sourcepack_build(const char *xc_root, const char *out_dir, const char *timestamp, int sort_within_source,
+                         const char *progress_file, fxc_sourcepack_totals *out, char *out_path,
+                         size_t out_path_cap, char *names, size_t names_cap);
+/* Background indexing of each timestamp as soon as its .done marker
+ * appears, polled every poll_interval_s (>= 0.5 s): replaces
+ * AsyncSourcePackMaterializer (builder.py:27-159). finish stops the poller,
+ * indexes what is left, writes the global _SUCCESS when mark_success (else
+ * removes it and records status_message in the progress sidecar) and frees
+ * the handle. */
+int fxc_sourcepack_async_start(const char *xc_root, const char *out_dir, int sort_within_source,
+                               const char *progress_file, double poll_interval_s, fxc_sourcepack_async **out);
+int fxc_sourcepack_async_finish(fxc_sourcepack_async *a, int mark_success, const char *status_message,
+                                fxc_sourcepack_totals *out);
+
 /* Allocation-free variant of fxc_xc_run. No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc (a host framework that
  * owns all device memory through its own pool, or a job whose device
@@ -423,13 +493,19 @@ int fxc_server_stats(fxc_server *s, fxc_server_stats_t *out);
  * array that every GPU loading the library holds until exit. Takes the pair
  * list on the host (h_src, h_rec as in fxc_pairplan_create) and the same
  * device inputs/outputs as fxc_xc_run; FXC_XC_PLAIN method only.
- * Limit: tiles + tables + npairs * round_up(nspec, 4) * 8 bytes must fit in
- * 64 MiB (about 450 pairs at nspec 18523), else FXC_ERR_INVALID with the
- * sizes in the message. The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress), so make that first call before any
- * stream capture. All calls share the array and it keeps the last call's
- * contents (each call rewrites everything it reads, nothing needs
- * clearing); calls whose work overlaps on the GPU race and must be
+ * Limits: nfft <= 40960 with nfft/2 a product of 2, 4, 8 and odd primes up
+ * to 31 (the one-CTA transform), and tiles + tables + npairs *
+ * round_up(nspec, 4) * 8 bytes within 64 MiB (about 450 pairs at nspec
+ * 18523); else FXC_ERR_INVALID / FXC_ERR_UNSUPPORTED with the sizes in the
+ * message. The pair tiles and FFT tables are built on the host inside the
+ * call and copied into the array on the context's stream.
+ * Set-up: the first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current and keeps it for the rest
+ * of the process; make that first call before any stream capture begins.
+ * A device reset (cudaDeviceReset) invalidates the kept address, so it is
+ * not supported between calls. All calls share the array and it keeps the
+ * last call's contents (each call rewrites everything it reads, nothing
+ * needs clearing); calls whose work overlaps on the GPU race and must be
  * serialised by the caller. */
 int fxc_xc_run_noalloc(fxc_ctx *ctx, const int32_t *h_src, const int32_t *h_rec, int64_t npairs,
                        const float *d_spec, int64_t nwin, int32_t nchan, int64_t spec_pitch,

@@ -115,3 +115,27 @@ def test_xc_fast_command_line_errors(tmp_path, built_lib):
     assert r.returncode == 1 and "required_argument_missing" in r.stderr
     r = subprocess.run([str(EXE), "--bogus"], capture_output=True, text=True)
     assert r.returncode == 1 and "argument_unknown" in r.stderr
+
+
+@pytest.mark.gpu
+def test_xc_fast_emits_sourcepack_index(tmp_path, built_lib, torch_cuda):
+    """xc_fast --sourcepack writes each timestamp's SourcePack index while it
+    runs; the files equal, byte for byte, what the materializer builds
+    afterwards from the same xcpack output."""
+    import os
+
+    from fastxc_gb300 import sourcepack
+
+    make_inputs(tmp_path)
+    out = tmp_path / "ncf"
+    emitted = tmp_path / "sp_emitted"
+    r = subprocess.run([str(EXE), "-I", str(tmp_path / "stepack"), "-P", str(tmp_path / "allowed_paths.tsv"), "-O",
+                        str(out), "-C", "20", "--sourcepack", str(emitted)],
+                       env=dict(os.environ, FASTXC_LOG_LEVEL="warn"), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    built = sourcepack.build_sourcepack(out, tmp_path / "sp_built")
+    assert built.index_paths and built.record_count > 0
+    for idx in built.index_paths:
+        mine = emitted / idx.parent.name
+        assert (mine / "sourcepack_index.tsv").read_bytes() == idx.read_bytes()
+        assert (mine / "_SUCCESS").read_bytes() == (idx.parent / "_SUCCESS").read_bytes()

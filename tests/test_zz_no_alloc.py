@@ -8,6 +8,11 @@ stops at its first failure has already run every other test. It builds its
 own context, so it passes alone in a fresh process as well as after the
 other tests.
 
+Checks: two calls in a row against fxc_xc_run and against the FP64 oracle
+(oracle/xc_oracle.py, the reference's stack + finalize restated); a third
+call with a new transform length and a new pair list leaves the device's
+free memory unchanged (cudaMemGetInfo); oversized requests are refused.
+
 Tolerance: the same NCF bound as the xc parity tests (relative L2 1e-5).
 """
 
@@ -30,6 +35,16 @@ def _pairs(nsta, ncomp=3):
                     src.append(s * ncomp + i)
                     rec.append(t * ncomp + j)
     return np.array(src, np.int32), np.array(rec, np.int32)
+
+
+def _oracle(spec, src, rec, nspec, dt, cc, scale):
+    from oracle import xc_oracle as xo
+
+    return xo.xc_run(spec[:, :, :nspec], src, rec, scale, xo.finalize_shape(nspec, spec.shape[0], dt, cc))
+
+
+def _rel(got, ref):
+    return np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
 
 
 def _run_both(torch, ctx, spec, src, rec, nspec, dt, cc, scale):
@@ -66,9 +81,9 @@ def test_noalloc_matches_allocating_entry_point_twice():
         spec = (rng.standard_normal((nwin, 3 * nsta, nspec)) + 1j * rng.standard_normal((nwin, 3 * nsta, nspec))).astype(np.complex64)
         src, rec = _pairs(nsta)
         got, ref = _run_both(torch, ctx, spec, src, rec, nspec, 0.1, 100.0, 1.0 / nwin)
-        err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
         assert np.all(np.isfinite(got))
-        assert err.max() < NCF_RTOL
+        assert _rel(got, ref).max() < NCF_RTOL
+        assert _rel(got, _oracle(spec, src, rec, nspec, 0.1, 100.0, 1.0 / nwin)).max() < NCF_RTOL
         # call 2 right after, different shape and pair list: the array keeps the
         # previous call's contents and must not leak into this result
         nwin, nsta, nspec = 9, 6, 1001
@@ -76,9 +91,49 @@ def test_noalloc_matches_allocating_entry_point_twice():
         src, rec = _pairs(nsta)
         src, rec = src[::-1].copy(), rec[::-1].copy()
         got, ref = _run_both(torch, ctx, spec, src, rec, nspec, 0.1, 20.0, 1.0 / nwin)
-        err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
         assert np.all(np.isfinite(got))
-        assert err.max() < NCF_RTOL
+        assert _rel(got, ref).max() < NCF_RTOL
+        assert _rel(got, _oracle(spec, src, rec, nspec, 0.1, 20.0, 1.0 / nwin)).max() < NCF_RTOL
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """A call whose transform length and pair list the process has not seen
+    (the case where the allocating path would add FFT tables and scratch)
+    leaves cudaMemGetInfo's free bytes exactly as they were."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fastxc_gb300 import build
+
+    build.build()
+    from fastxc_gb300._lib import lib
+    from fastxc_gb300.core import Context, xc_shape
+
+    with Context(0) as ctx:
+        rng = np.random.default_rng(7)
+
+        def call(nwin, nsta, nspec, cc, reverse):
+            spec = (rng.standard_normal((nwin, 3 * nsta, nspec)) +
+                    1j * rng.standard_normal((nwin, 3 * nsta, nspec))).astype(np.complex64)
+            src, rec = _pairs(nsta)
+            if reverse:
+                src, rec = src[::-1].copy(), rec[::-1].copy()
+            shape = xc_shape(nspec, nwin, 0.1, cc)
+            d_spec = torch.from_numpy(spec).cuda()
+            d_ncf = torch.empty((src.size, shape.cc_size), dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            lib().fxc_xc_run_noalloc(ctx.handle, src.ctypes.data, rec.ctypes.data, src.size, d_spec.data_ptr(),
+                                     nwin, 3 * nsta, nspec, None, 1.0 / nwin, C.byref(shape), d_ncf.data_ptr())
+            ctx.synchronize()
+            free1 = torch.cuda.mem_get_info()[0]
+            got = d_ncf.cpu().numpy()
+            assert _rel(got, _oracle(spec, src, rec, nspec, 0.1, cc, 1.0 / nwin)).max() < NCF_RTOL
+            return free0, free1
+
+        call(5, 3, 1001, 20.0, False)  # warm-up: the set-up lookup and first kernel loads
+        free0, free1 = call(7, 5, 1201, 30.0, True)  # nfft 2400, new pair list
+        assert free0 == free1, (free0, free1)
 
 
 def test_noalloc_rejects_oversized_requests():
