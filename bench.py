@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--batch-block", type=int, default=0, help="unused; kept for older command lines")
     ap.add_argument("--batch-days", type=int, default=10, help="days of the batching stage")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="serving stream length; 0 skips it")
+    ap.add_argument("--profile-case", choices=["sac2spec", "stacking"], default=None,
+                    help="run one small case of a stage (for ncu captures) and exit")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-wait-limit", type=float, default=240.0)
@@ -571,23 +573,38 @@ def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "aut
                            stack=torch.empty((src.size, pitch), dtype=torch.complex64, device=dev),
                            ncf=torch.empty((src.size, shape.cc_size), dtype=torch.float32, device=dev)))
 
-    def group_day(gr, d):
+    def group_day(gr, d, c=ctx):
         scale = 1.0 / gr["nstep"]
         sp, mk = gr["spec"][d], gr["mask"][d]
         if gr["packed"] is not None:
-            ctx.xc_pack(sp, gr["nstep"], gr["nchan"], gr["nspec"], gr["nspec"], mk, gr["packed"])
-            ctx.xc_stack_packed(gr["plan"], gr["packed"], gr["nstep"], gr["nspec"], scale, gr["stack"], gr["pitch"])
+            c.xc_pack(sp, gr["nstep"], gr["nchan"], gr["nspec"], gr["nspec"], mk, gr["packed"])
+            c.xc_stack_packed(gr["plan"], gr["packed"], gr["nstep"], gr["nspec"], scale, gr["stack"], gr["pitch"])
         else:
-            ctx.xc_stack(gr["plan"], sp, gr["nstep"], gr["nchan"], gr["nspec"], gr["nspec"], mk, scale, gr["stack"],
-                         gr["pitch"], gr["method"])
-        ctx.xc_finalize(gr["stack"], gr["src"].size, gr["pitch"], gr["shape"], gr["ncf"])
+            c.xc_stack(gr["plan"], sp, gr["nstep"], gr["nchan"], gr["nspec"], gr["nspec"], mk, scale, gr["stack"],
+                       gr["pitch"], gr["method"])
+        c.xc_finalize(gr["stack"], gr["src"].size, gr["pitch"], gr["shape"], gr["ncf"])
 
-    def step():
+    def step(c=ctx):
         for gr in groups:
             for d in range(days):
-                group_day(gr, d)
+                group_day(gr, d, c)
 
     ms = _timed(torch, stream, step, reps=2, warm=1)
+    # the same step recorded once as a CUDA graph on a stream of its own
+    # (one uncaptured run there sizes that context's scratch) and replayed
+    gstream = torch.cuda.Stream(dev)
+    gctx = Context(dev.index if dev.index is not None else 0, gstream.cuda_stream)
+    graph_ms = None
+    try:
+        step(gctx)
+        gstream.synchronize()
+        gctx.graph_begin()
+        step(gctx)
+        graph = gctx.graph_end()
+        graph_ms = _timed(torch, gstream, graph.launch, reps=2, warm=1)
+        graph.close()
+    finally:
+        gctx.close()
     per_group = []
     for gr in groups:
         gms = _timed(torch, stream, lambda: [group_day(gr, d) for d in range(days)], reps=1, warm=0)
@@ -600,7 +617,8 @@ def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "aut
     covered = sum(gr["covered"] for gr in groups)
     nominal = sum(int(gr["src"].size) * gr["nstep"] * days for gr in groups)
     out = {"pair_windows_per_s": covered / (ms / 1e3), "rate_basis": "covered pair-windows (both stations hold the window)",
-           "nominal_pair_windows_per_s": nominal / (ms / 1e3), "ms_per_step": ms, "days": days,
+           "nominal_pair_windows_per_s": nominal / (ms / 1e3), "ms_per_step": ms, "graph_ms_per_step": graph_ms,
+           "graph_launches_per_step": 3 * days * len(groups), "days": days,
            "covered_pair_windows": covered, "nominal_pair_windows": nominal, "groups": per_group,
            "workload": f"500 sta x 3 comp in a 400 km square, split into 3600-s and 1800-s window groups, pairs "
                        f"within 150 km per group, {days} days, coverage U(10%,100%) per station-day at a random "
@@ -628,8 +646,55 @@ def profile_traffic(kernel: str, workload: str):
     return None
 
 
+def profile_case(name: str) -> None:
+    """Small cases of the non-xc stages for ncu captures: sac2spec on one
+    day of 64 stations x 3 components, 4 windows (768 rows), run twice;
+    stacking: PWS on 64 pairs x 720 traces x 2001 lags (substack 1) and
+    TF-PWS on 8 of them (substacks of 10, 0.05-5 Hz)."""
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from fastxc_gb300 import sac2spec as s2s
+    from fastxc_gb300 import stack
+    from fastxc_gb300.core import Context
+
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    with Context(0) as ctx:
+        if name == "sac2spec":
+            F = s2s.read_filter_file(ROOT / "tests" / "golden" / "filter_d0.1_0.1-2.txt")
+            plan = s2s.plan(86400, 3600, 3600, 100, 0.1, F, s2s.WHITEN_AFTER, s2s.NORM_RUNABS)
+            resp = torch.from_numpy(s2s.filter_response(plan, F)).to(dev)
+            rows, npts = 192, plan.npts
+            series = torch.randn((rows, npts), generator=g, device=dev, dtype=torch.float32)
+            steps = np.arange(4, dtype=np.int32)
+            spec = torch.empty((4, rows, plan.nspec), dtype=torch.complex64, device=dev)
+            for _ in range(2):
+                s2s.run(ctx, plan, series, npts, npts, rows, 3, steps, resp, spec, plan.nspec)
+        else:
+            npairs, ntr, n = 64, 720, 2001
+            t = torch.randn((npairs * ntr, n), generator=g, device=dev, dtype=torch.float32)
+            offs = np.arange(npairs, dtype=np.int64) * ntr
+            cnts = np.full(npairs, ntr, np.int32)
+            out = torch.empty((npairs, n), dtype=torch.float32, device=dev)
+            dg, dw, dl, goff, gcnt = stack.prestack(ctx, torch, t, offs, cnts, n, 1, stack.MODE_PWS)
+            stack.pws(ctx, dg, dw, goff, gcnt, dl, n, out, 2.0)
+            dg, dw, dl, goff, gcnt = stack.prestack(ctx, torch, t[: 8 * ntr], offs[:8], cnts[:8], n, 10,
+                                                    stack.MODE_TFPWS)
+            o = torch.empty((8, n), dtype=torch.float32, device=dev)
+            stack.tfpws(ctx, dg, dw, goff, gcnt, dl, n, o, 0.1, band=(0.05, 5.0))
+        ctx.synchronize()
+    print(f"profile case {name} done")
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -888,10 +953,13 @@ def main():
         m = methods[head]
         ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
         barrier()
-        t0 = time.perf_counter()
         e2e_steps = max(1, min(args.steps, 5))
+        per_call = []
+        t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            c0 = time.perf_counter()
             ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
+            per_call.append((time.perf_counter() - c0) * 1e3)
         el = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, device=dev)
         # the floor: the same spectra copied over the host link in the
         # pipeline's 64-window chunks, back to back, with nothing else running
@@ -916,7 +984,7 @@ def main():
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps,
                        "h2d_copy_ms": copy_ms, "h2d_gbs": spec.numel() * 8 / (copy_ms / 1e3) / 1e9,
-                       "over_copy_floor": el * 1e3 / copy_ms, "phase_ms": phases,
+                       "over_copy_floor": el * 1e3 / copy_ms, "ms_per_call": per_call, "phase_ms": phases,
                        "phase_note": "one extra call with CUDA events on the copy and compute streams: copy_busy = "
                                      "sum of H2D copy durations, compute_busy = sum of per-chunk compute, "
                                      "tail = time after the last H2D copy ends"}

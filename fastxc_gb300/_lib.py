@@ -70,6 +70,10 @@ _SIGNATURES: dict[str, tuple] = {
     "fxc_ctx_destroy": (_int, [_vp]),
     "fxc_ctx_set_stream": (_int, [_vp, _vp]),
     "fxc_ctx_synchronize": (_int, [_vp]),
+    "fxc_graph_begin": (_int, [_vp]),
+    "fxc_graph_end": (_int, [_vp, C.POINTER(_vp)]),
+    "fxc_graph_launch": (_int, [_vp, _vp]),
+    "fxc_graph_destroy": (_int, [_vp]),
     "fxc_device_alloc": (_int, [_vp, C.c_size_t, C.POINTER(_vp)]),
     "fxc_device_free": (_int, [_vp, _vp]),
     "fxc_host_alloc": (_int, [C.c_size_t, C.POINTER(_vp)]),
@@ -262,6 +266,6 @@ _SIGNATURES.update({
     "fxc_xc_host_bytes": (_int, [_i64, _i64, _i32, _i64, C.POINTER(XcShape), _int, _int, C.POINTER(_i64)]),
     "fxc_plan_xc_pairs": (_int, [_i64, _i64, _i32, _i64, C.POINTER(XcShape), _int, _int, _i64, C.POINTER(_i64),
                                  C.POINTER(_i64)]),
-    "fxc_stack_batch_bytes": (_int, [_int, _i64, _i32, _i64, _i32, C.POINTER(_i64)]),
+    "fxc_stack_batch_bytes": (_int, [_int, _i64, _i32, _i64, _i64, _i32, C.POINTER(_i64)]),
     "fxc_plan_stack_traces": (_int, [_int, _i32, _i32, _i32, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
 })

@@ -14,6 +14,7 @@
 // GPU thread works on batch k.
 #pragma once
 
+#include <cuda_runtime.h>
 #include <getopt.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -59,6 +60,8 @@ struct Batch {
   std::vector<Item> items;
   float* h_traces = nullptr;  // page-locked, capacity cap_floats
   size_t cap_floats = 0, ntrace = 0;
+  int64_t ngroups = 0;     // substack groups of the batch (device sizing)
+  int64_t max_groups = 0;  // and the most of one pair
   unsigned nsamples = 0;
   float delta = 0;
   size_t failed_groups = 0;
@@ -157,8 +160,10 @@ inline void tfpws_header(SacHeader* hd, unsigned n, unsigned nseg) {
 
 class Worker {
  public:
-  Worker(Shared* sh, size_t index, int gpu, size_t budget_bytes)
-      : sh_(sh), index_(index), gpu_(gpu), budget_(budget_bytes) {}
+  // budget_bytes: host staging of one batch; device_budget: device bytes one
+  // batch may take (fxc_stack_batch_bytes), 0 = no limit
+  Worker(Shared* sh, size_t index, int gpu, size_t budget_bytes, int64_t device_budget)
+      : sh_(sh), index_(index), gpu_(gpu), budget_(budget_bytes), device_budget_(device_budget) {}
 
   std::vector<std::vector<SourcePackRecord>> groups;  // dealt round-robin, in order
 
@@ -183,6 +188,7 @@ class Worker {
   size_t index_;
   int gpu_;
   size_t budget_;
+  int64_t device_budget_ = 0;
   bool ok_ = true;
   BatchQueue q_;
   std::thread reader_, gpu_thread_;
@@ -209,6 +215,8 @@ class Worker {
   static void reset(Batch* b) {
     b->items.clear();
     b->ntrace = 0;
+    b->ngroups = 0;
+    b->max_groups = 0;
     b->nsamples = 0;
     b->delta = 0;
     b->failed_groups = 0;
@@ -255,9 +263,29 @@ class Worker {
         ++b->failed_groups;
         continue;
       }
+      const int64_t sub = sh_->opt.substack >= 2 ? sh_->opt.substack : 1;
+      const int64_t g_groups = ((int64_t)g.size() + sub - 1) / sub;
+      if (device_budget_ > 0) {
+        int64_t one = 0;
+        fxc_stack_batch_bytes(sh_->opt.tfpws ? 1 : 0, (int64_t)g.size(), 1, g_groups, g_groups, (int32_t)ns, &one);
+        if (one > device_budget_) {
+          FXLOG_ERROR("stack_group_above_memory_budget", "path_id=\"%s\" component_slot=%d traces=%zu samples=%u "
+                      "bytes=%lld budget=%lld", g[0].path_id.c_str(), g[0].component_slot, g.size(), ns,
+                      (long long)one, (long long)device_budget_);
+          ++b->failed_groups;
+          continue;
+        }
+      }
+      auto device_fits = [&]() {
+        if (device_budget_ <= 0) return true;
+        int64_t bytes = 0;
+        fxc_stack_batch_bytes(sh_->opt.tfpws ? 1 : 0, (int64_t)(b->ntrace + g.size()), (int32_t)b->items.size() + 1,
+                              b->ngroups + g_groups, std::max(b->max_groups, g_groups), (int32_t)ns, &bytes);
+        return bytes <= device_budget_;
+      };
       const bool fits = b->items.empty() ||
                         (b->nsamples == ns && b->delta == delta && (b->ntrace * (size_t)ns + need) <= b->cap_floats &&
-                         b->items.size() < 8192);
+                         b->items.size() < 8192 && device_fits());
       if (!fits) {
         q_.push(b);
         b = new_batch();
@@ -274,6 +302,9 @@ class Worker {
         FXLOG_ERROR("stack_group_read_failed", "worker=%zu path_id=\"%s\" component_slot=%d", index_,
                     g[0].path_id.c_str(), g[0].component_slot);
         ++b->failed_groups;
+      } else {
+        b->ngroups += g_groups;
+        b->max_groups = std::max(b->max_groups, g_groups);
       }
     }
     b->last = true;
@@ -424,9 +455,19 @@ inline int run(const Options& opt) {
   std::vector<Worker*> workers;
   for (size_t i = 0; i < gpus.size(); ++i) {
     // host staging per batch (3 batches circulate per worker): a quarter of
-    // the -M cap when given, else 2 GiB
+    // the -M cap when given, else 2 GiB. Device bytes per batch
+    // (fxc_stack_batch_bytes): the -M cap when given, else 0.9 x the GPU's
+    // free memory at start (the reference's resident-chunk budget,
+    // native/tfpws/include/tfpws_schedule.hpp:149-217, over this library's
+    // buffers).
     const size_t budget = mib[i] ? std::max<size_t>(mib[i] << 20, 64u << 20) / 4 : (size_t)2 << 30;
-    workers.push_back(new Worker(&sh, i, gpus[i], budget));
+    int64_t dev_budget = mib[i] ? (int64_t)(mib[i] << 20) : 0;
+    if (!dev_budget) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaSetDevice(gpus[i]) == cudaSuccess && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+        dev_budget = (int64_t)((double)free_b * 0.9);
+    }
+    workers.push_back(new Worker(&sh, i, gpus[i], budget, dev_budget));
   }
   std::vector<SourcePackRecord> g;
   size_t cursor = 0;

@@ -7,6 +7,11 @@
 // Output (native/xc/pack_io/pack_writer.cu): <ncf>/xcpack/<ts>.iAAAAAA.jBBBBBB.wWWW.pPPP.{xcpack,tsv},
 // <ts>.done per timestamp, _SUCCESS at the end; exit code 0 / 1.
 //
+// Memory: each timestamp's pairs run in blocks whose device footprint
+// (fxc_xc_host_bytes) fits the budget: -M MiB when given, else 0.9 x the free
+// device memory at start (the reference's pair-block sizing,
+// native/xc/memory/memory.cu:112-399, over this library's buffers).
+//
 // Option of this build: --sourcepack <dir> writes each timestamp's SourcePack
 // index (<dir>/<ts>/{sourcepack_index.tsv,_SUCCESS}, the files the
 // reference's build_sourcepack makes afterwards) as soon as the timestamp's
@@ -15,9 +20,12 @@
 // Environment: FASTXC_XC_METHOD=plain|tensor (default: autotuned per
 // timestamp shape with fxc_xc_autotune), FASTXC_XC_BLOCK=<files per block>
 // (default: the whole timestamp in one block), FASTXC_LOG_LEVEL.
+#include <cuda_runtime.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include <algorithm>
 
 #include <string>
 #include <vector>
@@ -39,6 +47,7 @@ int main(int argc, char** argv) {
   const char *input = nullptr, *out_dir = nullptr, *paths_file = nullptr, *progress = nullptr;
   const char* sourcepack_dir = nullptr;
   const char* gpus = "0";
+  const char* mem_mib = nullptr;
   float cclen = 0.0f;
   if (argc <= 1) {
     usage();
@@ -61,7 +70,7 @@ int main(int argc, char** argv) {
     else if (!strcmp(o, "-O")) out_dir = need(o);
     else if (!strcmp(o, "-C")) cclen = (float)atof(need(o));
     else if (!strcmp(o, "-G")) gpus = need(o);
-    else if (!strcmp(o, "-M")) (void)need(o);
+    else if (!strcmp(o, "-M")) mem_mib = need(o);
     else if (!strcmp(o, "-P")) paths_file = need(o);
     else if (!strcmp(o, "-J")) (void)need(o);
     else if (!strcmp(o, "--progress") || !strcmp(o, "--progress-file")) progress = need(o);
@@ -96,6 +105,18 @@ int main(int argc, char** argv) {
     FXLOG_ERROR("gpu_context_failed", "gpu=%d error=\"%s\"", device, fxc_last_error());
     return 1;
   }
+  int64_t budget = 0;
+  if (mem_mib && atoll(mem_mib) > 0) {
+    budget = (int64_t)atoll(mem_mib) << 20;
+  } else {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      FXLOG_ERROR("gpu_memory_query_failed", "gpu=%d", device);
+      return 1;
+    }
+    budget = (int64_t)((double)free_b * 0.9);
+  }
+  FXLOG_INFO("xc_memory_budget", "gpu=%d budget_mib=%lld", device, (long long)(budget >> 20));
   Progress prog;
   prog.init(progress, "xc", inputs.size(), "timestamp");
   const std::string root = std::string(out_dir) + "/xcpack";
@@ -146,18 +167,36 @@ int main(int argc, char** argv) {
       int method = -1;  // autotuned unless FASTXC_XC_METHOD names one
       if (menv && !strcmp(menv, "plain")) method = FXC_XC_PLAIN;
       if (menv && !strcmp(menv, "tensor")) method = FXC_XC_TENSOR;
+      const int64_t npairs = (int64_t)src.size();
       fxc_pairplan* plan = nullptr;
-      int rc = fxc_pairplan_create(ctx, src.data(), rec.data(), (int64_t)src.size(), (int32_t)nch, &plan);
-      if (rc == FXC_OK && method < 0) rc = autotune_host(ctx, plan, payload, nstep, (int32_t)nch, nspec, &method);
-      if (rc != FXC_OK ||
-          fxc_xc_run_host(ctx, plan, payload.data(), nstep, (int32_t)nch, nspec, nullptr,
-                          1.0f / (float)nstep, &shape, ncf.data(), method) != FXC_OK) {
-        FXLOG_ERROR("xc_gpu_failed", "timestamp=\"%s\" error=\"%s\"", ti.timestamp.c_str(), fxc_last_error());
+      int rc = FXC_OK;
+      if (method < 0) {
+        // the autotuner samples a few bins of every pair: its plan is the whole list
+        rc = fxc_pairplan_create(ctx, src.data(), rec.data(), npairs, (int32_t)nch, &plan);
+        if (rc == FXC_OK) rc = autotune_host(ctx, plan, payload, nstep, (int32_t)nch, nspec, &method);
         fxc_pairplan_destroy(plan);
+        plan = nullptr;
+      }
+      int64_t block = npairs;
+      if (rc == FXC_OK)
+        rc = fxc_plan_xc_pairs(npairs, nstep, (int32_t)nch, nspec, &shape, method, 0, budget, &block, nullptr);
+      if (rc == FXC_OK && block < npairs)
+        FXLOG_INFO("xc_pair_blocks", "timestamp=\"%s\" pairs=%lld per_block=%lld", ti.timestamp.c_str(),
+                   (long long)npairs, (long long)block);
+      for (int64_t p0 = 0; rc == FXC_OK && p0 < npairs; p0 += block) {
+        const int64_t np = std::min(block, npairs - p0);
+        rc = fxc_pairplan_create(ctx, src.data() + p0, rec.data() + p0, np, (int32_t)nch, &plan);
+        if (rc == FXC_OK)
+          rc = fxc_xc_run_host(ctx, plan, payload.data(), nstep, (int32_t)nch, nspec, nullptr, 1.0f / (float)nstep,
+                               &shape, ncf.data() + (size_t)p0 * shape.cc_size, method);
+        fxc_pairplan_destroy(plan);
+        plan = nullptr;
+      }
+      if (rc != FXC_OK) {
+        FXLOG_ERROR("xc_gpu_failed", "timestamp=\"%s\" error=\"%s\"", ti.timestamp.c_str(), fxc_last_error());
         failed = 1;
         break;
       }
-      fxc_pairplan_destroy(plan);
     }
     TimeInfo tinfo;
     const bool have_time = parse_timestamp(ti.timestamp, &tinfo);

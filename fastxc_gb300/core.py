@@ -65,6 +65,15 @@ class Context:
         lib().fxc_ctx_kernel_time(self.handle, kernel.encode(), C.byref(ms), C.byref(n))
         return ms.value, n.value
 
+    def graph_begin(self) -> None:
+        """Start recording this context's calls into a CUDA graph."""
+        lib().fxc_graph_begin(self.handle)
+
+    def graph_end(self) -> "Graph":
+        h = C.c_void_p()
+        lib().fxc_graph_end(self.handle, C.byref(h))
+        return Graph(self, h)
+
     def host_phases(self) -> dict:
         """Phases (ms) of the last xc_run_host made while kernel timing was on."""
         out = (C.c_double * 6)()
@@ -193,3 +202,25 @@ def xc_shape(nspec: int, nstep: int, dt: float, cc_length: float) -> XcShape:
     s = XcShape()
     lib().fxc_xc_shape_init(nspec, nstep, dt, cc_length, C.byref(s))
     return s
+
+
+class Graph:
+    """A recorded launch sequence of one context (fxc_graph_*)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def launch(self) -> None:
+        lib().fxc_graph_launch(self.ctx.handle, self.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().fxc_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -212,6 +212,69 @@ int fxc_ctx_synchronize(fxc_ctx* ctx) {
   return ctx_check_device_error(ctx);
 }
 
+// ---- CUDA-graph capture of a launch sequence --------------------------------
+
+struct fxc_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+};
+
+int fxc_graph_begin(fxc_ctx* ctx) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(ctx->stream != nullptr, "graph capture needs a context on a non-default stream");
+  FXC_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  return FXC_OK;
+}
+
+int fxc_graph_end(fxc_ctx* ctx, fxc_graph** out) {
+  clear_error();
+  FXC_CHECK_ARG(out != nullptr, "null output");
+  *out = nullptr;
+  FXC_TRY(ctx_enter(ctx));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (e != cudaSuccess || g == nullptr) {
+    (void)cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    set_error("graph capture failed (a captured call synchronised or allocated?): %s", cudaGetErrorString(e));
+    return FXC_ERR_CUDA;
+  }
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    cudaGraphDestroy(g);
+    set_error("graph instantiation failed: %s", cudaGetErrorString(e));
+    return FXC_ERR_CUDA;
+  }
+  fxc_graph* r = new fxc_graph();
+  r->graph = g;
+  r->exec = x;
+  r->device = ctx->device;
+  *out = r;
+  return FXC_OK;
+}
+
+int fxc_graph_launch(fxc_ctx* ctx, const fxc_graph* g) {
+  clear_error();
+  FXC_TRY(ctx_enter(ctx));
+  FXC_CHECK_ARG(g != nullptr && g->exec != nullptr, "null graph");
+  FXC_CHECK_ARG(g->device == ctx->device, "graph captured on device %d, context on %d", g->device, ctx->device);
+  FXC_CUDA_TRY(cudaGraphLaunch(g->exec, ctx->stream));
+  return FXC_OK;
+}
+
+int fxc_graph_destroy(fxc_graph* g) {
+  if (!g) return FXC_OK;
+  cudaSetDevice(g->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return FXC_OK;
+}
+
 int fxc_device_alloc(fxc_ctx* ctx, size_t bytes, void** out) {
   clear_error();
   FXC_CHECK_ARG(out != nullptr, "out is null");

@@ -10,8 +10,11 @@ namespace fxc {
 constexpr int kFftSmallT = 256;
 constexpr int kFftSmallNmax = 4096;
 // Long rows (the 36 000 .. 38 400-point real transforms of sac2spec / xc):
-// one 1024-thread CTA per SM holding the complex half-length row.
-constexpr int kFftLargeT = 1024;
+// one CTA per SM holding the complex half-length row.
+#ifndef FXC_FFT_LARGE_THREADS
+#define FXC_FFT_LARGE_THREADS 1024
+#endif
+constexpr int kFftLargeT = FXC_FFT_LARGE_THREADS;
 constexpr int kFftLargeNmax = 20480;
 
 template <typename K>

@@ -16,11 +16,26 @@ namespace fxc {
 
 static const int kOddRadices[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
 
+// Largest composite radix for lengths above kFftSmallNmax, whose kernels run
+// one 1024-thread CTA per SM (64 registers a thread): the register-resident
+// butterflies of radix 12, 14, 15 and 21 spill there, so those lengths take
+// one more pass over shared memory instead.
+#ifndef FXC_FFT_LARGE_MAX_COMPOSITE
+#define FXC_FFT_LARGE_MAX_COMPOSITE 21
+#endif
+constexpr int kSmallMaxComposite = 21;
+constexpr int kFftSmallNmaxPlan = 4096;  // kFftSmallNmax of fft_launch.cuh
+
+static int max_composite_for(int n) {
+  return n > kFftSmallNmaxPlan ? FXC_FFT_LARGE_MAX_COMPOSITE : kSmallMaxComposite;
+}
+
 // Stages of an n-point transform: radix-8 stages for the powers of two, the
 // leftover 2 or 4 folded with an odd prime into a composite radix (14, 10,
 // 6 or 12), 3s folded with 5s (15), with 7s (21) or with each other (9),
-// then the remaining primes. Fewer stages mean fewer passes over shared memory and
-// fewer barriers; every radix stays small enough for one thread's registers.
+// then the remaining primes; composites above max_composite_for(n) are not
+// formed. Fewer stages mean fewer passes over shared memory and fewer
+// barriers, as long as every radix fits one thread's registers.
 static bool factorize(int n, std::vector<int>* out, bool composites = true) {
   out->clear();
   if (n < 1) return false;
@@ -44,30 +59,28 @@ static bool factorize(int n, std::vector<int>* out, bool composites = true) {
     --it->second;
     return true;
   };
+  const int cmax = composites ? max_composite_for(n) : 0;
   for (; twos >= 3; twos -= 3) out->push_back(8);
-  if (!composites) {
-    if (twos == 2) out->push_back(4);
-    if (twos == 1) out->push_back(2);
-  } else if (twos == 1) {
-    if (take(7)) out->push_back(14);
-    else if (take(5)) out->push_back(10);
-    else if (take(3)) out->push_back(6);
+  if (twos == 1) {
+    if (cmax >= 14 && take(7)) out->push_back(14);
+    else if (cmax >= 10 && take(5)) out->push_back(10);
+    else if (cmax >= 6 && take(3)) out->push_back(6);
     else out->push_back(2);
   } else if (twos == 2) {
-    if (take(3)) out->push_back(12);
+    if (cmax >= 12 && take(3)) out->push_back(12);
     else out->push_back(4);
   }
-  while (composites && odd[3] >= 1 && odd[5] >= 1) {
+  while (cmax >= 15 && odd[3] >= 1 && odd[5] >= 1) {
     --odd[3];
     --odd[5];
     out->push_back(15);
   }
-  while (composites && odd[3] >= 1 && odd[7] >= 1) {
+  while (cmax >= 21 && odd[3] >= 1 && odd[7] >= 1) {
     --odd[3];
     --odd[7];
     out->push_back(21);
   }
-  while (composites && odd[3] >= 2) {
+  while (cmax >= 9 && odd[3] >= 2) {
     odd[3] -= 2;
     out->push_back(9);
   }

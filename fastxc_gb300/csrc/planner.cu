@@ -60,15 +60,19 @@ int64_t xc_host_bytes(int64_t npairs, int64_t nwin, int32_t nchan, int64_t spec_
 // library's scratch for the batch (PWS: the analytic-signal sums per pair;
 // TF-PWS: the analytic spectra of every group and linear stack, the output
 // spectra and the Gaussian window table).
-int64_t stack_batch_bytes(int mode, int64_t ntraces, int64_t npairs, int64_t ngroups, int32_t n) {
+int64_t stack_batch_bytes(int mode, int64_t ntraces, int64_t npairs, int64_t ngroups, int64_t max_groups,
+                          int32_t n) {
   const int64_t tr = 4 * ntraces * n;
   const int64_t pairs = 4 * npairs * n;
   int64_t b = al256(tr) + al256(tr) + al256(4 * ntraces) + al256(pairs) + al256(pairs);
   b += al256(16 * npairs) + 256;  // group offsets / counts staging
   if (mode == 0) {
-    // PWS partial sums: pairs x group chunks x n complex, the chunk count
-    // chosen for about eight waves of six resident CTAs per SM (bound: 160 SMs)
-    b += 8 * (int64_t)n * (npairs + 8 * 6 * 160);
+    // PWS partial sums: pairs x group chunks x n complex; fxc_pws_run takes
+    // ceil(8 waves x 6 CTAs x SMs / pairs) chunks of at least two groups of
+    // the pair with the most groups (bound: 160 SMs)
+    const int64_t want = std::max<int64_t>(1, (8 * 6 * 160 + npairs - 1) / std::max<int64_t>(npairs, 1));
+    const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(want, (max_groups + 1) / 2));
+    b += 8 * (int64_t)n * npairs * chunks;
   } else {
     const int64_t nfreq = n / 2 + 1;
     b += al256(8 * npairs) + al256(4 * npairs) + al256(8 * ngroups * n) + al256(8 * npairs * n) +
@@ -121,8 +125,8 @@ extern "C" int fxc_plan_stack_traces(int mode, int32_t nsamples, int32_t traces_
                 "invalid arguments");
   const int64_t b = substack >= 2 ? substack : 1;
   auto bytes = [&](int64_t npairs) {
-    const int64_t groups = npairs * ((traces_per_pair + b - 1) / b);
-    return stack_batch_bytes(mode, npairs * traces_per_pair, npairs, groups, nsamples);
+    const int64_t per_pair = (traces_per_pair + b - 1) / b;
+    return stack_batch_bytes(mode, npairs * traces_per_pair, npairs, npairs * per_pair, per_pair, nsamples);
   };
   if (bytes(1) > budget_bytes) {
     set_error("one pair of %d traces x %d samples needs %lld device bytes, above the budget of %lld",
@@ -144,13 +148,13 @@ extern "C" int fxc_plan_stack_traces(int mode, int32_t nsamples, int32_t traces_
   return FXC_OK;
 }
 
-extern "C" int fxc_stack_batch_bytes(int mode, int64_t ntraces, int32_t npairs, int64_t ngroups, int32_t nsamples,
-                                     int64_t* bytes) {
+extern "C" int fxc_stack_batch_bytes(int mode, int64_t ntraces, int32_t npairs, int64_t ngroups,
+                                     int64_t max_groups_per_pair, int32_t nsamples, int64_t* bytes) {
   clear_error();
   FXC_CHECK_ARG(bytes != nullptr && (mode == 0 || mode == 1) && ntraces >= 0 && npairs >= 0 && ngroups >= 0 &&
-                    nsamples > 0,
+                    max_groups_per_pair >= 0 && nsamples > 0,
                 "invalid arguments");
-  *bytes = stack_batch_bytes(mode, ntraces, npairs, ngroups, nsamples);
+  *bytes = stack_batch_bytes(mode, ntraces, npairs, ngroups, max_groups_per_pair, nsamples);
   return FXC_OK;
 }
 

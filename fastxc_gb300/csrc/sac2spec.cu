@@ -42,7 +42,10 @@
 
 namespace fxc {
 
-constexpr int kS2sT = 1024;
+#ifndef FXC_S2S_THREADS
+#define FXC_S2S_THREADS 1024
+#endif
+constexpr int kS2sT = FXC_S2S_THREADS;
 constexpr float kMaxVal = 20.0f;  // MAXVAL, native/sac2spec/include/config.h:13
 constexpr double kMinValD = 1e-30;  // MINVAL as a double literal (div2DKernel compares this)
 constexpr float kMinValF = 1e-30f;  // MINVAL passed as a float (clampmin2DKernel)

@@ -86,6 +86,23 @@ int fxc_ctx_destroy(fxc_ctx *ctx);
 int fxc_ctx_set_stream(fxc_ctx *ctx, void *stream);
 int fxc_ctx_synchronize(fxc_ctx *ctx);
 
+/* CUDA-graph capture of a launch sequence (no counterpart in the reference,
+ * which launches every kernel from the host each time). Between
+ * fxc_graph_begin and fxc_graph_end, calls on the context are recorded
+ * instead of run; fxc_graph_launch replays them on the context's stream
+ * with the same pointers and sizes. Only device-resident calls that neither
+ * synchronise nor allocate can be recorded: fxc_xc_pack,
+ * fxc_xc_stack_packed, fxc_xc_stack, fxc_xc_finalize and
+ * fxc_xc_stack_finalize_packed after one uncaptured call of the same shapes
+ * (which sizes the context's scratch and FFT tables). The context must use a
+ * non-default stream. fxc_graph_end fails with FXC_ERR_CUDA when a recorded
+ * call synchronised or allocated. */
+typedef struct fxc_graph fxc_graph;
+int fxc_graph_begin(fxc_ctx *ctx);
+int fxc_graph_end(fxc_ctx *ctx, fxc_graph **out);
+int fxc_graph_launch(fxc_ctx *ctx, const fxc_graph *g);
+int fxc_graph_destroy(fxc_graph *g);
+
 /* ---- memory helpers ------------------------------------------------------
  * For callers without a CUDA runtime of their own (the drop-in executables,
  * ctypes). No reference counterpart: the reference executables call
@@ -440,9 +457,10 @@ int fxc_plan_xc_pairs(int64_t npairs, int64_t nwin, int32_t nchan, int64_t spec_
                       int64_t *bytes_per_call);
 /* Device bytes of one stacking batch of ncf_pws (mode 0) / ncf_tfpws (mode 1):
  * the executables' trace, group, weight, linear and output buffers plus the
- * library scratch of fxc_pws_run / fxc_tfpws_run for the batch. */
-int fxc_stack_batch_bytes(int mode, int64_t ntraces, int32_t npairs, int64_t ngroups, int32_t nsamples,
-                          int64_t *bytes);
+ * library scratch of fxc_pws_run / fxc_tfpws_run for the batch
+ * (max_groups_per_pair: the largest substack-group count of one pair). */
+int fxc_stack_batch_bytes(int mode, int64_t ntraces, int32_t npairs, int64_t ngroups, int64_t max_groups_per_pair,
+                          int32_t nsamples, int64_t *bytes);
 /* Largest batch (in traces, whole pairs of traces_per_pair) whose bytes fit
  * budget_bytes. Replaces select_tfpws_resident_chunk_plan
  * (native/tfpws/include/tfpws_schedule.hpp:149-217): this library forms

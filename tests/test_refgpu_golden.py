@@ -10,7 +10,7 @@ needs neither the reference tree nor its built kernels.
 Tolerances as in ``tests/test_refgpu_parity.py``: relative L2 1e-5 (one-bit
 1e-3; phase-only on bins above 1e-2 of the row peak; the settings whose
 whitening reaches the Nyquist frequency within twice the reference's own
-distance to FP64, which the fixture stores).
+distance to FP64, which the fixture stores, x3 against the frozen reference).
 """
 
 import hashlib
@@ -66,7 +66,7 @@ def test_sac2spec_matches_frozen_reference(ctx, torch_cuda, gold, name, filter_f
         row, ref = np.where(keep, row, 0), np.where(keep, ref, 0)
     e = rel_rows(row, ref).max()
     print(f"{name}: vs frozen reference {e:.2e} (reference vs FP64 {meta[f's2s_{name}_ref_vs_fp64']:.2e})")
-    bound = 2.0 * meta[f"s2s_{name}_ref_vs_fp64"] + 1e-6 if tol is None else tol
+    bound = 3.0 * meta[f"s2s_{name}_ref_vs_fp64"] + 1e-6 if tol is None else tol
     assert e < bound, (e, bound)
 
 

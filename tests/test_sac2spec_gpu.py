@@ -141,3 +141,36 @@ def test_sac2spec_20hz_rows_above_shared_memory(ctx, torch_cuda, whiten, normali
     err = row_err(got, ref)
     print("20 Hz rows rel err", err.max())
     assert err.max() < 1e-5
+
+
+@pytest.mark.parametrize("offset,trend", [(1.0e4, 50.0), (-3.0e3, -400.0)])
+def test_sac2spec_detrend_large_offset_and_trend(ctx, torch_cuda, offset, trend):
+    """The reference sums the demean / detrend least squares in FP64; this
+    library in compensated FP32 with an FP64 block reduction. Adversarial
+    input: 72 000-sample windows (0.05 s x 3600 s) riding on a large DC
+    offset and a steep linear trend (over the day) on top of noise + the
+    coherent source. Checked against the FP64 oracle at 1e-5."""
+    torch = torch_cuda
+    from fastxc_gb300 import sac2spec as s2s
+    from fastxc_gb300 import synthetic as sy
+
+    delta = 0.05
+    F = s2s.read_filter_file(G / "filter_d0.05_0.05-5.txt")
+    plan = s2s.plan(86400, 3600, 3600, 100, delta, F, so.WHITEN_AFTER, so.NORM_RUNABS, False)
+    resp = s2s.filter_response(plan, F)
+    arr = sy.station_array(1, seed=3)
+    series = sy.station_series(arr, plan.npts, delta, seed=3).astype(np.float64)
+    t = np.arange(plan.npts) / plan.npts
+    series = (series + offset + trend * t[None, :]).astype(np.float32)
+    steps = [0, 11, 23]
+    d_out = torch.zeros((len(steps), 3, plan.nspec), dtype=torch.complex64, device="cuda")
+    s2s.run(ctx, plan, torch.from_numpy(series).cuda(), plan.npts, plan.npts, 3, 3, steps,
+            torch.from_numpy(resp).cuda(), d_out, plan.nspec)
+    ctx.synchronize()
+    got = d_out.cpu().numpy()
+    op = so.make_plan(86400, 3600, 3600, 100, delta, so.read_filter_file(G / "filter_d0.05_0.05-5.txt"),
+                      so.WHITEN_AFTER, so.NORM_RUNABS, 0)
+    ref = so.run_rows(so.windows(series.astype(np.float64), op, steps), op, 3)
+    err = row_err(got, ref)
+    print("large offset / trend rel err", err.max())
+    assert err.max() < 1e-5, err

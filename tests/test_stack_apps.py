@@ -146,3 +146,45 @@ def test_stack_apps_command_line_errors(tmp_path, built_lib):
     r = subprocess.run([str(BIN / "ncf_pws"), "--index-list", str(tmp_path / "none.txt"), "--output-dir",
                         str(tmp_path / "o")], capture_output=True, text=True)
     assert r.returncode == 1 and "sourcepack_list_open_failed" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("exe,args,mode,sub", [("ncf_pws", ["-B", "3"], 0, 3),
+                                               ("ncf_tfpws", ["-B", "2", "-F", "0.2/1.5"], 1, 2)])
+def test_stack_apps_memory_budget_batches(tmp_path, built_lib, torch_cuda, exe, args, mode, sub):
+    """-M below the whole job's device footprint splits the groups into
+    several batches (fxc_stack_batch_bytes); every output byte equals the
+    one-batch run's."""
+    import ctypes as C
+
+    from fastxc_gb300._lib import lib
+
+    n = 2001
+    lst, groups = make_sourcepack(tmp_path, nsamples=n, seed=5)
+    ng = (NTS + sub - 1) // sub
+
+    def nbytes(npairs):
+        out = C.c_int64()
+        lib().fxc_stack_batch_bytes(mode, npairs * NTS, npairs, npairs * ng, ng, n, C.byref(out))
+        return out.value
+
+    total = len(groups)
+    mib = -(-nbytes(3) // (1 << 20))
+    assert nbytes(total) > mib << 20, "budget must split the job"
+    flag = ["--gpu-memory-mib"] if exe == "ncf_pws" else ["-M"]
+    out_dirs = []
+    for tag, extra in (("whole", []), ("split", flag + [str(mib)])):
+        out = tmp_path / tag
+        cmd = [str(BIN / exe), "--index-list" if exe == "ncf_pws" else "-I", str(lst),
+               "--output-dir" if exe == "ncf_pws" else "-O", str(out), *args, *extra]
+        r = subprocess.run(cmd, env=dict(os.environ, FASTXC_LOG_LEVEL="warn"), capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out_dirs.append(out)
+    a, b = out_dirs
+    files = sorted(p.relative_to(a) for p in a.rglob("*") if p.is_file())
+    assert files == sorted(p.relative_to(b) for p in b.rglob("*") if p.is_file())
+    for f in files:
+        if f.suffix in (".tsv",) or f.name == "_SUCCESS":
+            assert (b / f).read_text().replace(str(b), "@") == (a / f).read_text().replace(str(a), "@"), f
+        else:
+            assert (b / f).read_bytes() == (a / f).read_bytes(), f

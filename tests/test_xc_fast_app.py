@@ -139,3 +139,49 @@ def test_xc_fast_emits_sourcepack_index(tmp_path, built_lib, torch_cuda):
         mine = emitted / idx.parent.name
         assert (mine / "sourcepack_index.tsv").read_bytes() == idx.read_bytes()
         assert (mine / "_SUCCESS").read_bytes() == (idx.parent / "_SUCCESS").read_bytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["plain", "tensor"])
+def test_xc_fast_memory_budget_pair_blocks(tmp_path, built_lib, torch_cuda, method):
+    """-M below one timestamp's footprint splits its pairs into blocks
+    (fxc_plan_xc_pairs); the records are byte-identical to one whole run."""
+    import ctypes as C
+    import os
+
+    from fastxc_gb300._lib import FXC_XC_PLAIN, FXC_XC_TENSOR, lib
+    from fastxc_gb300.core import xc_shape
+
+    nspec, nstep, nch = 8001, 6, 12
+    make_inputs(tmp_path, nspec=nspec, nstep=nstep)
+    env = dict(os.environ, FASTXC_XC_METHOD=method, FASTXC_LOG_LEVEL="info")
+
+    def run(out, extra):
+        r = subprocess.run([str(EXE), "-I", str(tmp_path / "stepack"), "-P", str(tmp_path / "allowed_paths.tsv"),
+                            "-O", str(out), "-C", "20", *extra], env=env, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        return r.stderr
+
+    run(tmp_path / "whole", [])
+    tsv = next((tmp_path / "whole" / "xcpack").glob("*.tsv"))
+    npairs = len(tsv.read_text().splitlines()) - 1
+    shape = xc_shape(nspec, nstep, 0.1, 20.0)
+    m = FXC_XC_TENSOR if method == "tensor" else FXC_XC_PLAIN
+
+    def nbytes(p):
+        out = C.c_int64()
+        lib().fxc_xc_host_bytes(p, nstep, nch, nspec, C.byref(shape), m, 0, C.byref(out))
+        return out.value
+
+    mib = (nbytes(1) + nbytes(npairs)) // 2 >> 20
+    per = C.c_int64()
+    lib().fxc_plan_xc_pairs(npairs, nstep, nch, nspec, C.byref(shape), m, 0, mib << 20, C.byref(per), None)
+    assert 1 <= per.value < npairs, (per.value, npairs)
+    log = run(tmp_path / "blocks", ["-M", str(mib)])
+    assert "xc_pair_blocks" in log
+    a, b = tmp_path / "whole" / "xcpack", tmp_path / "blocks" / "xcpack"
+    for f in sorted(a.glob("*.xcpack")):
+        assert (b / f.name).read_bytes() == f.read_bytes(), f.name
+    for f in sorted(a.glob("*.tsv")):
+        assert (b / f.name).read_text().replace(str(tmp_path / "blocks"), "@") == \
+            f.read_text().replace(str(tmp_path / "whole"), "@")
