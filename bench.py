@@ -46,6 +46,8 @@ NSPEC = 18523  # output_nfft 37044 / 2 + 1 for win_len 3600 s, lag 100 s at 10 H
 GAP_FRAC = 0.05
 
 
+LAYOUT_NAMES = {0: "auto", 1: "whole_bin", 2: "tiled"}
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -559,7 +561,7 @@ def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "aut
         shape = xc_shape(nspec, nstep, 0.1, 100.0)
         pitch = (nspec + 3) // 4 * 4
         pl = PairPlan(ctx, src, rec, nchan)
-        method, ms_plain, ms_tensor = ctx.xc_autotune(pl, spec[0], nstep, nchan, nspec, nspec)
+        method, layout, tune_ms = ctx.xc_autotune_layout(pl, spec[0], nstep, nchan, nspec, nspec)
         if method_arg != "auto":
             method = FXC_XC_TENSOR if method_arg == "tensor" else FXC_XC_PLAIN
         packed = None
@@ -568,7 +570,8 @@ def batching_run(torch, dev, ctx, stream, block: int = 0, method_arg: str = "aut
                                  device=dev)
         groups.append(dict(win=win, nsta=n, nchan=nchan, nstep=nstep, nspec=nspec, src=src, rec=rec,
                            station_pairs=int(si.size), covered=covered, spec=spec, mask=d_mask, shape=shape,
-                           pitch=pitch, plan=pl, method=method, autotune_ms={"plain": ms_plain, "tensor": ms_tensor},
+                           pitch=pitch, plan=pl, method=method,
+                           autotune_ms=dict(tune_ms, layout=LAYOUT_NAMES.get(layout, layout)),
                            packed=packed,
                            stack=torch.empty((src.size, pitch), dtype=torch.complex64, device=dev),
                            ncf=torch.empty((src.size, shape.cc_size), dtype=torch.float32, device=dev)))
@@ -712,7 +715,7 @@ def main():
 
     __graft_entry__.build()
     from fastxc_gb300 import lib
-    from fastxc_gb300._lib import FXC_XC_PLAIN, FXC_XC_TENSOR, FxcError
+    from fastxc_gb300._lib import FXC_XC_LAYOUT_WHOLE_BIN, FXC_XC_PLAIN, FXC_XC_TENSOR, FxcError
     from fastxc_gb300.core import Context, PairPlan, xc_shape
     from fastxc_gb300 import replicas
     from fastxc_gb300.synthetic import cross_station_pairs, spectra_device, station_array
@@ -744,10 +747,10 @@ def main():
         pass
     autotune = None
     if args.method == "auto":
-        m, ms_plain, ms_tensor = ctx.xc_autotune(plan, spec, nwin, nchan, nspec, nspec)
+        m, lay, ms = ctx.xc_autotune_layout(plan, spec, nwin, nchan, nspec, nspec)
         head = "tensor" if m == FXC_XC_TENSOR and "tensor" in methods else "plain"
-        autotune = {"method": head, "sample_bins": min(nspec, 512), "sample_ms_plain": ms_plain,
-                    "sample_ms_tensor": ms_tensor}
+        autotune = {"method": head, "layout": LAYOUT_NAMES.get(lay, lay), "sample_bins": min(nspec, 512),
+                    "sample_ms": ms}
     else:
         head = args.method
         if head not in methods:
@@ -779,11 +782,10 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
-    # up to 192 channels one CTA runs both triangle tiles of a bin
-    # (above 128 channels or 96 windows; shorter contractions over fewer
-    # channels, and more than 192 channels, run the persistent tiled kernel)
-    gemm_kernel = ("k_xc_tc_gemm_bin" if nchan <= 192 and (nchan > 128 or (nwin + 31) // 32 > 3)
-                   and not os.environ.get("FXC_GEMM_TILED") else "k_xc_tc_gemm")
+    # the contraction kernel of the plan's layout: one CTA per bin over both
+    # triangle tiles (whole bin, up to 192 channels) or persistent CTAs over
+    # (tile, bin) items
+    gemm_kernel = ("k_xc_tc_gemm_bin" if plan.layouts(nwin)[1] == FXC_XC_LAYOUT_WHOLE_BIN else "k_xc_tc_gemm")
     results = {}
     sampler = ClockSampler(local)
     clocks = None

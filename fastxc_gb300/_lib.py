@@ -26,6 +26,7 @@ FXC_ERR_NOTFOUND = -8
 
 FXC_XC_PLAIN = 0
 FXC_XC_TENSOR = 1
+FXC_XC_LAYOUT_AUTO, FXC_XC_LAYOUT_WHOLE_BIN, FXC_XC_LAYOUT_TILED = 0, 1, 2
 
 
 class FxcError(RuntimeError):
@@ -236,6 +237,10 @@ class ServerStats(C.Structure):
 _SIGNATURES.update({
     "fxc_xc_autotune": (_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, C.POINTER(_i32), C.POINTER(_f32),
                                 C.POINTER(_f32)]),
+    "fxc_xc_autotune_layout": (_int, [_vp, _vp, _vp, _i64, _i32, _i32, _i64, C.POINTER(_i32), C.POINTER(_i32),
+                                       C.POINTER(_f32)]),
+    "fxc_pairplan_set_layout": (_int, [_vp, _i32]),
+    "fxc_pairplan_layouts": (_int, [_vp, _i64, C.POINTER(_i32), C.POINTER(_i32)]),
     "fxc_server_create": (_int, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "fxc_server_destroy": (_int, [_vp]),
     "fxc_server_geometry": (_int, [_vp, _f32, C.POINTER(_i32), C.POINTER(_i32)]),

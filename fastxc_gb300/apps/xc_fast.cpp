@@ -17,8 +17,9 @@
 // reference's build_sourcepack makes afterwards) as soon as the timestamp's
 // records and .done marker are on disk.
 //
-// Environment: FASTXC_XC_METHOD=plain|tensor (default: autotuned per
-// timestamp shape with fxc_xc_autotune), FASTXC_XC_BLOCK=<files per block>
+// Environment: FASTXC_XC_METHOD=plain|tensor (default: method and
+// contraction layout autotuned per timestamp shape with
+// fxc_xc_autotune_layout), FASTXC_XC_BLOCK=<files per block>
 // (default: the whole timestamp in one block), FASTXC_LOG_LEVEL.
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -170,10 +171,11 @@ int main(int argc, char** argv) {
       const int64_t npairs = (int64_t)src.size();
       fxc_pairplan* plan = nullptr;
       int rc = FXC_OK;
+      int32_t layout = FXC_XC_LAYOUT_AUTO;
       if (method < 0) {
         // the autotuner samples a few bins of every pair: its plan is the whole list
         rc = fxc_pairplan_create(ctx, src.data(), rec.data(), npairs, (int32_t)nch, &plan);
-        if (rc == FXC_OK) rc = autotune_host(ctx, plan, payload, nstep, (int32_t)nch, nspec, &method);
+        if (rc == FXC_OK) rc = autotune_host(ctx, plan, payload, nstep, (int32_t)nch, nspec, &method, &layout);
         fxc_pairplan_destroy(plan);
         plan = nullptr;
       }
@@ -186,6 +188,8 @@ int main(int argc, char** argv) {
       for (int64_t p0 = 0; rc == FXC_OK && p0 < npairs; p0 += block) {
         const int64_t np = std::min(block, npairs - p0);
         rc = fxc_pairplan_create(ctx, src.data() + p0, rec.data() + p0, np, (int32_t)nch, &plan);
+        // the layout tuned on the whole list, where a block's plan admits it
+        if (rc == FXC_OK && method == FXC_XC_TENSOR) rc = fxc_pairplan_set_layout(plan, layout);
         if (rc == FXC_OK)
           rc = fxc_xc_run_host(ctx, plan, payload.data(), nstep, (int32_t)nch, nspec, nullptr, 1.0f / (float)nstep,
                                &shape, ncf.data() + (size_t)p0 * shape.cc_size, method);

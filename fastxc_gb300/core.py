@@ -124,6 +124,14 @@ class Context:
                               C.byref(a), C.byref(b))
         return int(m.value), float(a.value), float(b.value)
 
+    def xc_autotune_layout(self, plan: "PairPlan", d_spec, nwin, nchan, nspec, spec_pitch):
+        """(method, tensor layout, {"plain", "whole_bin", "tiled"} sample ms)
+        from fxc_xc_autotune_layout; the plan takes the faster layout."""
+        m, lay, ms = C.c_int32(), C.c_int32(), (C.c_float * 3)()
+        lib().fxc_xc_autotune_layout(self.handle, plan.handle, _ptr(d_spec), nwin, nchan, nspec, spec_pitch,
+                                     C.byref(m), C.byref(lay), ms)
+        return int(m.value), int(lay.value), dict(zip(("plain", "whole_bin", "tiled"), (float(v) for v in ms)))
+
     @staticmethod
     def xc_packed_bytes(nchan, nwin, nspec) -> int:
         out = C.c_int64()
@@ -184,6 +192,17 @@ class PairPlan:
     @property
     def ntiles(self) -> int:
         return int(lib().fxc_pairplan_ntiles(self._h))
+
+    def set_layout(self, layout: int) -> None:
+        """Contraction layout preference (FXC_XC_LAYOUT_*; fxc_pairplan_set_layout)."""
+        lib().fxc_pairplan_set_layout(self._h, layout)
+
+    def layouts(self, nwin: int) -> tuple[int, int]:
+        """(admitted layouts as a bit mask of 1 << FXC_XC_LAYOUT_*, the layout
+        a run of nwin windows takes)."""
+        a, e = C.c_int32(), C.c_int32()
+        lib().fxc_pairplan_layouts(self._h, nwin, C.byref(a), C.byref(e))
+        return int(a.value), int(e.value)
 
     def close(self):
         if self._h:

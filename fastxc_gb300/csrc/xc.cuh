@@ -48,6 +48,12 @@ int xc_finalize_launch_tables(fxc_ctx* ctx, const float2* stack, int64_t npairs,
 
 int xc_tensor_plan_init(fxc_ctx* ctx, fxc_pairplan* plan);
 void xc_tensor_plan_free(fxc_pairplan* plan);
+// Contraction layouts (FXC_XC_LAYOUT_*): the admitted ones as a bit mask,
+// the plan's preference, and the layout a run of nwin windows takes.
+int xc_tensor_layouts(const fxc_pairplan* plan);
+int xc_tensor_layout(const fxc_pairplan* plan);
+void xc_tensor_set_layout(const fxc_pairplan* plan, int layout);
+int xc_tensor_effective_layout(const fxc_pairplan* plan, int64_t nwin);
 int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec,
                            int64_t nwin, int nchan, int nspec, int64_t spec_pitch,
                            const uint8_t* mask, float scale, float2* stack, int64_t stack_pitch,

@@ -73,6 +73,7 @@ struct XcTensorPlan {
   int32_t* d_maps = nullptr;  // per tile [128][n]: q, -(q+2) for a reversed pair, -1 none
   int32_t* d_perm = nullptr;  // perm[q] = pair index p of bin-major slot q
   std::vector<TcTile> h_tiles;
+  int32_t layout = FXC_XC_LAYOUT_AUTO;  // contraction layout preference
 };
 
 static int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
@@ -898,16 +899,42 @@ static bool whole_bin_plan(const XcTensorPlan* tp) {
          t[1].b0 == kTcM && t[1].am == C - kTcM && t[1].bn == C - kTcM;
 }
 
-// The whole-bin kernel (one CTA per bin, C <= 192) unless the contraction
-// is short (at most three K-blocks) over at most 128 channels: then the
-// persistent tiled kernel, which pays the per-CTA setup once per SM rather
-// than once per bin, is ahead (at 90 channels and 24 windows 0.038 ms
-// against 0.050 ms per 512 bins; at 192 channels the two tie for short
-// contractions and from 264 windows the whole-bin kernel leads).
-static bool use_whole_bin(const fxc_pairplan* plan, int nkb) {
+// Whether the whole-bin kernel (one CTA per bin) can run this plan: the
+// whole-bin tile geometry and a bin-major row that fits its staging.
+static bool whole_bin_eligible(const fxc_pairplan* plan) {
   return plan->tensor && whole_bin_plan(plan->tensor) &&
-         plan->npairs * (int64_t)sizeof(float2) <= (int64_t)kBinStages * kBinStageBytes &&
-         (nkb > 3 || plan->tensor->nchan > kTcM) && !getenv("FXC_GEMM_TILED");
+         plan->npairs * (int64_t)sizeof(float2) <= (int64_t)kBinStages * kBinStageBytes;
+}
+
+// The layout a tensor contraction runs. A plan's preference
+// (xc_tensor_set_layout, chosen by the autotuner from timings) wins where
+// the plan is eligible for it. Without one: the whole-bin kernel unless the
+// contraction is short (at most three K-blocks) over at most 128 channels,
+// where the persistent tiled kernel, which pays the per-CTA setup once per
+// SM rather than once per bin, is ahead (at 90 channels and 24 windows
+// 0.038 ms against 0.050 ms per 512 bins; at 192 channels the two tie for
+// short contractions and from 264 windows the whole-bin kernel leads).
+static bool use_whole_bin(const fxc_pairplan* plan, int nkb) {
+  if (!whole_bin_eligible(plan) || getenv("FXC_GEMM_TILED")) return false;
+  if (plan->tensor->layout == FXC_XC_LAYOUT_WHOLE_BIN) return true;
+  if (plan->tensor->layout == FXC_XC_LAYOUT_TILED) return false;
+  return nkb > 3 || plan->tensor->nchan > kTcM;
+}
+
+int xc_tensor_layouts(const fxc_pairplan* plan) {
+  if (!plan->tensor || plan->tensor->ntiles == 0) return 0;
+  return (1 << FXC_XC_LAYOUT_TILED) | (whole_bin_eligible(plan) ? 1 << FXC_XC_LAYOUT_WHOLE_BIN : 0);
+}
+
+int xc_tensor_layout(const fxc_pairplan* plan) { return plan->tensor ? plan->tensor->layout : FXC_XC_LAYOUT_AUTO; }
+
+void xc_tensor_set_layout(const fxc_pairplan* plan, int layout) {
+  if (plan->tensor) plan->tensor->layout = layout;
+}
+
+int xc_tensor_effective_layout(const fxc_pairplan* plan, int64_t nwin) {
+  if (!plan->tensor) return FXC_XC_LAYOUT_AUTO;
+  return use_whole_bin(plan, (int)((nwin + kTcKb - 1) / kTcKb)) ? FXC_XC_LAYOUT_WHOLE_BIN : FXC_XC_LAYOUT_TILED;
 }
 
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec) {

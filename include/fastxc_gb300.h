@@ -46,6 +46,10 @@ extern "C" {
 
 #define FXC_XC_PLAIN 0  /* FP32 CUDA-core per-pair product, register blocked */
 #define FXC_XC_TENSOR 1 /* BF16 hi/lo split tcgen05 contraction S(f)=Y^H Y */
+/* layouts of the tensor contraction (fxc_pairplan_set_layout) */
+#define FXC_XC_LAYOUT_AUTO 0      /* whole-bin unless a short contraction over <= 128 channels */
+#define FXC_XC_LAYOUT_WHOLE_BIN 1 /* one CTA per bin over every tile (<= 192 channels, one tile layer) */
+#define FXC_XC_LAYOUT_TILED 2     /* persistent CTAs over (tile, bin) items */
 
 typedef struct fxc_ctx fxc_ctx;
 typedef struct fxc_pairplan fxc_pairplan;
@@ -363,15 +367,37 @@ int fxc_tfpws_run(fxc_ctx *ctx, const float *d_groups, const float *d_weights,
                   const float *d_linear, int32_t nsamples, float delta, int32_t band_limited,
                   float fmin, float fmax, float taper_hz, float power, float *d_out);
 
-/* Autotuner of the stack method (tile shape): times the plain FP32 kernel
- * (16 x 16 channel tiles) and the tcgen05 BF16 hi/lo contraction (128 x N
- * tiles + pack) on the first min(nspec, 512) bins of d_spec and returns the
- * faster in *method (FXC_XC_PLAIN / FXC_XC_TENSOR) with the sample times
- * (ms, -1 when a candidate does not apply; ms_* may be null). Decisions are
- * cached per (device, channels, windows, pairs, tiles) for the process. No
- * reference counterpart (the reference has one kernel). Synchronous. */
+/* Autotuner of the stack method and contraction layout: times the plain
+ * FP32 kernel (16 x 16 channel tiles) and the tcgen05 BF16 hi/lo
+ * contraction (pack + 128 x N tiles) in each layout the plan admits (whole
+ * bin: one CTA per bin over every tile; tiled: persistent CTAs over (tile,
+ * bin) items) on the first min(nspec, 512) bins of d_spec. Returns the
+ * faster method in *method (FXC_XC_PLAIN / FXC_XC_TENSOR) with the sample
+ * times (ms, -1 when a candidate does not apply; ms_* may be null;
+ * *ms_tensor is the faster layout's), and sets the plan's contraction
+ * layout to the faster one. Decisions are cached per (device, channels,
+ * windows, pairs, tiles) for the process. Must not overlap a run of the
+ * same plan. No reference counterpart (the reference has one kernel).
+ * Synchronous. */
 int fxc_xc_autotune(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, int64_t nwin, int32_t nchan,
                     int32_t nspec, int64_t spec_pitch, int32_t *method, float *ms_plain, float *ms_tensor);
+
+/* fxc_xc_autotune with every candidate's time: *layout the faster tensor
+ * layout (FXC_XC_LAYOUT_WHOLE_BIN / _TILED), ms[3] = plain, whole-bin,
+ * tiled (-1 where a candidate does not apply; ms may be null). */
+int fxc_xc_autotune_layout(fxc_ctx *ctx, const fxc_pairplan *plan, const float *d_spec, int64_t nwin,
+                           int32_t nchan, int32_t nspec, int64_t spec_pitch, int32_t *method, int32_t *layout,
+                           float *ms);
+
+/* Contraction layout preference of a plan's tensor path (FXC_XC_LAYOUT_*),
+ * honoured where the plan admits it (a whole-bin preference on a plan
+ * without the whole-bin tile geometry runs tiled). For plans of pair
+ * blocks that take a layout tuned on the whole pair list. */
+int fxc_pairplan_set_layout(fxc_pairplan *plan, int32_t layout);
+
+/* Layouts the plan admits, as a bit mask of 1 << FXC_XC_LAYOUT_* (0: no
+ * tensor tiles), and the layout a run of nwin windows takes. */
+int fxc_pairplan_layouts(const fxc_pairplan *plan, int64_t nwin, int32_t *admitted, int32_t *effective);
 
 /* ---- serving: correlation jobs over resident station spectra ------------
  * No counterpart in the reference (its stages are batch executables). A

@@ -16,7 +16,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 BIN = ROOT / "fastxc_gb300" / "bin"
 FILTER = HERE / "filter_d1.0_0.2-0.4_0.1-0.2.txt"
-TS = "2022.137.0000"
+TS = "2022.138.0000"
 STATIONS = ("A7K2", "B4Q8", "C9M3", "D2X6")
 COMPS = ("E", "N", "Z")
 SAC_LEN, WIN, LAG, DELTA = 86400.0, 3600.0, 100.0, 1.0
@@ -81,6 +81,34 @@ def run_ours(tmp: Path, sac, method: str = "plain") -> dict:
     return out
 
 
+def pairs():
+    """(keys, src rows, rec rows) of the 54 component pairs."""
+    keys, src, rec = [], [], []
+    for a in range(4):
+        for b in range(a + 1, 4):
+            for i in range(3):
+                for j in range(3):
+                    keys.append((STATIONS[a], COMPS[i], STATIONS[b], COMPS[j]))
+                    src.append(3 * a + i)
+                    rec.append(3 * b + j)
+    return keys, np.array(src), np.array(rec)
+
+
+def fp64_ncfs(sac) -> dict:
+    """The FP64 oracle's NCFs of the same data: {key: NCF}."""
+    from oracle import sac2spec_oracle as so
+    from oracle import xc_oracle as xo
+
+    op = so.make_plan(SAC_LEN, WIN, WIN, LAG, DELTA, so.read_filter_file(FILTER), WHITEN_AFTER, NORM_RUNABS_MF, 0)
+    wins = so.windows(series(sac), op, list(range(op.nstep))).astype(np.float32)
+    spec = so.run_rows(wins.astype(np.float64), op, 3)
+    keys, src, rec = pairs()
+    nwin, _, nspec = spec.shape
+    shape = xo.finalize_shape(nspec, nwin, DELTA, LAG)
+    out = xo.xc_run(spec, src, rec, 1.0 / nwin, shape)
+    return {k: out[i] for i, k in enumerate(keys)}
+
+
 def reference_ncfs(sac) -> tuple[dict, dict]:
     """The reference's kernels (oracle/ref_gpu.py) and the FP64 oracle on the
     same data: ({key: NCF}, {key: FP64 NCF})."""
@@ -93,18 +121,11 @@ def reference_ncfs(sac) -> tuple[dict, dict]:
     wins = so.windows(x, op, list(range(op.nstep))).astype(np.float32)
     ref_spec = ref_gpu.sac2spec_rows(wins, op, op.responses, 3)
     fp64_spec = so.run_rows(wins.astype(np.float64), op, 3)
-    keys, src, rec = [], [], []
-    for a in range(4):
-        for b in range(a + 1, 4):
-            for i in range(3):
-                for j in range(3):
-                    keys.append((STATIONS[a], COMPS[i], STATIONS[b], COMPS[j]))
-                    src.append(3 * a + i)
-                    rec.append(3 * b + j)
+    keys, src, rec = pairs()
     nwin, _, nspec = ref_spec.shape
     shape = xo.finalize_shape(nspec, nwin, DELTA, LAG)
-    ref = ref_gpu.xc_run(ref_spec, np.array(src), np.array(rec), shape.nfft, shape.half_cc, shape.dt)
-    fp64 = xo.xc_run(fp64_spec, np.array(src), np.array(rec), 1.0 / nwin, shape)
+    ref = ref_gpu.xc_run(ref_spec, src, rec, shape.nfft, shape.half_cc, shape.dt)
+    fp64 = xo.xc_run(fp64_spec, src, rec, 1.0 / nwin, shape)
     return {k: ref[i] for i, k in enumerate(keys)}, {k: fp64[i] for i, k in enumerate(keys)}
 
 

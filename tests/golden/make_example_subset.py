@@ -1,8 +1,9 @@
 """Copies one day of the reference's public smoke-test data into a fixture.
 
 The reference ships 84 anonymised 1 Hz SAC files (4 stations x E/N/Z x 7
-days, example/data, with example/config.ini). This keeps the first day of
-all four stations -- 12 files, byte for byte -- in example_1hz_sac.npz:
+days, example/data, with example/config.ini). This keeps one day
+(2022.138, the first with no zero-filled gap on any station) of all four
+stations -- 12 files, byte for byte -- in example_1hz_sac.npz:
 
     python tests/golden/make_example_subset.py [reference root]
 
@@ -22,7 +23,7 @@ sys.path.insert(0, str(HERE.parents[1]))
 from oracle.build_ref import reference_root  # noqa: E402
 
 STATIONS = ("A7K2", "B4Q8", "C9M3", "D2X6")
-DAY = "2022.137.0000"
+DAY = "2022.138.0000"
 
 
 def main(root: Path) -> None:

