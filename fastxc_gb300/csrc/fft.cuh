@@ -458,7 +458,7 @@ __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, con
 // after buf and the twiddle table stw (fft_twiddles_to_smem) are written and
 // the CTA synchronised; the result is visible to the CTA on return.
 template <int T, bool COMP = true>
-__device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ __noinline__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = p.n;
   int Rprod = 1;  // r_0 ... r_{s-1}
   for (int s = 0; s < p.nstages; ++s) {
@@ -474,7 +474,7 @@ __device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool i
 
 // Digit-reversed input (the layout fft_dif produces), natural-order output.
 template <int T, bool COMP = true>
-__device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ __noinline__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = 1;
   int Rprod = p.n;
   for (int s = p.nstages - 1; s >= 0; --s) {

@@ -27,14 +27,23 @@
 //                   C2R, then either the output transform or the time row
 //   k_s2s_output    [RAM divide] zero-pad, R2C(output_nfft), x dt,
 //                   sanitize, optional phase-only
+//   k_s2s_station   (opt-in) the whole chain for the three components of a
+//                   station window in one 3-CTA cluster, the weights
+//                   exchanged through distributed shared memory
+// Each thread issues the global loads of 4-8 items before using any, and
+// the pointwise passes read a batch of bin pairs before writing: one CTA per
+// SM leaves no other CTA to hide load latency.
 // Boxcar smoothing keeps the reference's window and divisor. The reference's
 // FP64 sums and products (demean, detrend, normalisations) run as FP32 with
-// Kahan-compensated sums and two-float constants (F2c below): GB300's FP64
-// pipe is a small fraction of its FP32 rate.
+// Kahan-compensated sums, double-float block reductions and two-float
+// constants (F2c below) formed on the host or by one thread: GB300's FP64
+// pipe issues at 1/64 of its FP32 rate.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "context.cuh"
 #include "fft.cuh"
@@ -47,8 +56,18 @@ namespace fxc {
 #endif
 constexpr int kS2sT = FXC_S2S_THREADS;
 constexpr float kMaxVal = 20.0f;  // MAXVAL, native/sac2spec/include/config.h:13
-constexpr double kMinValD = 1e-30;  // MINVAL as a double literal (div2DKernel compares this)
 constexpr float kMinValF = 1e-30f;  // MINVAL passed as a float (clampmin2DKernel)
+
+// A double constant c as the unevaluated sum hi + lo of two floats.
+struct F2c {
+  float hi, lo;
+};
+__host__ __device__ inline F2c f2c(double c) {
+  F2c r;
+  r.hi = (float)c;
+  r.lo = (float)(c - (double)r.hi);
+  return r;
+}
 
 struct S2sDev {
   float delta;
@@ -58,46 +77,67 @@ struct S2sDev {
   int phase_only;
   int num_ch;
   int nrows;  // rows per step
+  F2c inrm_f;  // 1 / (filter_nfft dt): prefilter round trip
+  F2c inrm_s;  // 1 / (seg dt): whitening round trip
+  F2c inv_rw;  // 1 / runabs_win
+  F2c inv_ww;  // 1 / whiten_win
+  // detrend least squares over i = 0 .. seg-1 (rtr2DKernel):
+  double a11, a12, a22, inv_det;
 };
 
 // ---------------------------------------------------------------------------
 // block helpers
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ double block_sum_f64(double v, double* sred) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+// Sums over the CTA of N threads' compensated values (v_i = hi_i + lo_i),
+// returned in double by thread 0 (0 elsewhere). Warps reduce in
+// double-float FP32 arithmetic (error-free two-sums), so the only FP64
+// operations are one warp's: GB300 issues FP64 at 1/64 of the FP32 rate.
+__device__ __forceinline__ void df_add(float& ah, float& al, float bh, float bl) {
+  const float s = ah + bh;
+  const float v = s - ah;
+  float e = (ah - (s - v)) + (bh - v);
+  e += al + bl;
+  ah = s + e;
+  al = e - (ah - s);
+}
+
+template <int N>
+__device__ __forceinline__ void block_sums_t0(const float (&hi)[N], const float (&lo)[N], double* sred,
+                                              double (&out)[N]) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) sred[w] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (w == 0) {
-    t = (l < (int)(blockDim.x >> 5)) ? sred[l] : 0.0;
+  const int nw = (int)(blockDim.x >> 5);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (l == 0) sred[0] = t;
+  for (int q = 0; q < N; ++q) {
+    float h = hi[q], e = lo[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+      const float oe = __shfl_xor_sync(0xffffffffu, e, o);
+      df_add(h, e, oh, oe);
+    }
+    if (l == 0) sred[q * 32 + w] = (double)h + (double)e;
   }
   __syncthreads();
-  t = sred[0];
-  __syncthreads();
-  return t;
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    double t = 0.0;
+    if (w == 0) {
+      t = l < nw ? sred[q * 32 + l] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    out[q] = threadIdx.x == 0 ? t : 0.0;
+  }
+  __syncthreads();  // sred free again
 }
 
 // GB300 runs FP64 at a small fraction of its FP32 rate, so per-sample work
 // stays in FP32. A double constant c becomes the unevaluated sum hi + lo of
 // two floats; x * c = fma(x, hi, x * lo) is within an ulp of the float of
 // the double product. Sums over a row are Kahan-compensated FP32 per thread
-// with only the 1024-way block reduction in double.
-struct F2c {
-  float hi, lo;
-};
-__device__ __forceinline__ F2c f2c(double c) {
-  F2c r;
-  r.hi = (float)c;
-  r.lo = (float)(c - (double)r.hi);
-  return r;
-}
+// with the block reduction in double-float. Plan constants are formed on the
+// host, per-row ones by one thread.
 __device__ __forceinline__ float mul_f2c(float x, F2c c) { return fmaf(x, c.hi, x * c.lo); }
 struct Kahan {
   float s = 0.f, c = 0.f;
@@ -107,7 +147,6 @@ struct Kahan {
     c = (t - s) - y;
     s = t;
   }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
 __device__ __forceinline__ bool finite2(float2 v) { return isfinite(v.x) && isfinite(v.y); }
@@ -116,16 +155,16 @@ __device__ __forceinline__ float2 sanitize2(float2 v) {
 }
 
 // Centred boxcar of width win over src[0, n) (reference smoothRowsRollingKernel:
-// window [c - win/2, c - win/2 + win - 1] clipped to the row, divided by win).
-// Each thread owns a contiguous run of outputs and slides a Kahan-compensated
-// FP32 sum across it. abs_src takes |src|.
+// window [c - win/2, c - win/2 + win - 1] clipped to the row, divided by win)
+// for the outputs c in [a, b). Each thread owns a contiguous run of outputs
+// and slides a Kahan-compensated FP32 sum across it. ABS takes |src|.
 template <bool ABS, typename Store>
-__device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, Store store) {
-  const int per = (n + kS2sT - 1) / kS2sT;
-  const int c0 = threadIdx.x * per;
-  if (c0 >= n) return;
-  const int c1 = min(n, c0 + per);
-  const F2c inv = f2c(1.0 / (double)win);
+__device__ __forceinline__ void boxcar_range(const float* src, int n, int win, F2c inv, int a, int b,
+                                             Store store) {
+  const int per = (b - a + kS2sT - 1) / kS2sT;
+  const int c0 = a + threadIdx.x * per;
+  if (c0 >= b) return;
+  const int c1 = min(b, c0 + per);
   const int half = win / 2;
   float s = 0.f, comp = 0.f;
   auto kadd = [&](float v) {
@@ -145,13 +184,53 @@ __device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, St
   }
 }
 
-// RAM divide of one sample (runabsNormalizeSharedWeight): the station weight
-// is the float sum of the component weights, clamped to MINVAL; x / w, NaN
-// -> 0, clip to +-MAXVAL.
-__device__ __forceinline__ float ram_divide(float x, const float* __restrict__ w, int64_t row0,
-                                            int64_t pitch, int num_ch, int i) {
-  float s = 0.f;
-  for (int c = 0; c < num_ch; ++c) s += w[(row0 + c) * pitch + i];
+template <bool ABS, typename Store>
+__device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, F2c inv, Store store) {
+  boxcar_range<ABS>(src, n, win, inv, 0, n, store);
+}
+
+// The boxcar of a[0, n) (no abs) written back over a (n <= RMAX x threads):
+// each thread keeps its run of outputs in registers until every thread has
+// read its window, then stores it. Ends with the CTA synchronised.
+template <int RMAX>
+__device__ __forceinline__ void boxcar_inplace(float* a, int n, int win, F2c inv) {
+  const int per = (n + kS2sT - 1) / kS2sT;
+  const int c0 = threadIdx.x * per;
+  const int c1 = min(n, c0 + per);
+  float r[RMAX];
+  if (c0 < n) {
+    const int half = win / 2;
+    float s = 0.f, comp = 0.f;
+    auto kadd = [&](float v) {
+      const float y = v - comp;
+      const float t = s + y;
+      comp = (t - s) - y;
+      s = t;
+    };
+    const int lo = max(0, c0 - half), hi = min(n - 1, c0 - half + win - 1);
+    for (int j = lo; j <= hi; ++j) kadd(a[j]);
+#pragma unroll
+    for (int j = 0; j < RMAX; ++j) {
+      const int c = c0 + j;
+      if (c < c1) {
+        r[j] = mul_f2c(s, inv);
+        const int out = c - half, in = c - half + win;
+        if (out >= 0 && out < n) kadd(-a[out]);
+        if (in >= 0 && in < n) kadd(a[in]);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < RMAX; ++j)
+    if (c0 + j < c1) a[c0 + j] = r[j];
+  __syncthreads();
+}
+
+// RAM divide of one sample (runabsNormalizeSharedWeight) by the station
+// weight s, the float sum of the component weights in component order:
+// s clamped to MINVAL, x / s, NaN -> 0, clip to +-MAXVAL.
+__device__ __forceinline__ float ram_divide_s(float x, float s) {
   if (!isfinite(s) || s < kMinValF) s = kMinValF;
   // (double)s < MINVAL in double is s < (float)MINVAL for a float s (no
   // float lies in [1e-30, (float)1e-30)), and never true after the clamp
@@ -160,43 +239,138 @@ __device__ __forceinline__ float ram_divide(float x, const float* __restrict__ w
   return fminf(fmaxf(y, -kMaxVal), kMaxVal);
 }
 
+__device__ __forceinline__ float ram_divide(float x, const float* __restrict__ w, int64_t row0,
+                                            int64_t pitch, int num_ch, int i) {
+  float s = 0.f;
+  for (int c = 0; c < num_ch; ++c) s += w[(row0 + c) * pitch + i];
+  return ram_divide_s(x, s);
+}
+
+// Bins in flight per thread in the pointwise passes: the digit-reversal
+// table and the row reads of kPw bins are issued before any of them is
+// used, so their latencies overlap (one CTA per SM leaves no other CTA to
+// hide them).
+constexpr int kPw = 4;
+
+// store(i, load(i)) for i in [0, n), each thread over i = tid, tid + T, ...
+// in that order, with the loads of U consecutive items of a thread issued
+// before the first store (global-memory latency overlapped U ways).
+template <int U, typename Ld, typename St>
+__device__ __forceinline__ void batched_rows(int n, Ld load, St store) {
+  for (int i0 = threadIdx.x; i0 < n; i0 += U * kS2sT) {
+    decltype(load(0)) v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) v[u] = load(min(i0 + u * kS2sT, n - 1));
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i0 + u * kS2sT < n) store(i0 + u * kS2sT, v[u]);
+  }
+}
+
+// Real-transform twiddle w_{2M}^k (k <= M) from the shared-memory copy of a
+// real plan's table (tw_stride 2: the table is of the real length 2M).
+__device__ __forceinline__ float2 real_tw(const float2* stw, int k, int M) {
+  return k == M ? make_float2(-1.f, 0.f) : tw_lookup(stw, k);
+}
+
+// Forward post-processing (r2c_post) of the loaded pair za = Z[k],
+// zb = Z[M-k] (Z[M] == Z[0]).
+__device__ __forceinline__ float2 r2c_post_vals(float2 za, float2 zb, int k, int M, const float2* stw) {
+  const float2 zc = conjf2(zb);
+  const float2 xe = make_float2(0.5f * (za.x + zc.x), 0.5f * (za.y + zc.y));
+  const float2 d = make_float2(0.5f * (za.x - zc.x), 0.5f * (za.y - zc.y));
+  return cadd(xe, cmul(real_tw(stw, k, M), mul_mi(d)));
+}
+
+// g(k, X[k]) for the bins k in [0, kend) (kend <= M + 1) of the real
+// forward transform whose length-M complex FFT Z sits digit-reversed in buf.
+template <typename G>
+__device__ __forceinline__ void r2c_post_bins(const float2* buf, const FftPlan& p, const float2* stw, int kend,
+                                              G g) {
+  const int M = p.n;
+  for (int k0 = threadIdx.x; k0 < kend; k0 += kPw * kS2sT) {
+    int pa[kPw], pb[kPw];
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      const int k = min(k0 + u * kS2sT, kend - 1);
+      pa[u] = __ldg(p.perm + (k == M ? 0 : k));
+      pb[u] = __ldg(p.perm + (k == 0 ? 0 : M - k));
+    }
+    float2 za[kPw], zb[kPw];
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      za[u] = buf[pa[u]];
+      zb[u] = buf[pb[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      const int k = k0 + u * kS2sT;
+      if (k < kend) g(k, r2c_post_vals(za[u], zb[u], k, M, stw));
+    }
+  }
+}
+
 // Pointwise pass of a real round trip: Z is the DIF output of the length-M
 // complex FFT of a real row of length 2M. For every bin pair (k, M-k) the
 // thread forms the real-spectrum bins X[k], X[M-k] (X[M] for k = 0), maps
-// them through f(k, X) and writes back the pre-processed inverse input Z'
-// at the same digit-reversed points, ready for fft_dit(inverse).
-template <typename F>
-__device__ __forceinline__ void real_roundtrip_pointwise(float2* buf, const FftPlan& p,
-                                                         const float2* __restrict__ twn, F f) {
+// them through f(k, X, pre(k)) and writes back the pre-processed inverse
+// input Z' at the same digit-reversed points, ready for fft_dit(inverse).
+// pre(k) is a per-bin value (a table entry, a weight) loaded with the
+// batch's other reads. Each pair owns its two points, so a thread may read
+// kPw pairs before writing any.
+template <typename Pre, typename F>
+__device__ __forceinline__ void real_roundtrip_pointwise_pre(float2* buf, const FftPlan& p, const float2* stw,
+                                                             Pre pre, F f) {
   const int M = p.n;
-  for (int k = threadIdx.x; k <= M / 2; k += kS2sT) {
-    const int k2 = M - k;  // == M for k == 0
-    const int pk = __ldg(p.perm + k);
-    const int pk2 = (k == 0) ? pk : __ldg(p.perm + k2);
-    const float2 zk = buf[pk];
-    const float2 zk2 = buf[pk2];
-    // forward post-processing (r2c_post with Z[M] == Z[0])
-    auto post = [&](float2 za, float2 zb, int kk) {
-      const float2 zc = conjf2(zb);
-      const float2 xe = make_float2(0.5f * (za.x + zc.x), 0.5f * (za.y + zc.y));
-      const float2 d = make_float2(0.5f * (za.x - zc.x), 0.5f * (za.y - zc.y));
-      const float2 w = (kk == M) ? make_float2(-1.f, 0.f) : __ldg(twn + kk);
-      return cadd(xe, cmul(w, mul_mi(d)));
-    };
-    float2 Xk = post(zk, zk2, k);
-    float2 Xk2 = (k == 0) ? post(zk, zk, M) : post(zk2, zk, k2);
-    Xk = f(k, Xk);
-    Xk2 = f(k2, Xk2);
-    if (k == 0) {
-      // Z'[0] from Y[0], Y[M] (imaginary parts of DC / Nyquist ignored)
-      buf[pk] = c2r_pre_vals(make_float2(Xk.x, 0.f), make_float2(Xk2.x, 0.f), 0, twn);
-    } else if (k == k2) {
-      buf[pk] = c2r_pre_vals(Xk, Xk, k, twn);
-    } else {
-      buf[pk] = c2r_pre_vals(Xk, Xk2, k, twn);
-      buf[pk2] = c2r_pre_vals(Xk2, Xk, k2, twn);
+  const int H = M / 2;
+  for (int k0 = threadIdx.x; k0 <= H; k0 += kPw * kS2sT) {
+    int pk[kPw], pk2[kPw];
+    decltype(pre(0)) va[kPw], vb[kPw];
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      const int k = min(k0 + u * kS2sT, H);
+      pk[u] = __ldg(p.perm + k);
+      pk2[u] = __ldg(p.perm + (k == 0 ? 0 : M - k));  // k == 0: X[M] comes from Z[0] too
+      va[u] = pre(k);
+      vb[u] = pre(M - k);
+    }
+    float2 zk[kPw], zk2[kPw];
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      zk[u] = buf[pk[u]];
+      zk2[u] = buf[pk2[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      const int k = k0 + u * kS2sT;
+      if (k > H) continue;
+      const int k2 = M - k;  // == M for k == 0
+      float2 Xk = r2c_post_vals(zk[u], zk2[u], k, M, stw);
+      float2 Xk2 = (k == 0) ? r2c_post_vals(zk[u], zk[u], M, M, stw) : r2c_post_vals(zk2[u], zk[u], k2, M, stw);
+      Xk = f(k, Xk, va[u]);
+      Xk2 = f(k2, Xk2, vb[u]);
+      if (k == 0) {
+        // Z'[0] from Y[0], Y[M] (imaginary parts of DC / Nyquist ignored)
+        buf[pk[u]] = c2r_pre_w(make_float2(Xk.x, 0.f), make_float2(Xk2.x, 0.f), real_tw(stw, 0, M));
+      } else if (k == k2) {
+        buf[pk[u]] = c2r_pre_w(Xk, Xk, real_tw(stw, k, M));
+      } else {
+        buf[pk[u]] = c2r_pre_w(Xk, Xk2, real_tw(stw, k, M));
+        buf[pk2[u]] = c2r_pre_w(Xk2, Xk, real_tw(stw, k2, M));
+      }
     }
   }
+}
+
+// The prefilter's pointwise map (x dt, sanitize, x |H|^2), |H|^2 from resp.
+__device__ __forceinline__ void prefilter_pointwise(float2* buf, const FftPlan& p, const float2* stw, float dt,
+                                                    const float* __restrict__ resp) {
+  real_roundtrip_pointwise_pre(
+      buf, p, stw, [&](int k) { return __ldg(resp + k); },
+      [&](int, float2 X, float h) {
+        X = sanitize2(make_float2(X.x * dt, X.y * dt));
+        return make_float2(X.x * h, X.y * h);
+      });
 }
 
 // InvNormalize2DKernel weight: 1 / (width * dt) with width*dt in float.
@@ -222,37 +396,43 @@ __device__ __forceinline__ float2* after_row(float2* smraw, const RowBuf& rb, in
 // k_s2s_front: window load, preprocess, prefilter, one-bit / RAM weight
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kS2sT, 1)
-    k_s2s_front(const float* __restrict__ series, int64_t series_pitch, int64_t series_len,
-                const int* __restrict__ steps, S2sDev d, FftPlan pf, const float2* __restrict__ twf,
-                const float* __restrict__ resp, int mode, int raw_win, float* __restrict__ xout,
-                float* __restrict__ wout, RowBuf rb) {
-  // mode: 0 = write x only, 1 = one-bit, 2 = x and smoothed |x| weight
-  extern __shared__ float2 smraw[];
-  __shared__ double sred[32];
-  const int Mf = pf.n;
-  float2* sbuf = row_buffer(smraw, rb);
-  float2* stw = after_row(smraw, rb, Mf);
+// Window load, NaN/Inf -> 0 (isnan2DKernel), demean (rdc2DKernel), detrend
+// (rtr2DKernel), Hann end taper (timetaper2DKernel) and the prefilter round
+// trip (R2C(filter_nfft), x dt, sanitize, x |H|^2, C2R) of one row: on
+// return xs[0, seg) holds the unnormalised inverse (the caller applies
+// 1 / (filter_nfft dt)); stw holds the prefilter plan's twiddles. Samples
+// past the series are zero.
+__device__ __forceinline__ void s2s_front_row(float2* sbuf, float2* stw, const float* __restrict__ src,
+                                              int64_t start, int64_t series_len, const S2sDev& d,
+                                              const FftPlan& pf, const float* __restrict__ resp) {
+  __shared__ double sred[64];
   float* xs = reinterpret_cast<float*>(sbuf);
-  const int r = blockIdx.x;
-  const int sidx = r / d.nrows, row = r % d.nrows;
-  const int64_t start = (int64_t)steps[sidx] * d.shift;
-  const float* src = series + (int64_t)row * series_pitch + start;
+  const int Mf = pf.n;
   const int seg = d.seg;
   fft_twiddles_to_smem<kS2sT>(pf, stw);
-  // load + NaN/Inf -> 0 (isnan2DKernel); samples past the series are zero
   Kahan s1;
-  for (int i = threadIdx.x; i < 2 * Mf; i += kS2sT) {
-    float v = 0.f;
-    if (i < seg && start + i < series_len) {
-      v = src[i];
-      if (!isfinite(v)) v = 0.f;
+  batched_rows<8>(
+      seg, [&](int i) { return start + i < series_len ? src[i] : 0.f; },
+      [&](int i, float v) {
+        if (!isfinite(v)) v = 0.f;
+        xs[i] = v;
+        s1.add(v);
+      });
+  for (int i = seg + threadIdx.x; i < 2 * Mf; i += kS2sT) xs[i] = 0.f;
+  // demean: x -= sum/width
+  __shared__ float srow[4];
+  {
+    const float hi[1] = {s1.s}, lo[1] = {-s1.c};
+    double t[1];
+    block_sums_t0<1>(hi, lo, sred, t);
+    if (threadIdx.x == 0) {
+      const F2c m = f2c(t[0] / (double)seg);
+      srow[0] = m.hi;
+      srow[1] = m.lo;
     }
-    xs[i] = v;
-    if (i < seg) s1.add(v);
+    __syncthreads();
   }
-  // demean (rdc2DKernel): x -= sum/width
-  const F2c mean = f2c(block_sum_f64(s1.value(), sred) / (double)seg);
+  const F2c mean{srow[0], srow[1]};
   Kahan s2, si;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
     const float v = (xs[i] - mean.hi) - mean.lo;
@@ -260,20 +440,23 @@ __global__ void __launch_bounds__(kS2sT, 1)
     s2.add(v);
     si.add(v * (float)i);
   }
-  // detrend (rtr2DKernel): closed-form least squares
-  const double y2 = block_sum_f64(s2.value(), sred);
-  const double y1 = block_sum_f64(si.value(), sred);
-  const double a12 = 0.5 * seg * (seg - 1);
-  const double a11 = a12 * (2 * seg - 1) / 3.0;
-  const double a22 = seg;
-  const double det = a11 * a22 - a12 * a12;
-  const double ca = (a22 * y1 - a12 * y2) / det;
-  const double cb = (a11 * y2 - a12 * y1) / det;
+  // detrend: closed-form least squares (slope ca, intercept cb)
+  {
+    const float hi[2] = {s2.s, si.s}, lo[2] = {-s2.c, -si.c};
+    double t[2];
+    block_sums_t0<2>(hi, lo, sred, t);
+    if (threadIdx.x == 0) {
+      const double y2 = t[0], y1 = t[1];
+      srow[2] = (float)((d.a22 * y1 - d.a12 * y2) * d.inv_det);
+      srow[3] = (float)((d.a11 * y2 - d.a12 * y1) * d.inv_det);
+    }
+    __syncthreads();
+  }
   const int tap = d.taper;
-  const float caf = (float)ca, cbf = (float)cb, itap = 1.0f / (float)tap;
+  const float caf = srow[2], cbf = srow[3], itap = 1.0f / (float)tap;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
     const float v = xs[i] - fmaf(caf, (float)i, cbf);
-    // timetaper2DKernel: 0.5 (1 - cos(pi i / tap)) at both ends
+    // 0.5 (1 - cos(pi i / tap)) at both ends
     float fac = 1.0f;
     if (i < tap)
       fac = 0.5f * (1.0f - cospif((float)i * itap));
@@ -282,17 +465,29 @@ __global__ void __launch_bounds__(kS2sT, 1)
     xs[i] = v * fac;
   }
   __syncthreads();
-  // prefilter: R2C(filter_nfft), x dt, sanitize, x |H|^2, C2R
   fft_dif<kS2sT>(sbuf, pf, stw, false);
   const float dt = d.delta;
-  real_roundtrip_pointwise(sbuf, pf, twf, [&](int k, float2 X) {
-    X = sanitize2(make_float2(X.x * dt, X.y * dt));
-    const float h = __ldg(resp + k);
-    return make_float2(X.x * h, X.y * h);
-  });
+  prefilter_pointwise(sbuf, pf, stw, dt, resp);
   __syncthreads();
   fft_dit<kS2sT>(sbuf, pf, stw, true);
-  const F2c inrm = f2c(inv_norm(2 * Mf, dt));
+}
+
+__global__ void __launch_bounds__(kS2sT, 1)
+    k_s2s_front(const float* __restrict__ series, int64_t series_pitch, int64_t series_len,
+                const int* __restrict__ steps, S2sDev d, FftPlan pf, const float* __restrict__ resp, int mode,
+                int raw_win, float* __restrict__ xout, float* __restrict__ wout, RowBuf rb) {
+  // mode: 0 = write x only, 1 = one-bit, 2 = x and smoothed |x| weight
+  extern __shared__ float2 smraw[];
+  const int Mf = pf.n;
+  float2* sbuf = row_buffer(smraw, rb);
+  float2* stw = after_row(smraw, rb, Mf);
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int r = blockIdx.x;
+  const int sidx = r / d.nrows, row = r % d.nrows;
+  const int64_t start = (int64_t)steps[sidx] * d.shift;
+  const int seg = d.seg;
+  s2s_front_row(sbuf, stw, series + (int64_t)row * series_pitch + start, start, series_len, d, pf, resp);
+  const F2c inrm = d.inrm_f;
   float* xo = xout + (int64_t)r * seg;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
     float v = mul_f2c(xs[i], inrm);
@@ -303,7 +498,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
   if (mode == 2) {
     __syncthreads();
     float* wo = wout + (int64_t)r * seg;
-    boxcar_rows<true>(xs, seg, raw_win, [&](int c, float v) { wo[c] = v; });
+    boxcar_rows<true>(xs, seg, raw_win, d.inv_rw, [&](int c, float v) { wo[c] = v; });
   }
 }
 
@@ -312,8 +507,8 @@ __global__ void __launch_bounds__(kS2sT, 1)
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(kS2sT, 1)
-    k_s2s_mfband(const float* __restrict__ xin, S2sDev d, FftPlan pf, const float2* __restrict__ twf,
-                 const float* __restrict__ resp, int raw_win, float* __restrict__ xb,
+    k_s2s_mfband(const float* __restrict__ xin, S2sDev d, FftPlan pf, const float* __restrict__ resp, int raw_win,
+                 F2c inv_win, float* __restrict__ xb,
                  float* __restrict__ wb, RowBuf rb) {
   extern __shared__ float2 smraw[];
   const int Mf = pf.n;
@@ -324,18 +519,15 @@ __global__ void __launch_bounds__(kS2sT, 1)
   const int seg = d.seg;
   fft_twiddles_to_smem<kS2sT>(pf, stw);
   const float* xi = xin + (int64_t)r * seg;
-  for (int i = threadIdx.x; i < 2 * Mf; i += kS2sT) xs[i] = (i < seg) ? xi[i] : 0.f;
+  batched_rows<8>(seg, [&](int i) { return xi[i]; }, [&](int i, float v) { xs[i] = v; });
+  for (int i = seg + threadIdx.x; i < 2 * Mf; i += kS2sT) xs[i] = 0.f;
   __syncthreads();
   fft_dif<kS2sT>(sbuf, pf, stw, false);
   const float dt = d.delta;
-  real_roundtrip_pointwise(sbuf, pf, twf, [&](int k, float2 X) {
-    X = sanitize2(make_float2(X.x * dt, X.y * dt));
-    const float h = __ldg(resp + k);
-    return make_float2(X.x * h, X.y * h);
-  });
+  prefilter_pointwise(sbuf, pf, stw, dt, resp);
   __syncthreads();
   fft_dit<kS2sT>(sbuf, pf, stw, true);
-  const F2c inrm = f2c(inv_norm(2 * Mf, dt));
+  const F2c inrm = d.inrm_f;
   float* xo = xb + (int64_t)r * seg;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
     const float v = mul_f2c(xs[i], inrm);
@@ -344,7 +536,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
   }
   __syncthreads();
   float* wo = wb + (int64_t)r * seg;
-  boxcar_rows<true>(xs, seg, raw_win, [&](int c, float v) { wo[c] = v; });
+  boxcar_rows<true>(xs, seg, raw_win, inv_win, [&](int c, float v) { wo[c] = v; });
 }
 
 __global__ void k_s2s_mfsum(const float* __restrict__ xb, const float* __restrict__ wb, int nbands,
@@ -383,25 +575,22 @@ __global__ void __launch_bounds__(kS2sT, 1)
   const int seg = d.seg;
   fft_twiddles_to_smem<kS2sT>(ps, stw);
   const float* xi = xin + (int64_t)r * seg;
-  for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    float v = xi[i];
-    if (win_w) v = ram_divide(v, win_w, row0, seg, d.num_ch, i);
-    xs[i] = v;
-  }
+  batched_rows<4>(
+      seg, [&](int i) { return win_w ? ram_divide(xi[i], win_w, row0, seg, d.num_ch, i) : xi[i]; },
+      [&](int i, float v) { xs[i] = v; });
   __syncthreads();
   fft_dif<kS2sT>(sbuf, ps, stw, false);
   const int fw = Ms + 1;
   const float dt = d.delta;
   float2* Xo = Xout + (int64_t)r * fpitch;
-  for (int k = threadIdx.x; k < fw; k += kS2sT) {
-    float2 X = r2c_post(sbuf, ps.perm, Ms, k, tws);
+  r2c_post_bins(sbuf, ps, stw, fw, [&](int k, float2 X) {
     X = sanitize2(make_float2(X.x * dt, X.y * dt));
     Xo[k] = X;
     amp[k] = hypotf(X.x, X.y);
-  }
+  });
   __syncthreads();
   float* Ao = Aout + (int64_t)r * fpitch;
-  boxcar_rows<false>(amp, fw, ww, [&](int c, float v) { Ao[c] = v; });
+  boxcar_rows<false>(amp, fw, ww, d.inv_ww, [&](int c, float v) { Ao[c] = v; });
 }
 
 // ---------------------------------------------------------------------------
@@ -420,6 +609,21 @@ __device__ __forceinline__ float spec_taper_factor(int col, int width, const S2s
   return 1.f;
 }
 
+// One whitened bin (cdiv2DKernel after clampmin2DKernel, then the band
+// taper and sanitize): X / s for the station weight s (the float sum of the
+// components' smoothed amplitudes, clamped to MINVAL), times the taper.
+__device__ __forceinline__ float2 whiten_bin(float2 X, float s, int k, int width, const S2sDev& d) {
+  if (!isfinite(s) || s < kMinValF) s = kMinValF;  // clampmin2DKernel
+  // cdiv2DKernel's double compare against MINVAL, as in ram_divide
+  if (s < kMinValF) X = make_float2(0.f, 0.f);
+  else X = make_float2(X.x / s, X.y / s);
+  // (float)((double)x * f) of two floats is the correctly rounded float
+  // product: the double product is exact
+  const float f = spec_taper_factor(k, width, d);
+  X = make_float2(X.x * f, X.y * f);
+  return sanitize2(X);
+}
+
 __device__ __forceinline__ void output_transform(float2* sbuf, float* xs, int nvalid,
                                                  const FftPlan& po, const float2* twp,
                                                  float2* stw, const S2sDev& d,
@@ -432,8 +636,7 @@ __device__ __forceinline__ void output_transform(float2* sbuf, float* xs, int nv
   __syncthreads();
   fft_dif<kS2sT>(sbuf, po, stw, false);
   const float dt = d.delta;
-  for (int k = threadIdx.x; k < d.nspec; k += kS2sT) {
-    float2 X = r2c_post(sbuf, po.perm, Mo, k, twp);
+  r2c_post_bins(sbuf, po, stw, d.nspec, [&](int k, float2 X) {
     X = sanitize2(make_float2(X.x * dt, X.y * dt));
     if (d.phase_only) {
       // spectralOnebit2DKernel (hypotf, amp <= MINVAL -> 0), then sanitize
@@ -446,7 +649,7 @@ __device__ __forceinline__ void output_transform(float2* sbuf, float* xs, int nv
       }
     }
     out[k] = X;
-  }
+  });
 }
 
 __global__ void __launch_bounds__(kS2sT, 1)
@@ -468,33 +671,43 @@ __global__ void __launch_bounds__(kS2sT, 1)
   fft_twiddles_to_smem<kS2sT>(ps, stw);
   const float2* Xr = Xin + (int64_t)r * fpitch;
   // whitened, tapered, sanitised bins written as the C2R pre-processed input
-  // at the digit-reversed points of the length-Ms transform
-  auto wbin = [&](int k) -> float2 {
+  // at the digit-reversed points of the length-Ms transform; the reads of
+  // kPw bin pairs are issued before any is used
+  auto wsum = [&](int k) {
     float s = 0.f;
     for (int c = 0; c < d.num_ch; ++c) s += Ain[(row0 + c) * fpitch + k];
-    if (!isfinite(s) || s < kMinValF) s = kMinValF;  // clampmin2DKernel
-    float2 X = Xr[k];
-    if (s < kMinValF) X = make_float2(0.f, 0.f);  // cdiv2DKernel's double compare, as in ram_divide
-    else X = make_float2(X.x / s, X.y / s);
-    // (float)((double)x * f) of two floats is the correctly rounded float
-    // product: the double product is exact
-    const float f = spec_taper_factor(k, fw, d);
-    X = make_float2(X.x * f, X.y * f);
-    return sanitize2(X);
+    return s;
   };
-  for (int k = threadIdx.x; k < Ms; k += kS2sT) {
-    float2 a = wbin(k);
-    float2 b = wbin(Ms - k);
-    if (k == 0) {
-      a.y = 0.f;
-      b.y = 0.f;
+  for (int k0 = threadIdx.x; k0 < Ms; k0 += kPw * kS2sT) {
+    int pos[kPw];
+    float2 xa[kPw], xb[kPw];
+    float sa[kPw], sb[kPw];
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      const int k = min(k0 + u * kS2sT, Ms - 1);
+      pos[u] = __ldg(ps.perm + k);
+      xa[u] = Xr[k];
+      xb[u] = Xr[Ms - k];
+      sa[u] = wsum(k);
+      sb[u] = wsum(Ms - k);
     }
-    sbuf[__ldg(ps.perm + k)] = c2r_pre_vals(a, b, k, tws);
+#pragma unroll
+    for (int u = 0; u < kPw; ++u) {
+      const int k = k0 + u * kS2sT;
+      if (k >= Ms) continue;
+      float2 a = whiten_bin(xa[u], sa[u], k, fw, d);
+      float2 b = whiten_bin(xb[u], sb[u], Ms - k, fw, d);
+      if (k == 0) {
+        a.y = 0.f;
+        b.y = 0.f;
+      }
+      sbuf[pos[u]] = c2r_pre_w(a, b, real_tw(stw, k, Ms));
+    }
   }
   __syncthreads();
   fft_dit<kS2sT>(sbuf, ps, stw, true);
   const int seg = d.seg;
-  const F2c inrm = f2c(inv_norm(seg, d.delta));
+  const F2c inrm = d.inrm_s;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
     float v = mul_f2c(xs[i], inrm);
     if (to_time && time_mode == 1) v = (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f);
@@ -506,7 +719,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
     for (int i = threadIdx.x; i < seg; i += kS2sT) xo[i] = xs[i];
     if (time_mode == 2) {
       float* wo = wout + (int64_t)r * seg;
-      boxcar_rows<true>(xs, seg, raw_win, [&](int c, float v) { wo[c] = v; });
+      boxcar_rows<true>(xs, seg, raw_win, d.inv_rw, [&](int c, float v) { wo[c] = v; });
     }
     return;
   }
@@ -527,17 +740,214 @@ __global__ void __launch_bounds__(kS2sT, 1)
   const int64_t row0 = (int64_t)(r - row) + (row / d.num_ch) * d.num_ch;
   const int seg = d.seg;
   const float* xi = xin + (int64_t)r * seg;
-  for (int i = threadIdx.x; i < seg; i += kS2sT) {
-    float v = xi[i];
-    if (win_w) v = ram_divide(v, win_w, row0, seg, d.num_ch, i);
-    xs[i] = v;
-  }
+  batched_rows<4>(
+      seg, [&](int i) { return win_w ? ram_divide(xi[i], win_w, row0, seg, d.num_ch, i) : xi[i]; },
+      [&](int i, float v) { xs[i] = v; });
   output_transform(sbuf, xs, seg, po, two, stw, d, out + (int64_t)r * out_pitch);
+}
+
+// ---------------------------------------------------------------------------
+// k_s2s_station: the whole chain for the three components of a station
+// window, one 3-CTA thread-block cluster per station window
+// ---------------------------------------------------------------------------
+//
+// Used for three components with RAM / one-bit / no normalisation and
+// whitening after normalisation (or none), when a row, the twiddles and the
+// exchange buffer fit one CTA's shared memory. The components' coupling --
+// the station RAM weight (the sum of the three smoothed |x|) and the
+// station whitening weight (the sum of the three smoothed |X|) -- goes
+// through distributed shared memory: each CTA keeps its component's values
+// in its own `aux` buffer and reads the two others' at the same index, in
+// component order. Rows never leave shared memory between the window load
+// and the spectrum store.
+//
+// RAM weights cover seg samples, more than `aux` holds next to the row, so
+// they go in chunks of aux_floats outputs: a chunk's weights need the
+// undivided |x| up to half a window past its end, so the last half window
+// of each chunk is divided only after the next chunk's weights are formed
+// (its station weights wait in `side`). The whitening amplitudes (seg/2 + 1
+// bins) fit `aux` whole; each thread smooths its run of bins in registers
+// and writes it back in place.
+//
+// Every cluster barrier below is reached unconditionally or under a
+// condition uniform over the grid (the mode and plan), so the three CTAs
+// always meet at the same barriers.
+
+constexpr int kStationCtas = 3;
+constexpr int kFusedRunMax = 21;      // smoothed-amplitude run per thread (bins <= 21 x 1024)
+constexpr int kFusedSideMax = 2048;   // half RAM window held between chunks (samples)
+
+struct S2sFused {
+  int mode;        // 0 = none, 1 = one-bit, 2 = RAM
+  int whiten;      // 1: whitening after the normalisation
+  int raw_win;     // RAM boxcar width
+  int ww;          // whitening boxcar width
+  int aux_floats;  // exchange buffer (floats): a RAM chunk, or the whitening bins
+  int twmax;       // twiddle table elements (largest of the plans)
+  int mbuf;        // row buffer (complex elements)
+};
+
+__global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
+    k_s2s_station(const float* __restrict__ series, int64_t series_pitch, int64_t series_len,
+                  const int* __restrict__ steps, S2sDev d, FftPlan pf, FftPlan ps, FftPlan po,
+                  const float* __restrict__ resp, S2sFused fz, float2* __restrict__ out, int64_t out_pitch) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ float2 smraw[];
+  float2* sbuf = smraw;
+  float2* stw = smraw + fz.mbuf;
+  float* aux = reinterpret_cast<float*>(stw + fz.twmax);
+  float* side = aux + fz.aux_floats;
+  float* xs = reinterpret_cast<float*>(sbuf);
+  const int rank = (int)cl.block_rank();
+  const float* peer[kStationCtas];
+#pragma unroll
+  for (int c = 0; c < kStationCtas; ++c) peer[c] = c == rank ? aux : cl.map_shared_rank(aux, c);
+  const int r = blockIdx.x;
+  const int sidx = r / d.nrows, row = r % d.nrows;
+  const int64_t start = (int64_t)steps[sidx] * d.shift;
+  const int seg = d.seg;
+  const float dt = d.delta;
+
+  // window load, preprocessing, prefilter
+  s2s_front_row(sbuf, stw, series + (int64_t)row * series_pitch + start, start, series_len, d, pf, resp);
+  {
+    const F2c inrm = d.inrm_f;
+    for (int i = threadIdx.x; i < seg; i += kS2sT) {
+      float v = mul_f2c(xs[i], inrm);
+      if (fz.mode == 1) v = (v > 0.f) ? 1.f : ((v < 0.f) ? -1.f : 0.f);
+      xs[i] = v;
+    }
+    __syncthreads();
+  }
+
+  // RAM: station weight = sum of the components' smoothed |x|
+  if (fz.mode == 2) {
+    const int win = fz.raw_win, half = win / 2;
+    const int L = fz.aux_floats;
+    int prev_tail = 0;
+    for (int lo = 0; lo < seg; lo += L) {
+      const int hi = min(seg, lo + L);
+      boxcar_range<true>(xs, seg, win, d.inv_rw, lo, hi, [&](int c, float v) { aux[c - lo] = v; });
+      cl.sync();  // the three components' weights of [lo, hi) are in place
+      // the previous chunk's last half window, now that this chunk's
+      // weights have read it
+      for (int i = threadIdx.x; i < prev_tail; i += kS2sT) {
+        const int c = lo - prev_tail + i;
+        xs[c] = ram_divide_s(xs[c], side[i]);
+      }
+      __syncthreads();
+      const int tail = hi == seg ? 0 : min(half, hi - lo);
+      batched_rows<4>(
+          hi - lo, [&](int i) { return peer[0][i] + peer[1][i] + peer[2][i]; },
+          [&](int i, float sw) {
+            if (i < hi - lo - tail)
+              xs[lo + i] = ram_divide_s(xs[lo + i], sw);
+            else
+              side[i - (hi - lo - tail)] = sw;
+          });
+      prev_tail = tail;
+      cl.sync();  // every component done reading this chunk's weights
+    }
+  }
+
+  // whitening: X / (sum of the components' smoothed |X|), band taper
+  if (fz.whiten) {
+    fft_twiddles_to_smem<kS2sT>(ps, stw);
+    __syncthreads();
+    fft_dif<kS2sT>(sbuf, ps, stw, false);
+    const int fw = ps.n + 1;
+    r2c_post_bins(sbuf, ps, stw, fw, [&](int k, float2 X) {
+      X = sanitize2(make_float2(X.x * dt, X.y * dt));
+      aux[k] = hypotf(X.x, X.y);
+    });
+    __syncthreads();
+    boxcar_inplace<kFusedRunMax>(aux, fw, fz.ww, d.inv_ww);
+    cl.sync();  // the three components' smoothed amplitudes are in place
+    real_roundtrip_pointwise_pre(
+        sbuf, ps, stw, [&](int k) { return peer[0][k] + peer[1][k] + peer[2][k]; },
+        [&](int k, float2 X, float sw) {
+          X = sanitize2(make_float2(X.x * dt, X.y * dt));
+          return whiten_bin(X, sw, k, fw, d);
+        });
+    cl.sync();  // every component done reading the amplitudes
+    fft_dit<kS2sT>(sbuf, ps, stw, true);
+    const F2c inrm = d.inrm_s;
+    for (int i = threadIdx.x; i < seg; i += kS2sT) xs[i] = mul_f2c(xs[i], inrm);
+  }
+  output_transform(sbuf, xs, seg, po, nullptr, stw, d, out + (int64_t)r * out_pitch);
 }
 
 // ---------------------------------------------------------------------------
 // host
 // ---------------------------------------------------------------------------
+
+// The fused chain (k_s2s_station) for this call, or FXC_ERR_UNSUPPORTED
+// when it does not apply: not selected (FXC_S2S_FUSED=1 in the environment
+// selects it: at 0.1 s and 18 000-bin spectra it measured slower than the
+// kernel chain, its distributed-shared-memory reads and the L1 left next to
+// 220 KB of shared memory costing more than the global round trips it
+// saves), other than three components, RUN-ABS-MF, whitening before the
+// normalisation, or rows or exchange buffers beyond one CTA's shared memory.
+static int s2s_run_fused(fxc_ctx* ctx, const fxc_s2s_plan* plan, const S2sDev& d, const FftPlan& pf,
+                         const FftPlan& ps, const FftPlan& po, const float* d_series, int64_t series_pitch,
+                         int64_t series_len, const int32_t* h_steps, int32_t nsteps, int64_t nr, int32_t num_ch,
+                         const float* d_responses, float* d_out, int64_t out_pitch) {
+  const char* env = getenv("FXC_S2S_FUSED");
+  if (!env || env[0] != '1') return FXC_ERR_UNSUPPORTED;
+  if (num_ch != kStationCtas) return FXC_ERR_UNSUPPORTED;
+  S2sFused fz{};
+  switch (plan->normalize) {
+    case 0: fz.mode = 0; break;
+    case 2: fz.mode = 1; break;
+    case 3: fz.mode = 2; break;
+    default: return FXC_ERR_UNSUPPORTED;
+  }
+  if (plan->whiten != 0 && plan->whiten != 2) return FXC_ERR_UNSUPPORTED;
+  fz.whiten = plan->whiten == 2;
+  fz.raw_win = std::max(plan->runabs_win, 1);
+  fz.ww = std::max(plan->whiten_win, 1);
+  fz.mbuf = std::max(pf.n, po.n);
+  fz.twmax = std::max(fft_tw_smem_elems(pf), fft_tw_smem_elems(po));
+  if (fz.whiten) {
+    fz.mbuf = std::max(fz.mbuf, ps.n);
+    fz.twmax = std::max(fz.twmax, fft_tw_smem_elems(ps));
+  }
+  const int half = fz.mode == 2 ? fz.raw_win / 2 : 0;
+  if (half > kFusedSideMax) return FXC_ERR_UNSUPPORTED;
+  const int side = (half + 3) / 4 * 4;
+  cudaFuncAttributes attr;
+  FXC_CUDA_TRY(cudaFuncGetAttributes(&attr, k_s2s_station));
+  const int64_t budget = 227 * 1024 - (int64_t)attr.sharedSizeBytes;
+  const int64_t fixed = 8 * (int64_t)fz.mbuf + 8 * (int64_t)fz.twmax + 4 * (int64_t)side;
+  const int64_t aux = (budget - fixed) / 16 * 4;
+  if (aux < 4) return FXC_ERR_UNSUPPORTED;
+  fz.aux_floats = (int)aux;
+  if (fz.whiten && (ps.n + 1 > fz.aux_floats || ps.n + 1 > kFusedRunMax * kS2sT)) return FXC_ERR_UNSUPPORTED;
+  if (fz.mode == 2 && fz.aux_floats <= half) return FXC_ERR_UNSUPPORTED;
+  const size_t smem = (size_t)(fixed + 4 * aux);
+  FXC_CUDA_TRY(cudaFuncSetAttribute(k_s2s_station, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)kStationCtas);
+    cfg.blockDim = dim3((unsigned)kS2sT);
+    cfg.dynamicSmemBytes = smem;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_s2s_station, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      return FXC_ERR_UNSUPPORTED;
+    }
+  }
+  FXC_TRY(ctx->scratch4.reserve(sizeof(int) * (size_t)nsteps));
+  int* d_steps = reinterpret_cast<int*>(ctx->scratch4.ptr);
+  FXC_CUDA_TRY(cudaMemcpyAsync(d_steps, h_steps, sizeof(int) * nsteps, cudaMemcpyHostToDevice, ctx->stream));
+  k_s2s_station<<<(unsigned)nr, kS2sT, smem, ctx->stream>>>(d_series, series_pitch, series_len, d_steps, d, pf, ps,
+                                                            po, d_responses, fz, reinterpret_cast<float2*>(d_out),
+                                                            out_pitch);
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
 
 static int make_real_plan(int n, FftPlan* p, const float2** tw) {
   FXC_CHECK_ARG(n % 2 == 0 && n / 2 <= 65536, "real transform length %d not supported (must be even and "
@@ -748,6 +1158,22 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   d.phase_only = plan->phase_only;
   d.num_ch = num_ch;
   d.nrows = nrows;
+  d.inrm_f = f2c(inv_norm(plan->filter_nfft, plan->delta));
+  d.inrm_s = f2c(inv_norm(seg, plan->delta));
+  d.inv_rw = f2c(1.0 / (double)std::max(plan->runabs_win, 1));
+  d.inv_ww = f2c(1.0 / (double)std::max(plan->whiten_win, 1));
+  d.a12 = 0.5 * seg * (seg - 1.0);
+  d.a11 = d.a12 * (2.0 * seg - 1.0) / 3.0;
+  d.a22 = seg;
+  d.inv_det = 1.0 / (d.a11 * d.a22 - d.a12 * d.a12);
+
+  // one 3-CTA cluster per station window where the plan allows it
+  {
+    int rc = s2s_run_fused(ctx, plan, d, pf, ps, po, d_series, series_pitch, series_len, h_steps, nsteps, nr,
+                           num_ch, d_responses, d_out, out_pitch);
+    if (rc != FXC_ERR_UNSUPPORTED) return rc;
+    clear_error();
+  }
 
   const int nbands = plan->normalize == 1 ? plan->nfilters - 1 : 0;
   const int64_t fpitch = (int64_t)(seg / 2 + 1 + 3) / 4 * 4;
@@ -822,7 +1248,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
   }
   FXC_TRY(set_smem_limit(k_s2s_front, smf));
   k_s2s_front<<<(unsigned)nr, kS2sT, smf, ctx->stream>>>(d_series, series_pitch, series_len,
-                                                         d_steps, d, pf, twf, resp0, mode,
+                                                         d_steps, d, pf, resp0, mode,
                                                          plan->runabs_win, x, w, rb_of(smf_));
   count_launch();
   FXC_LAUNCH_CHECK();
@@ -854,7 +1280,7 @@ int fxc_s2s_run(fxc_ctx* ctx, const fxc_s2s_plan* plan, const float* d_series, i
       int win = 2 * (int)(1.0 / (double)(fl * plan->delta)) + 1;
       if (win < 1) win = 1;
       k_s2s_mfband<<<(unsigned)nr, kS2sT, smf, ctx->stream>>>(
-          x, d, pf, twf, resp0 + (size_t)(b + 1) * rpitch, win, xb + (size_t)b * nr * seg,
+          x, d, pf, resp0 + (size_t)(b + 1) * rpitch, win, f2c(1.0 / (double)win), xb + (size_t)b * nr * seg,
           wb + (size_t)b * nr * seg, rb_of(smf_));
       count_launch();
       FXC_LAUNCH_CHECK();

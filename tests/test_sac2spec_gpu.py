@@ -174,3 +174,44 @@ def test_sac2spec_detrend_large_offset_and_trend(ctx, torch_cuda, offset, trend)
     err = row_err(got, ref)
     print("large offset / trend rel err", err.max())
     assert err.max() < 1e-5, err
+
+
+@pytest.mark.parametrize("filter_file,delta,whiten,normalize", [
+    ("filter_d0.1_0.1-2.txt", 0.1, so.WHITEN_AFTER, so.NORM_RUNABS),
+    ("filter_d0.1_0.1-2.txt", 0.1, so.WHITEN_NONE, so.NORM_RUNABS),
+    ("filter_d0.1_0.1-2.txt", 0.1, so.WHITEN_AFTER, so.NORM_ONEBIT),
+    ("filter_d0.1_0.1-2.txt", 0.1, so.WHITEN_NONE, so.NORM_NONE),
+    ("filter_d0.2_0.1-1_0.5-2.txt", 0.2, so.WHITEN_AFTER, so.NORM_RUNABS),
+])
+def test_station_cluster_kernel_matches_three_kernel_path(ctx, torch_cuda, monkeypatch, filter_file, delta, whiten,
+                                                          normalize):
+    """Three components per station run as one 3-CTA cluster (k_s2s_station,
+    one launch) whose CTAs exchange the RAM and whitening weights through
+    distributed shared memory (selected by FXC_S2S_FUSED=1); the same call
+    with FXC_S2S_FUSED=0 runs the kernel chain that passes rows and weights
+    through global memory. Both
+    against the FP64 oracle, and against each other within 1e-6 (the RAM
+    weights are chunked in the cluster kernel, the whitening weight is the
+    same float sum in both). One-bit rows can flip within FP32 rounding of
+    zero: 1e-3 there, as in the mode tests."""
+    torch = torch_cuda
+    from fastxc_gb300._lib import lib
+
+    # step 5 holds a partial gap on one component: well conditioned for RAM,
+    # not for one-bit (see test_sac2spec_modes_match_oracle)
+    steps = [0, 13, 23] if normalize == so.NORM_ONEBIT else [0, 5, 13]
+    monkeypatch.setenv("FXC_S2S_FUSED", "1")
+    lib().fxc_launch_count_reset()
+    fused, ref = run_case(ctx, torch, filter_file, delta, whiten, normalize, 0, steps, nsta=3)
+    n_fused = lib().fxc_launch_count()
+    monkeypatch.setenv("FXC_S2S_FUSED", "0")
+    lib().fxc_launch_count_reset()
+    chain, _ = run_case(ctx, torch, filter_file, delta, whiten, normalize, 0, steps, nsta=3)
+    n_chain = lib().fxc_launch_count()
+    assert n_fused == 1 and n_chain >= 2, (n_fused, n_chain)
+    onebit = normalize == so.NORM_ONEBIT
+    for got in (fused, chain):
+        assert row_err(got, ref).max() < (1e-3 if onebit else 1e-5)
+    e = row_err(fused, chain)
+    print("cluster kernel vs kernel chain, row errors", np.array2string(e, precision=2))
+    assert e.max() < (1e-3 if onebit else 1e-6), e
