@@ -358,12 +358,19 @@ __device__ __forceinline__ void dft_any(float2 (&x)[R]) {
 // Stage twiddles w^k (k < n*tw_stride) come from a two-level table in shared
 // memory: w^k = coarse[k >> 8] * fine[k & 255], both entries of the global
 // table copied by fft_twiddles_to_smem (about 3 KB for the longest rows).
+// The fine table keeps one unused slot after every 16 entries: a stage reads
+// fine[(j * step) & 255] across the lanes' j, and for steps of 16 (or 32 x an
+// odd factor) the unpadded entries fall 16 (or 8) to a shared-memory bank;
+// padded, they land on distinct banks.
 constexpr int kTwFineShift = 8;
 constexpr int kTwFine = 1 << kTwFineShift;
+constexpr int kTwFinePadded = kTwFine + kTwFine / 16;
+
+__host__ __device__ inline int tw_fine_slot(int i) { return i + (i >> 4); }
 
 __host__ __device__ inline int fft_tw_smem_elems(const FftPlan& p) {
   const int nt = p.n * p.tw_stride;
-  return kTwFine + (nt - 1) / kTwFine + 1;
+  return kTwFinePadded + (nt - 1) / kTwFine + 1;
 }
 
 // All T threads copy; the caller synchronises before the first stage.
@@ -371,13 +378,13 @@ template <int T>
 __device__ __forceinline__ void fft_twiddles_to_smem(const FftPlan& p, float2* stw) {
   const int nt = p.n * p.tw_stride;
   for (int i = threadIdx.x; i < kTwFine; i += T)
-    stw[i] = i < nt ? __ldg(p.tw + i) : make_float2(1.f, 0.f);
+    stw[tw_fine_slot(i)] = i < nt ? __ldg(p.tw + i) : make_float2(1.f, 0.f);
   const int nc = (nt - 1) / kTwFine + 1;
-  for (int h = threadIdx.x; h < nc; h += T) stw[kTwFine + h] = __ldg(p.tw + h * kTwFine);
+  for (int h = threadIdx.x; h < nc; h += T) stw[kTwFinePadded + h] = __ldg(p.tw + h * kTwFine);
 }
 
 __device__ __forceinline__ float2 tw_lookup(const float2* stw, int k) {
-  return cmul(stw[kTwFine + (k >> kTwFineShift)], stw[k & (kTwFine - 1)]);
+  return cmul(stw[kTwFinePadded + (k >> kTwFineShift)], stw[tw_fine_slot(k & (kTwFine - 1))]);
 }
 
 // x[t] *= w^(t*jt), t = 1..R-1: a table lookup for t = 1, 9, 17, ... and

@@ -27,9 +27,10 @@
 //                   C2R, then either the output transform or the time row
 //   k_s2s_output    [RAM divide] zero-pad, R2C(output_nfft), x dt,
 //                   sanitize, optional phase-only
-//   k_s2s_station   (opt-in) the whole chain for the three components of a
-//                   station window in one 3-CTA cluster, the weights
-//                   exchanged through distributed shared memory
+//   k_s2s_station   the whole chain for the three components of a station
+//                   window in one 3-CTA cluster, the weights exchanged
+//                   through distributed shared memory (used where it
+//                   applies; the kernels above otherwise)
 // Each thread issues the global loads of 4-8 items before using any, and
 // the pointwise passes read a batch of bin pairs before writing: one CTA per
 // SM leaves no other CTA to hide load latency.
@@ -156,74 +157,95 @@ __device__ __forceinline__ float2 sanitize2(float2 v) {
 
 // Centred boxcar of width win over src[0, n) (reference smoothRowsRollingKernel:
 // window [c - win/2, c - win/2 + win - 1] clipped to the row, divided by win)
-// for the outputs c in [a, b). Each thread owns a contiguous run of outputs
-// and slides a Kahan-compensated FP32 sum across it. ABS takes |src|.
-template <bool ABS, typename Store>
-__device__ __forceinline__ void boxcar_range(const float* src, int n, int win, F2c inv, int a, int b,
-                                             Store store) {
-  const int per = (b - a + kS2sT - 1) / kS2sT;
+// for the outputs c in [a, b), written to dst[c - a]. Each thread owns a
+// contiguous run of outputs and slides a Kahan-compensated FP32 sum across
+// it; the first window is summed in four interleaved compensated sums (four
+// independent dependency chains) and combined. Out of line: the caller's
+// live values stay out of the loop's registers. ABS takes |src|.
+__device__ __forceinline__ void kahan_add(float& s, float& comp, float v) {
+  const float y = v - comp;
+  const float t = s + y;
+  comp = (t - s) - y;
+  s = t;
+}
+
+// Runs of an odd length: the 32 lanes of a warp then start 32 distinct
+// shared-memory banks apart (an even run length folds them onto 16 or fewer
+// banks, a 4-way conflict for a run of 36 on every window read).
+__device__ __forceinline__ int odd_run(int n) { return ((n + kS2sT - 1) / kS2sT) | 1; }
+
+template <bool ABS>
+__device__ __noinline__ void boxcar_range(const float* src, int n, int win, F2c inv, int a, int b, float* dst) {
+  const int per = odd_run(b - a);
   const int c0 = a + threadIdx.x * per;
   if (c0 >= b) return;
   const int c1 = min(b, c0 + per);
   const int half = win / 2;
+  const int lo = max(0, c0 - half), hi = min(n - 1, c0 - half + win - 1);
+  float s4[4] = {0.f, 0.f, 0.f, 0.f}, k4[4] = {0.f, 0.f, 0.f, 0.f};
+  int j = lo;
+  for (; j + 3 <= hi; j += 4) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) kahan_add(s4[q], k4[q], ABS ? fabsf(src[j + q]) : src[j + q]);
+  }
+  for (; j <= hi; ++j) kahan_add(s4[0], k4[0], ABS ? fabsf(src[j]) : src[j]);
   float s = 0.f, comp = 0.f;
-  auto kadd = [&](float v) {
-    const float y = v - comp;
-    const float t = s + y;
-    comp = (t - s) - y;
-    s = t;
-  };
-  int lo = max(0, c0 - half), hi = min(n - 1, c0 - half + win - 1);
-  for (int j = lo; j <= hi; ++j) kadd(ABS ? fabsf(src[j]) : src[j]);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    kahan_add(s, comp, s4[q]);
+    kahan_add(s, comp, -k4[q]);
+  }
   for (int c = c0; c < c1; ++c) {
-    store(c, mul_f2c(s, inv));
+    dst[c - a] = mul_f2c(s, inv);
     const int out = c - half;      // leaves the window
     const int in = c - half + win;  // enters the window
-    if (out >= 0 && out < n) kadd(-(ABS ? fabsf(src[out]) : src[out]));
-    if (in >= 0 && in < n) kadd(ABS ? fabsf(src[in]) : src[in]);
+    if (out >= 0 && out < n) kahan_add(s, comp, -(ABS ? fabsf(src[out]) : src[out]));
+    if (in >= 0 && in < n) kahan_add(s, comp, ABS ? fabsf(src[in]) : src[in]);
   }
-}
-
-template <bool ABS, typename Store>
-__device__ __forceinline__ void boxcar_rows(const float* src, int n, int win, F2c inv, Store store) {
-  boxcar_range<ABS>(src, n, win, inv, 0, n, store);
 }
 
 // The boxcar of a[0, n) (no abs) written back over a (n <= RMAX x threads):
 // each thread keeps its run of outputs in registers until every thread has
 // read its window, then stores it. Ends with the CTA synchronised.
+constexpr int kRunRegs = 21;  // boxcar_inplace run per thread (odd): n <= 21 x 1024
+
 template <int RMAX>
-__device__ __forceinline__ void boxcar_inplace(float* a, int n, int win, F2c inv) {
-  const int per = (n + kS2sT - 1) / kS2sT;
+__device__ __noinline__ void boxcar_inplace(float* a, int n, int win, F2c inv) {
+  const int per = odd_run(n);
   const int c0 = threadIdx.x * per;
   const int c1 = min(n, c0 + per);
   float r[RMAX];
   if (c0 < n) {
     const int half = win / 2;
-    float s = 0.f, comp = 0.f;
-    auto kadd = [&](float v) {
-      const float y = v - comp;
-      const float t = s + y;
-      comp = (t - s) - y;
-      s = t;
-    };
     const int lo = max(0, c0 - half), hi = min(n - 1, c0 - half + win - 1);
-    for (int j = lo; j <= hi; ++j) kadd(a[j]);
+    float s4[4] = {0.f, 0.f, 0.f, 0.f}, k4[4] = {0.f, 0.f, 0.f, 0.f};
+    int j = lo;
+    for (; j + 3 <= hi; j += 4) {
 #pragma unroll
-    for (int j = 0; j < RMAX; ++j) {
-      const int c = c0 + j;
+      for (int q = 0; q < 4; ++q) kahan_add(s4[q], k4[q], a[j + q]);
+    }
+    for (; j <= hi; ++j) kahan_add(s4[0], k4[0], a[j]);
+    float s = 0.f, comp = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      kahan_add(s, comp, s4[q]);
+      kahan_add(s, comp, -k4[q]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < RMAX; ++jj) {
+      const int c = c0 + jj;
       if (c < c1) {
-        r[j] = mul_f2c(s, inv);
+        r[jj] = mul_f2c(s, inv);
         const int out = c - half, in = c - half + win;
-        if (out >= 0 && out < n) kadd(-a[out]);
-        if (in >= 0 && in < n) kadd(a[in]);
+        if (out >= 0 && out < n) kahan_add(s, comp, -a[out]);
+        if (in >= 0 && in < n) kahan_add(s, comp, a[in]);
       }
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int j = 0; j < RMAX; ++j)
-    if (c0 + j < c1) a[c0 + j] = r[j];
+  for (int jj = 0; jj < RMAX; ++jj)
+    if (c0 + jj < c1) a[c0 + jj] = r[jj];
   __syncthreads();
 }
 
@@ -498,7 +520,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
   if (mode == 2) {
     __syncthreads();
     float* wo = wout + (int64_t)r * seg;
-    boxcar_rows<true>(xs, seg, raw_win, d.inv_rw, [&](int c, float v) { wo[c] = v; });
+    boxcar_range<true>(xs, seg, raw_win, d.inv_rw, 0, seg, wo);
   }
 }
 
@@ -536,7 +558,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
   }
   __syncthreads();
   float* wo = wb + (int64_t)r * seg;
-  boxcar_rows<true>(xs, seg, raw_win, inv_win, [&](int c, float v) { wo[c] = v; });
+  boxcar_range<true>(xs, seg, raw_win, inv_win, 0, seg, wo);
 }
 
 __global__ void k_s2s_mfsum(const float* __restrict__ xb, const float* __restrict__ wb, int nbands,
@@ -590,7 +612,13 @@ __global__ void __launch_bounds__(kS2sT, 1)
   });
   __syncthreads();
   float* Ao = Aout + (int64_t)r * fpitch;
-  boxcar_rows<false>(amp, fw, ww, d.inv_ww, [&](int c, float v) { Ao[c] = v; });
+  if (fw <= kRunRegs * kS2sT) {
+    // smoothed in place, then stored coalesced
+    boxcar_inplace<kRunRegs>(amp, fw, ww, d.inv_ww);
+    for (int k = threadIdx.x; k < fw; k += kS2sT) Ao[k] = amp[k];
+  } else {
+    boxcar_range<false>(amp, fw, ww, d.inv_ww, 0, fw, Ao);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -719,7 +747,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
     for (int i = threadIdx.x; i < seg; i += kS2sT) xo[i] = xs[i];
     if (time_mode == 2) {
       float* wo = wout + (int64_t)r * seg;
-      boxcar_rows<true>(xs, seg, raw_win, d.inv_rw, [&](int c, float v) { wo[c] = v; });
+      boxcar_range<true>(xs, seg, raw_win, d.inv_rw, 0, seg, wo);
     }
     return;
   }
@@ -774,7 +802,6 @@ __global__ void __launch_bounds__(kS2sT, 1)
 // always meet at the same barriers.
 
 constexpr int kStationCtas = 3;
-constexpr int kFusedRunMax = 21;      // smoothed-amplitude run per thread (bins <= 21 x 1024)
 constexpr int kFusedSideMax = 2048;   // half RAM window held between chunks (samples)
 
 struct S2sFused {
@@ -828,7 +855,7 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
     int prev_tail = 0;
     for (int lo = 0; lo < seg; lo += L) {
       const int hi = min(seg, lo + L);
-      boxcar_range<true>(xs, seg, win, d.inv_rw, lo, hi, [&](int c, float v) { aux[c - lo] = v; });
+      boxcar_range<true>(xs, seg, win, d.inv_rw, lo, hi, aux);
       cl.sync();  // the three components' weights of [lo, hi) are in place
       // the previous chunk's last half window, now that this chunk's
       // weights have read it
@@ -862,7 +889,7 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
       aux[k] = hypotf(X.x, X.y);
     });
     __syncthreads();
-    boxcar_inplace<kFusedRunMax>(aux, fw, fz.ww, d.inv_ww);
+    boxcar_inplace<kRunRegs>(aux, fw, fz.ww, d.inv_ww);
     cl.sync();  // the three components' smoothed amplitudes are in place
     real_roundtrip_pointwise_pre(
         sbuf, ps, stw, [&](int k) { return peer[0][k] + peer[1][k] + peer[2][k]; },
@@ -883,18 +910,16 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
 // ---------------------------------------------------------------------------
 
 // The fused chain (k_s2s_station) for this call, or FXC_ERR_UNSUPPORTED
-// when it does not apply: not selected (FXC_S2S_FUSED=1 in the environment
-// selects it: at 0.1 s and 18 000-bin spectra it measured slower than the
-// kernel chain, its distributed-shared-memory reads and the L1 left next to
-// 220 KB of shared memory costing more than the global round trips it
-// saves), other than three components, RUN-ABS-MF, whitening before the
-// normalisation, or rows or exchange buffers beyond one CTA's shared memory.
+// when it does not apply: other than three components, RUN-ABS-MF,
+// whitening before the normalisation, rows or exchange buffers beyond one
+// CTA's shared memory, or FXC_S2S_FUSED=0 in the environment (the kernel
+// chain instead).
 static int s2s_run_fused(fxc_ctx* ctx, const fxc_s2s_plan* plan, const S2sDev& d, const FftPlan& pf,
                          const FftPlan& ps, const FftPlan& po, const float* d_series, int64_t series_pitch,
                          int64_t series_len, const int32_t* h_steps, int32_t nsteps, int64_t nr, int32_t num_ch,
                          const float* d_responses, float* d_out, int64_t out_pitch) {
   const char* env = getenv("FXC_S2S_FUSED");
-  if (!env || env[0] != '1') return FXC_ERR_UNSUPPORTED;
+  if (env && env[0] == '0') return FXC_ERR_UNSUPPORTED;
   if (num_ch != kStationCtas) return FXC_ERR_UNSUPPORTED;
   S2sFused fz{};
   switch (plan->normalize) {
@@ -923,7 +948,7 @@ static int s2s_run_fused(fxc_ctx* ctx, const fxc_s2s_plan* plan, const S2sDev& d
   const int64_t aux = (budget - fixed) / 16 * 4;
   if (aux < 4) return FXC_ERR_UNSUPPORTED;
   fz.aux_floats = (int)aux;
-  if (fz.whiten && (ps.n + 1 > fz.aux_floats || ps.n + 1 > kFusedRunMax * kS2sT)) return FXC_ERR_UNSUPPORTED;
+  if (fz.whiten && (ps.n + 1 > fz.aux_floats || ps.n + 1 > kRunRegs * kS2sT)) return FXC_ERR_UNSUPPORTED;
   if (fz.mode == 2 && fz.aux_floats <= half) return FXC_ERR_UNSUPPORTED;
   const size_t smem = (size_t)(fixed + 4 * aux);
   FXC_CUDA_TRY(cudaFuncSetAttribute(k_s2s_station, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

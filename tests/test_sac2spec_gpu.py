@@ -187,9 +187,8 @@ def test_station_cluster_kernel_matches_three_kernel_path(ctx, torch_cuda, monke
                                                           normalize):
     """Three components per station run as one 3-CTA cluster (k_s2s_station,
     one launch) whose CTAs exchange the RAM and whitening weights through
-    distributed shared memory (selected by FXC_S2S_FUSED=1); the same call
-    with FXC_S2S_FUSED=0 runs the kernel chain that passes rows and weights
-    through global memory. Both
+    distributed shared memory; the same call with FXC_S2S_FUSED=0 runs the
+    kernel chain that passes rows and weights through global memory. Both
     against the FP64 oracle, and against each other within 1e-6 (the RAM
     weights are chunked in the cluster kernel, the whitening weight is the
     same float sum in both). One-bit rows can flip within FP32 rounding of
@@ -200,7 +199,7 @@ def test_station_cluster_kernel_matches_three_kernel_path(ctx, torch_cuda, monke
     # step 5 holds a partial gap on one component: well conditioned for RAM,
     # not for one-bit (see test_sac2spec_modes_match_oracle)
     steps = [0, 13, 23] if normalize == so.NORM_ONEBIT else [0, 5, 13]
-    monkeypatch.setenv("FXC_S2S_FUSED", "1")
+    monkeypatch.delenv("FXC_S2S_FUSED", raising=False)
     lib().fxc_launch_count_reset()
     fused, ref = run_case(ctx, torch, filter_file, delta, whiten, normalize, 0, steps, nsta=3)
     n_fused = lib().fxc_launch_count()
