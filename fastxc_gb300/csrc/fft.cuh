@@ -32,7 +32,17 @@ struct FftPlan {
   const float2* tw;          // tw[k] = exp(-2*pi*i*k/(n*tw_stride)), k < n*tw_stride
   int tw_stride;             // 1 for a plain complex table, 2 when the table is the real length
   const int* perm;           // perm[k] = point holding frequency k after fft_dif (n entries)
+  // b / L_s by a multiply-high: lmag[s] = floor(2^32 / L_s) + 1 for the
+  // sub-transform length L_s = n / (radix[0] ... radix[s]) of stage s (the
+  // same for the DIF and the DIT pass), exact for b, L_s below 2^16; 0 where
+  // L_s == 1. Formed on the host: a 64-bit division per thread and stage runs
+  // as FP64 instructions on the GPU.
+  uint32_t lmag[kFftMaxStages];
 };
+
+__host__ __device__ inline uint32_t fft_lmag(int L) {
+  return L > 1 ? (uint32_t)(0x100000000ull / (uint32_t)L) + 1u : 0u;
+}
 
 // Host side (fft_plan.cu). composites = false keeps to the prime radices
 // and 4, 8 (the row kernels of the stacking stages, whose shared dispatch
@@ -402,13 +412,12 @@ __device__ __forceinline__ void apply_twiddles(const float2* stw, int jt, float2
 }
 
 template <int R, int T, bool DIT>
-__device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float2* stw,
+__device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, uint32_t m, const float2* stw,
                                           int tw_step, bool conj_in, bool conj_out) {
   const int nb = n / R;
   const int B = L * R;
-  // b / L by a multiply-high with m = floor(2^32 / L) + 1 (exact for b, L
-  // below 2^16 as here); L == 1 has no twiddles
-  const uint32_t m = L > 1 ? (uint32_t)(0x100000000ull / (uint32_t)L) + 1u : 0u;
+  // b / L by a multiply-high with m = fft_lmag(L) (exact for b, L below
+  // 2^16 as here); L == 1 has no twiddles
   for (int b = threadIdx.x; b < nb; b += T) {
     const int blk = L > 1 ? (int)__umulhi((uint32_t)b, m) : b;
     const int j = b - blk * L;
@@ -430,33 +439,33 @@ __device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, const float
 
 template <int T, bool DIT, bool COMP = true>
 __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, const float2* stw,
-                                              int R, int L, int tw_step, bool ci, bool co) {
+                                              int R, int L, uint32_t m, int tw_step, bool ci, bool co) {
   if constexpr (COMP) {
     switch (R) {
-      case 6: fft_stage_ip<6, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
-      case 9: fft_stage_ip<9, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
-      case 10: fft_stage_ip<10, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
-      case 12: fft_stage_ip<12, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
-      case 14: fft_stage_ip<14, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
-      case 15: fft_stage_ip<15, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
-      case 21: fft_stage_ip<21, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); return;
+      case 6: fft_stage_ip<6, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
+      case 9: fft_stage_ip<9, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
+      case 10: fft_stage_ip<10, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
+      case 12: fft_stage_ip<12, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
+      case 14: fft_stage_ip<14, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
+      case 15: fft_stage_ip<15, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
+      case 21: fft_stage_ip<21, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
       default: break;
     }
   }
   switch (R) {
-    case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 8: fft_stage_ip<8, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 3: fft_stage_ip<3, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 5: fft_stage_ip<5, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 7: fft_stage_ip<7, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 11: fft_stage_ip<11, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 13: fft_stage_ip<13, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 17: fft_stage_ip<17, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 19: fft_stage_ip<19, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 23: fft_stage_ip<23, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 29: fft_stage_ip<29, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
-    case 31: fft_stage_ip<31, T, DIT>(buf, p.n, L, stw, tw_step, ci, co); break;
+    case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 8: fft_stage_ip<8, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 3: fft_stage_ip<3, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 5: fft_stage_ip<5, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 7: fft_stage_ip<7, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 11: fft_stage_ip<11, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 13: fft_stage_ip<13, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 17: fft_stage_ip<17, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 19: fft_stage_ip<19, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 23: fft_stage_ip<23, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 29: fft_stage_ip<29, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+    case 31: fft_stage_ip<31, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
     default: break;  // rejected by fft_make_plan
   }
 }
@@ -465,7 +474,7 @@ __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, con
 // after buf and the twiddle table stw (fft_twiddles_to_smem) are written and
 // the CTA synchronised; the result is visible to the CTA on return.
 template <int T, bool COMP = true>
-__device__ __noinline__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = p.n;
   int Rprod = 1;  // r_0 ... r_{s-1}
   for (int s = 0; s < p.nstages; ++s) {
@@ -473,23 +482,23 @@ __device__ __noinline__ void fft_dif(float2* buf, const FftPlan& p, const float2
     L /= R;
     // block length B = L*R = n / Rprod; twiddle w_B^{tj} = w_n^{t j Rprod}
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, false, COMP>(buf, p, stw, R, L, tw_step, inverse && s == 0,
-                            inverse && s == p.nstages - 1);
+    fft_run_stage<T, false, COMP>(buf, p, stw, R, L, p.lmag[s], tw_step, inverse && s == 0,
+                                  inverse && s == p.nstages - 1);
     Rprod *= R;
   }
 }
 
 // Digit-reversed input (the layout fft_dif produces), natural-order output.
 template <int T, bool COMP = true>
-__device__ __noinline__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = 1;
   int Rprod = p.n;
   for (int s = p.nstages - 1; s >= 0; --s) {
     const int R = p.radix[s];
     Rprod /= R;
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, true, COMP>(buf, p, stw, R, L, tw_step, inverse && s == p.nstages - 1,
-                           inverse && s == 0);
+    fft_run_stage<T, true, COMP>(buf, p, stw, R, L, p.lmag[s], tw_step, inverse && s == p.nstages - 1,
+                                 inverse && s == 0);
     L *= R;
   }
 }
@@ -507,6 +516,19 @@ __host__ __device__ inline int fft_digit_pos(const FftPlan& p, int k) {
     pos += d * L;
   }
   return pos;
+}
+
+// Out-of-line forms for kernels with many live values around their
+// transforms (the sac2spec row kernels): the call keeps the caller's values
+// out of the stage loops' registers. Kernels that run many short transforms
+// per CTA keep the inline forms.
+template <int T, bool COMP = true>
+__device__ __noinline__ void fft_dif_nl(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+  fft_dif<T, COMP>(buf, p, stw, inverse);
+}
+template <int T, bool COMP = true>
+__device__ __noinline__ void fft_dit_nl(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+  fft_dit<T, COMP>(buf, p, stw, inverse);
 }
 
 }  // namespace fxc

@@ -90,6 +90,20 @@ static bool factorize(int n, std::vector<int>* out, bool composites = true) {
   return true;
 }
 
+// Sub-transform lengths L_s = n / (radix[0] ... radix[s]) and their
+// multiply-high magic numbers.
+static void fill_lmag(FftPlan* p) {
+  int L = p->n;
+  for (int s = 0; s < kFftMaxStages; ++s) {
+    if (s < p->nstages) {
+      L /= p->radix[s];
+      p->lmag[s] = fft_lmag(L);
+    } else {
+      p->lmag[s] = 0;
+    }
+  }
+}
+
 bool fft_length_supported(int n) {
   std::vector<int> f;
   return factorize(n, &f);
@@ -105,6 +119,7 @@ int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out, bool com
   p.n = n;
   p.nstages = (int)f.size();
   for (int i = 0; i < p.nstages; ++i) p.radix[i] = f[i];
+  fill_lmag(&p);
   p.tw = tw;
   p.tw_stride = tw_stride;
   p.perm = nullptr;
@@ -123,6 +138,7 @@ int fft_make_plan_with(int n, const float2* tw, int tw_stride, const int* perm, 
   p.n = n;
   p.nstages = (int)f.size();
   for (int i = 0; i < p.nstages; ++i) p.radix[i] = f[i];
+  fill_lmag(&p);
   p.tw = tw;
   p.tw_stride = tw_stride;
   p.perm = perm;

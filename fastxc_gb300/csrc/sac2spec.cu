@@ -487,11 +487,11 @@ __device__ __forceinline__ void s2s_front_row(float2* sbuf, float2* stw, const f
     xs[i] = v * fac;
   }
   __syncthreads();
-  fft_dif<kS2sT>(sbuf, pf, stw, false);
+  fft_dif_nl<kS2sT>(sbuf, pf, stw, false);
   const float dt = d.delta;
   prefilter_pointwise(sbuf, pf, stw, dt, resp);
   __syncthreads();
-  fft_dit<kS2sT>(sbuf, pf, stw, true);
+  fft_dit_nl<kS2sT>(sbuf, pf, stw, true);
 }
 
 __global__ void __launch_bounds__(kS2sT, 1)
@@ -544,11 +544,11 @@ __global__ void __launch_bounds__(kS2sT, 1)
   batched_rows<8>(seg, [&](int i) { return xi[i]; }, [&](int i, float v) { xs[i] = v; });
   for (int i = seg + threadIdx.x; i < 2 * Mf; i += kS2sT) xs[i] = 0.f;
   __syncthreads();
-  fft_dif<kS2sT>(sbuf, pf, stw, false);
+  fft_dif_nl<kS2sT>(sbuf, pf, stw, false);
   const float dt = d.delta;
   prefilter_pointwise(sbuf, pf, stw, dt, resp);
   __syncthreads();
-  fft_dit<kS2sT>(sbuf, pf, stw, true);
+  fft_dit_nl<kS2sT>(sbuf, pf, stw, true);
   const F2c inrm = d.inrm_f;
   float* xo = xb + (int64_t)r * seg;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
       seg, [&](int i) { return win_w ? ram_divide(xi[i], win_w, row0, seg, d.num_ch, i) : xi[i]; },
       [&](int i, float v) { xs[i] = v; });
   __syncthreads();
-  fft_dif<kS2sT>(sbuf, ps, stw, false);
+  fft_dif_nl<kS2sT>(sbuf, ps, stw, false);
   const int fw = Ms + 1;
   const float dt = d.delta;
   float2* Xo = Xout + (int64_t)r * fpitch;
@@ -662,7 +662,7 @@ __device__ __forceinline__ void output_transform(float2* sbuf, float* xs, int nv
   __syncthreads();
   fft_twiddles_to_smem<kS2sT>(po, stw);
   __syncthreads();
-  fft_dif<kS2sT>(sbuf, po, stw, false);
+  fft_dif_nl<kS2sT>(sbuf, po, stw, false);
   const float dt = d.delta;
   r2c_post_bins(sbuf, po, stw, d.nspec, [&](int k, float2 X) {
     X = sanitize2(make_float2(X.x * dt, X.y * dt));
@@ -733,7 +733,7 @@ __global__ void __launch_bounds__(kS2sT, 1)
     }
   }
   __syncthreads();
-  fft_dit<kS2sT>(sbuf, ps, stw, true);
+  fft_dit_nl<kS2sT>(sbuf, ps, stw, true);
   const int seg = d.seg;
   const F2c inrm = d.inrm_s;
   for (int i = threadIdx.x; i < seg; i += kS2sT) {
@@ -882,7 +882,7 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
   if (fz.whiten) {
     fft_twiddles_to_smem<kS2sT>(ps, stw);
     __syncthreads();
-    fft_dif<kS2sT>(sbuf, ps, stw, false);
+    fft_dif_nl<kS2sT>(sbuf, ps, stw, false);
     const int fw = ps.n + 1;
     r2c_post_bins(sbuf, ps, stw, fw, [&](int k, float2 X) {
       X = sanitize2(make_float2(X.x * dt, X.y * dt));
@@ -898,7 +898,7 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
           return whiten_bin(X, sw, k, fw, d);
         });
     cl.sync();  // every component done reading the amplitudes
-    fft_dit<kS2sT>(sbuf, ps, stw, true);
+    fft_dit_nl<kS2sT>(sbuf, ps, stw, true);
     const F2c inrm = d.inrm_s;
     for (int i = threadIdx.x; i < seg; i += kS2sT) xs[i] = mul_f2c(xs[i], inrm);
   }
