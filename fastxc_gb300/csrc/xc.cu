@@ -752,9 +752,20 @@ int fxc_xc_run(fxc_ctx* ctx, const fxc_pairplan* plan, const float* d_spec, int6
   FXC_CHECK_ARG(plan != nullptr && shape != nullptr, "null plan or shape");
   if (plan->npairs == 0) return FXC_OK;
   if (method == FXC_XC_TENSOR && plan->tensor) {
-    // pack, then contraction + finalize without a [pair][bin] stack
     FXC_CHECK_ARG(nchan == plan->nchan && nwin >= 0 && spec_pitch >= shape->nspec && d_spec && d_ncf,
                   "invalid arguments");
+    {
+      // the fused pack + whole-bin contraction where the plan takes it
+      const int64_t pitch = xc_stack_pitch(shape->nspec);
+      FXC_TRY(ctx->scratch.reserve(sizeof(float2) * (size_t)pitch * (size_t)plan->npairs));
+      float2* stack = reinterpret_cast<float2*>(ctx->scratch.ptr);
+      const int rc = xc_gemm_f32_launch(ctx, plan, reinterpret_cast<const float2*>(d_spec), nwin, nchan,
+                                        shape->nspec, spec_pitch, d_mask, 0, scale, stack, pitch, 0);
+      if (rc == FXC_OK) return xc_finalize_launch(ctx, stack, plan->npairs, pitch, shape, d_ncf);
+      if (rc != FXC_ERR_UNSUPPORTED) return rc;
+      clear_error();
+    }
+    // pack, then contraction + finalize without a [pair][bin] stack
     const int64_t chunks = xc_packed_chunks(nchan, nwin, shape->nspec);
     if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
     uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);
@@ -928,12 +939,20 @@ int fxc_xc_run_host(fxc_ctx* ctx, const fxc_pairplan* plan, const float* h_spec,
                            scale, stack, pitch, FXC_XC_PLAIN, 1);
       cuda_ok(cudaEventRecord(used[r], ctx->stream));
     } else if (tensor) {
-      // pack the chunk (the slot is free again once packed: the GEMM reads
-      // the packed copy), then contract it into the stack
-      rc = xc_pack_launch(ctx, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,
-                          packed);
-      cuda_ok(cudaEventRecord(used[r], ctx->stream));
-      if (rc == FXC_OK) rc = xc_gemm_launch(ctx, plan, packed, nw, nspec, scale, stack, pitch, c > 0 ? 1 : 0);
+      // the fused pack + contraction reads the slot itself; otherwise pack
+      // the chunk (the slot is free again once packed: the GEMM reads the
+      // packed copy), then contract it into the stack
+      const uint8_t* cmask = d_mask ? d_mask + (size_t)w0 * nchan : nullptr;
+      rc = xc_gemm_f32_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch, cmask, 0, scale, stack, pitch,
+                              c > 0 ? 1 : 0);
+      if (rc == FXC_ERR_UNSUPPORTED) {
+        clear_error();
+        rc = xc_pack_launch(ctx, spec, nw, nchan, nspec, spec_pitch, cmask, packed);
+        cuda_ok(cudaEventRecord(used[r], ctx->stream));
+        if (rc == FXC_OK) rc = xc_gemm_launch(ctx, plan, packed, nw, nspec, scale, stack, pitch, c > 0 ? 1 : 0);
+      } else {
+        cuda_ok(cudaEventRecord(used[r], ctx->stream));
+      }
     } else {
       rc = xc_stack_launch(ctx, plan, spec, nw, nchan, nspec, spec_pitch, d_mask ? d_mask + (size_t)w0 * nchan : nullptr,
                            scale, stack, pitch, FXC_XC_PLAIN, c > 0);

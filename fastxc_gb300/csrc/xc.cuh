@@ -65,6 +65,12 @@ int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, in
                    int64_t w_base = 0);
 int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int64_t nwin,
                    int nspec, float scale, float2* stack, int64_t stack_pitch, int accumulate = 0);
+// Fused pack + whole-bin contraction of FP32 spectra (windows from w_base
+// on in spec) into the stack; FXC_ERR_UNSUPPORTED where the plan does not
+// take the whole-bin layout.
+int xc_gemm_f32_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin, int nchan,
+                       int nspec, int64_t spec_pitch, const uint8_t* mask, int64_t w_base, float scale,
+                       float2* stack, int64_t stack_pitch, int accumulate);
 int64_t xc_packed_chunks(int32_t nchan, int64_t nwin, int32_t nspec);
 int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_t stack_pitch,
                        const fxc_xc_shape* s, float* ncf);

@@ -30,6 +30,11 @@
 //                    (two warps per TMEM lane quarter, alternate chunks).
 //      Only the upper triangle of channel tiles is computed (a pair is
 //      computed in the orientation (min, max) and conjugated if reversed).
+//   Up to 192 channels k_xc_tc_gemm_bin computes a whole bin per CTA; its
+//   F32 form fuses step 1: the epilogue warps, idle during the K loop,
+//   gather the bin's FP32 values of each K-block, split them into the four
+//   bf16 planes and store the core-matrix chunks into the operand ring
+//   themselves, so the spectra are read once and no packed copy exists.
 //      Every mbarrier wait is bounded by %globaltimer (2 s); a timeout sets
 //      the context's device error word, the CTA drains its copies and frees
 //      TMEM before it exits.
@@ -628,8 +633,50 @@ constexpr int kBinStageBytes = kTcPlanes * kTcKc * kBinRows * 16;  // 64 KB
 constexpr size_t kBinSmemBytes = (size_t)kBinStages * kBinStageBytes + 256;
 static_assert(kBinSmemBytes <= 227 * 1024, "whole-bin ring exceeds shared memory");
 
+// Operand source of the whole-bin kernel when it reads the FP32 spectra
+// itself (F32 = true): complex64 [w - w_base][c][pitch] with windows
+// [0, nwin) of the call, and an optional [w][c] window mask.
+struct BinSrc {
+  const float2* spec;
+  int64_t nwin, pitch, w_base;
+  const uint8_t* mask;
+};
+constexpr int kConvThreads = kTcThreads - 64;                       // warps 2..9
+constexpr int kConvUnits = (192 * kTcKc + kConvThreads - 1) / kConvThreads;  // (row, chunk) units per thread
+
+// Eight windows of one complex value -> the four bf16 planes of one 16-byte
+// core-matrix row: re-hi, re-lo, im-hi, im-lo (hi = rn(x), lo = rn(x - hi)).
+__device__ __forceinline__ void split_bf16x8(const float2 (&v)[8], uint4 (&o)[4]) {
+  uint32_t w_rh[4], w_rl[4], w_ih[4], w_il[4];
+#pragma unroll
+  for (int e2 = 0; e2 < 4; ++e2) {
+    const float2 v0 = v[2 * e2], v1 = v[2 * e2 + 1];
+    const uint32_t rh = bf16x2_rn(v0.x, v1.x);
+    const uint32_t ih = bf16x2_rn(v0.y, v1.y);
+    w_rh[e2] = rh;
+    w_ih[e2] = ih;
+    w_rl[e2] = bf16x2_rn(v0.x - __uint_as_float(rh << 16), v1.x - __uint_as_float(rh & 0xffff0000u));
+    w_il[e2] = bf16x2_rn(v0.y - __uint_as_float(ih << 16), v1.y - __uint_as_float(ih & 0xffff0000u));
+  }
+  o[0] = make_uint4(w_rh[0], w_rh[1], w_rh[2], w_rh[3]);
+  o[1] = make_uint4(w_rl[0], w_rl[1], w_rl[2], w_rl[3]);
+  o[2] = make_uint4(w_ih[0], w_ih[1], w_ih[2], w_ih[3]);
+  o[3] = make_uint4(w_il[0], w_il[1], w_il[2], w_il[3]);
+}
+
+// F32 = false: the operands come packed (k_xc_pack) and warp 0 moves them
+// with bulk copies. F32 = true: the pack is fused in -- warps 2..9, idle
+// until the epilogue, gather each K-block's FP32 values of this bin (one
+// 8-byte load per (window, channel); the CTAs of the neighbouring bins read
+// the rest of each 32-byte sector, so it is fetched from DRAM once), split
+// them into the four bf16 planes in registers and store the chunks into the
+// ring stage; each warp then fences the generic writes for the async proxy
+// and arrives on the stage's full barrier (8 arrivals). The packed operand
+// copy -- written and read back once each, as large as the spectra -- is
+// never formed.
+template <bool F32>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_xc_tc_gemm_bin(const uint4* __restrict__ packed, int nkb, int cpad, int nchan,
+    k_xc_tc_gemm_bin(const uint4* __restrict__ packed, BinSrc src, int nkb, int cpad, int nchan,
                      const TcTile* __restrict__ tiles, int ntiles, const int32_t* __restrict__ maps,
                      float scale, float2* __restrict__ binmajor, int64_t bin_pitch, int npairs,
                      int* __restrict__ err) {
@@ -665,7 +712,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kBinStages; ++s) {
-      mbar_init(bar_full0 + 8 * s, 1);
+      mbar_init(bar_full0 + 8 * s, F32 ? kConvThreads / 32 : 1);
       mbar_init(bar_empty0 + 8 * s, 1);
     }
     mbar_init(bar_acc, 1);
@@ -687,7 +734,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t c_re0 = 0, c_im0 = (uint32_t)n0, c_re1 = 2u * n0, c_im1 = 2u * n0 + n1;
 
   if (warp == 0) {
-    if (lane == 0) {
+    if (!F32 && lane == 0) {
       const uint32_t tx = (uint32_t)kTcPlanes * kTcKc * (uint32_t)nchan * 16u;
       int issued = 0;
       bool failed = false;
@@ -779,6 +826,55 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       umma_commit(bar_acc);
     }
   } else {
+    if constexpr (F32) {
+      // operand producer: unit u = kc * nchan + c is row c of 8-window chunk
+      // kc (consecutive lanes store consecutive rows: conflict-free)
+      const int t = threadIdx.x - 64;
+      const int nunits = nchan * kTcKc;
+      bool failed = false;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % kBinStages;
+        const uint32_t ph = (uint32_t)(kb / kBinStages) & 1u;
+        float2 v[kConvUnits][8];
+#pragma unroll
+        for (int j = 0; j < kConvUnits; ++j) {
+          const int u = t + j * kConvThreads;
+          const int c = u < nunits ? u % nchan : 0;
+          const int kc = u < nunits ? u / nchan : 0;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            const int64_t w = (int64_t)kb * kTcKb + kc * 8 + e;
+            bool ok = u < nunits && w < src.nwin;
+            if (ok && src.mask) ok = __ldg(src.mask + w * nchan + c) != 0;
+            v[j][e] = ok ? __ldg(src.spec + ((w - src.w_base) * nchan + c) * src.pitch + f) : make_float2(0.f, 0.f);
+          }
+        }
+        // one lane waits and the warp follows its verdict: every lane leaves
+        // the loop together, so the __syncwarp below never waits on a lane
+        // that has left
+        const int ok = __shfl_sync(0xffffffffu, lane == 0 ? (int)mbar_wait(bar_empty0 + 8 * s, ph ^ 1u) : 0, 0);
+        if (!ok) {
+          failed = true;
+          break;
+        }
+        uint4* st = reinterpret_cast<uint4*>(stage_base + (size_t)s * kBinStageBytes);
+#pragma unroll
+        for (int j = 0; j < kConvUnits; ++j) {
+          const int u = t + j * kConvThreads;
+          if (u < nunits) {
+            const int c = u % nchan, kc = u / nchan;
+            uint4 o[4];
+            split_bf16x8(v[j], o);
+#pragma unroll
+            for (int pl = 0; pl < kTcPlanes; ++pl) st[(size_t)(pl * kTcKc + kc) * kBinRows + c] = o[pl];
+          }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_full0 + 8 * s);
+      }
+      if (failed) atomicExch(err, 1);
+    }
     // epilogue: lane quarter q = warp % 4 holds rows q*32.. of both tiles;
     // the two warps of a quarter take alternate 16-column chunks of the
     // combined column space [0, n0) + [n0, n0 + n1)
@@ -964,18 +1060,59 @@ int xc_pack_launch(fxc_ctx* ctx, const float2* spec, int64_t nwin, int nchan, in
 // The whole-bin contraction into bin-major rows ([bin][bin_pitch] complex,
 // context scratch): the producer of both the [pair][bin] transpose and the
 // direct finalize.
-static int gemm_bin_rows(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, int nkb, int nspec,
-                         float scale, float2** rows, int64_t* bin_pitch) {
+// Operands from `packed` (src == null) or straight from the FP32 spectra
+// (the fused pack, src != null).
+static int gemm_bin_rows(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, const BinSrc* src, int nkb,
+                         int nspec, float scale, float2** rows, int64_t* bin_pitch) {
   const XcTensorPlan* tp = plan->tensor;
   *bin_pitch = round_up(plan->npairs, 4);
   FXC_TRY(ctx->scratch5.reserve(sizeof(float2) * (size_t)*bin_pitch * (size_t)nspec));
   *rows = reinterpret_cast<float2*>(ctx->scratch5.ptr);
-  FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin, kBinSmemBytes));
   KernelTimer kt(ctx, "k_xc_tc_gemm_bin");
-  k_xc_tc_gemm_bin<<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
-      packed, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, *rows, *bin_pitch,
-      (int)plan->npairs, ctx->d_err);
+  if (src) {
+    FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin<true>, kBinSmemBytes));
+    k_xc_tc_gemm_bin<true><<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
+        nullptr, *src, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, *rows,
+        *bin_pitch, (int)plan->npairs, ctx->d_err);
+  } else {
+    FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin<false>, kBinSmemBytes));
+    k_xc_tc_gemm_bin<false><<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
+        packed, BinSrc{}, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, *rows,
+        *bin_pitch, (int)plan->npairs, ctx->d_err);
+  }
   kt.stop();
+  count_launch();
+  FXC_LAUNCH_CHECK();
+  return FXC_OK;
+}
+
+// The fused pack + whole-bin contraction of FP32 spectra into the stack, or
+// FXC_ERR_UNSUPPORTED where the plan does not take the whole-bin layout or
+// the fused form is not selected (FXC_GEMM_FUSED=1 selects it; the caller
+// then packs). Measured at 192 channels x 720 windows: 0.72 ms for 512 bins
+// against 0.42 ms for k_xc_pack + the packed whole-bin kernel -- one CTA
+// gathers its bin's 8-byte values one (window, channel) at a time, 6144
+// scattered loads per K-block, about 2.5x the time its MMAs take; the
+// neighbouring bins of each 32-byte sector would have to be loaded once
+// and shared between the CTAs of a cluster to pay off.
+int xc_gemm_f32_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin, int nchan,
+                       int nspec, int64_t spec_pitch, const uint8_t* mask, int64_t w_base, float scale,
+                       float2* stack, int64_t stack_pitch, int accumulate) {
+  const XcTensorPlan* tp = plan->tensor;
+  FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
+  const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
+  const char* fe = getenv("FXC_GEMM_FUSED");
+  if (!fe || fe[0] != '1' || nkb == 0 || !use_whole_bin(plan, nkb)) return FXC_ERR_UNSUPPORTED;
+  FXC_CHECK_ARG(nchan == tp->nchan && nchan <= 192, "channel count %d does not match the plan", nchan);
+  FXC_CHECK_ARG(nspec <= 65535, "nspec %d above the tensor grid limit", nspec);
+  if (tp->ntiles == 0 || nspec == 0) return FXC_OK;
+  const BinSrc src{spec, nwin, spec_pitch, w_base, mask};
+  float2* binmajor = nullptr;
+  int64_t bin_pitch = 0;
+  FXC_TRY(gemm_bin_rows(ctx, plan, nullptr, &src, nkb, nspec, scale, &binmajor, &bin_pitch));
+  const dim3 tg((unsigned)((plan->npairs + 31) / 32), (unsigned)((nspec + 31) / 32));
+  k_xc_binmajor_to_stack<<<tg, 256, 0, ctx->stream>>>(binmajor, bin_pitch, plan->npairs, nspec, tp->d_perm, stack,
+                                                       stack_pitch, accumulate);
   count_launch();
   FXC_LAUNCH_CHECK();
   return FXC_OK;
@@ -1000,7 +1137,7 @@ int xc_gemm_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* packed, 
     // bin-major rows in context scratch, then transposed into the stack
     float2* binmajor = nullptr;
     int64_t bin_pitch = 0;
-    FXC_TRY(gemm_bin_rows(ctx, plan, packed, nkb, nspec, scale, &binmajor, &bin_pitch));
+    FXC_TRY(gemm_bin_rows(ctx, plan, packed, nullptr, nkb, nspec, scale, &binmajor, &bin_pitch));
     const dim3 tg((unsigned)((plan->npairs + 31) / 32), (unsigned)((nspec + 31) / 32));
     k_xc_binmajor_to_stack<<<tg, 256, 0, ctx->stream>>>(binmajor, bin_pitch, plan->npairs, nspec, tp->d_perm,
                                                          stack, stack_pitch, accumulate);
@@ -1059,6 +1196,12 @@ int xc_stack_tensor_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2*
   const XcTensorPlan* tp = plan->tensor;
   FXC_CHECK_ARG(tp != nullptr, "pair plan has no tensor tiles");
   if (tp->ntiles == 0) return FXC_OK;
+  {
+    const int rc = xc_gemm_f32_launch(ctx, plan, spec, nwin, nchan, nspec, spec_pitch, mask, 0, scale, stack,
+                                      stack_pitch, accumulate);
+    if (rc != FXC_ERR_UNSUPPORTED) return rc;
+    clear_error();
+  }
   const int64_t chunks = xc_packed_chunks(nchan, nwin, nspec);
   if (chunks > 0) FXC_TRY(ctx->scratch3.reserve((size_t)chunks * 16));
   uint4* packed = reinterpret_cast<uint4*>(ctx->scratch3.ptr);

@@ -148,6 +148,47 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
 
 
+@pytest.mark.parametrize("nchan,nwin", [(192, 70), (150, 33), (96, 130)])
+def test_fused_pack_contraction_equals_packed(ctx, torch_cuda, monkeypatch, nchan, nwin):
+    """The whole-bin contraction that reads the FP32 spectra itself (the
+    pack fused into its idle epilogue warps, FXC_GEMM_FUSED=1) forms the same bf16 hi/lo
+    operands as k_xc_pack and runs the same MMAs in the same order: its
+    stack equals the packed path's bit for bit, with a window mask, a
+    partial last K-block, autocorrelations and reversed pairs; and the FP64
+    oracle within 2e-5."""
+    torch = torch_cuda
+    from fastxc_gb300._lib import FXC_XC_LAYOUT_WHOLE_BIN as WHOLE
+    from fastxc_gb300.core import PairPlan
+
+    rng = np.random.default_rng(nchan * 7 + nwin)
+    nspec = 301
+    spec = make_spec(rng, nwin, nchan, nspec)
+    iu, ju = np.triu_indices(nchan)
+    keep = rng.random(iu.size) < 0.4
+    src, rec = iu[keep].astype(np.int32), ju[keep].astype(np.int32)
+    flip = rng.random(src.size) < 0.3
+    src, rec = np.where(flip, rec, src).astype(np.int32), np.where(flip, src, rec).astype(np.int32)
+    mask = (rng.random((nwin, nchan)) > 0.1).astype(np.uint8)
+    plan = PairPlan(ctx, src, rec, nchan)
+    plan.set_layout(WHOLE)
+    assert plan.layouts(nwin)[1] == WHOLE
+    d_spec = torch.from_numpy(spec).cuda()
+    d_mask = torch.from_numpy(mask).cuda()
+    out = {}
+    for packed in (False, True):
+        monkeypatch.setenv("FXC_GEMM_FUSED", "0" if packed else "1")
+        ctx.kernel_timing(True)
+        st = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+        ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, d_mask, 0.5, st, nspec, 1)
+        ctx.synchronize()
+        assert ctx.kernel_time("k_xc_tc_gemm_bin")[1] == 1
+        ctx.kernel_timing(False)
+        out[packed] = st.cpu().numpy()
+    assert np.array_equal(out[False], out[True])
+    ref = xo.xc_stack(spec, src, rec, 0.5, mask)
+    assert rel_l2(out[False], ref) < 2e-5
+
+
 @pytest.mark.parametrize("nchan,nwin", [(96, 24), (192, 130)])
 def test_layout_autotune_and_preference(ctx, torch_cuda, nchan, nwin):
     """The autotuner times the plain kernel and the tensor contraction in
