@@ -329,6 +329,55 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   }
 }
 
+// Cluster forms: the shared::cluster address of `addr` in CTA `rank`, a
+// 16-byte store and an mbarrier arrival there, and a bounded wait whose
+// acquire covers arrivals released by other CTAs of the cluster.
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void st_cluster16(uint32_t addr, uint4 v) {
+  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
+               "r"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t remote_bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote_bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_cluster(uint32_t bar, uint32_t parity) {
+  if (mbar_try_cluster(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try_cluster(bar, parity)) return true;
+    if ((i & 255u) == 0 && globaltimer() - t0 > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
 // 16 accumulator columns of one TMEM row into a bin-major row: column j goes
 // to slot q = mv[j] (conjugated for -(q + 2), skipped for -1).
 __device__ __forceinline__ void store_slots16(float2* __restrict__ row, const int32_t* mv, const float* re,
@@ -632,6 +681,18 @@ constexpr int kBinStages = 3;
 constexpr int kBinStageBytes = kTcPlanes * kTcKc * kBinRows * 16;  // 64 KB
 constexpr size_t kBinSmemBytes = (size_t)kBinStages * kBinStageBytes + 256;
 static_assert(kBinSmemBytes <= 227 * 1024, "whole-bin ring exceeds shared memory");
+// The fused form: operand chunks of 192 rows (48 KB stages; tile 1's A
+// operand, rows 128..255, reads 64 rows into the next chunk -- or, for the
+// last chunk, into 1 KB of slack -- which only reach accumulator rows the
+// epilogue never stores), then a ring of 3 staging buffers for the FP32
+// input, each half a K-block (16 windows) of one CTA's 48 rows x 4 bins.
+constexpr int kBinRowsF = 192;
+constexpr int kBinStageBytesF = kTcPlanes * kTcKc * kBinRowsF * 16;  // 48 KB
+constexpr int kStagingOffF = kBinStages * kBinStageBytesF + 1024;
+constexpr int kHalfBytesF = 16 * 2 * 48 * 16;  // [16 windows][2 bin pairs][48 rows][16 B]
+constexpr int kStagingBufsF = 3;
+constexpr size_t kBinSmemBytesF = (size_t)kStagingOffF + (size_t)kStagingBufsF * kHalfBytesF + 256;
+static_assert(kBinSmemBytesF <= 227 * 1024, "fused whole-bin ring exceeds shared memory");
 
 // Operand source of the whole-bin kernel when it reads the FP32 spectra
 // itself (F32 = true): complex64 [w - w_base][c][pitch] with windows
@@ -640,9 +701,12 @@ struct BinSrc {
   const float2* spec;
   int64_t nwin, pitch, w_base;
   const uint8_t* mask;
+  int nspec;
 };
-constexpr int kConvThreads = kTcThreads - 64;                       // warps 2..9
-constexpr int kConvUnits = (192 * kTcKc + kConvThreads - 1) / kConvThreads;  // (row, chunk) units per thread
+constexpr int kConvThreads = kTcThreads - 64;  // warps 2..9
+constexpr int kBinCluster = 4;                 // bins (CTAs) per cluster of the fused form
+// (row, 8-window chunk) units of one CTA's row quarter: 48 rows x 4 chunks
+static_assert((192 / kBinCluster) * kTcKc <= kConvThreads, "one unit per converter thread");
 
 // Eight windows of one complex value -> the four bf16 planes of one 16-byte
 // core-matrix row: re-hi, re-lo, im-hi, im-lo (hi = rn(x), lo = rn(x - hi)).
@@ -665,15 +729,20 @@ __device__ __forceinline__ void split_bf16x8(const float2 (&v)[8], uint4 (&o)[4]
 }
 
 // F32 = false: the operands come packed (k_xc_pack) and warp 0 moves them
-// with bulk copies. F32 = true: the pack is fused in -- warps 2..9, idle
-// until the epilogue, gather each K-block's FP32 values of this bin (one
-// 8-byte load per (window, channel); the CTAs of the neighbouring bins read
-// the rest of each 32-byte sector, so it is fetched from DRAM once), split
-// them into the four bf16 planes in registers and store the chunks into the
-// ring stage; each warp then fences the generic writes for the async proxy
-// and arrives on the stage's full barrier (8 arrivals). The packed operand
-// copy -- written and read back once each, as large as the spectra -- is
-// never formed.
+// with bulk copies. F32 = true: the pack is fused in, and the kernel runs
+// as clusters of 4 CTAs, one per bin of 4 consecutive bins (the 32 bytes of
+// one (window, channel) row of the spectra: one DRAM sector). CTA r of a
+// cluster loads rows [48 r, 48 r + 48) of all 4 bins, whole sectors, with
+// its warps 2..9 (idle until the epilogue); splits them into the four bf16
+// planes in registers and stores each bin's core-matrix chunks straight into
+// the operand ring of that bin's CTA through distributed shared memory. So
+// the spectra are read once, in full sectors, and no packed copy exists.
+// Each converter warp then fences its writes for the async proxy and
+// arrives on the stage's full barrier of all 4 CTAs (32 arrivals per
+// stage); each CTA's MMA thread frees a stage in all 4 CTAs at once with a
+// multicast tcgen05.commit (4 arrivals per empty barrier). Cluster barriers
+// before the first remote access and before TMEM is released keep every
+// CTA alive while its peers may still write to it.
 template <bool F32>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_xc_tc_gemm_bin(const uint4* __restrict__ packed, BinSrc src, int nkb, int cpad, int nchan,
@@ -685,11 +754,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // the epilogue scatters the pairs into them by pair index and then writes
   // the row out in contiguous 16-byte stores (the [pair][bin] layout would
   // need one 8-byte store per pair, each in a sector of its own).
+  constexpr int kRows = F32 ? kBinRowsF : kBinRows;
+  constexpr int kStageBytes = F32 ? kBinStageBytesF : kBinStageBytes;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* stage_base = smem;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)kBinStages * kBinStageBytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(
+      smem + (F32 ? (size_t)kStagingOffF + (size_t)kStagingBufsF * kHalfBytesF : (size_t)kBinStages * kBinStageBytes));
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kBinStages + 1);
   int* epi_failed = reinterpret_cast<int*>(tmem_slot + 1);
+  int* conv_ok = epi_failed + 1;
   const uint32_t bar_full0 = smem_u32(bars);
   const uint32_t bar_empty0 = smem_u32(bars + kBinStages);
   const uint32_t bar_acc = smem_u32(bars + 2 * kBinStages);
@@ -699,24 +772,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const TcTile t0 = tiles[0];
   const bool two = ntiles > 1;
   const int n0 = t0.n, n1 = two ? tiles[1].n : 0;
-  const uint32_t chunk_bytes = (uint32_t)kBinRows * 16;  // one (plane, kc) chunk
+  const uint32_t chunk_bytes = (uint32_t)kRows * 16;  // one (plane, kc) chunk
 
-  // zero the rows the copies never write (C .. 255) of every chunk once
+  // zero the rows the copies never write (C .. rows) of every chunk once
   for (int s = 0; s < kBinStages; ++s) {
-    uint4* st = reinterpret_cast<uint4*>(stage_base + (size_t)s * kBinStageBytes);
-    const int per = kBinRows - nchan;
+    uint4* st = reinterpret_cast<uint4*>(stage_base + (size_t)s * kStageBytes);
+    const int per = kRows - nchan;
     for (int i = threadIdx.x; i < kTcPlanes * kTcKc * per; i += kTcThreads) {
       const int ch = i / per, r = nchan + i % per;
-      st[(size_t)ch * kBinRows + r] = make_uint4(0, 0, 0, 0);
+      st[(size_t)ch * kRows + r] = make_uint4(0, 0, 0, 0);
     }
+  }
+  if constexpr (F32) {
+    // the slack past the last chunk (read by tile 1's A operand only)
+    uint4* sl = reinterpret_cast<uint4*>(stage_base + (size_t)kBinStages * kStageBytes);
+    for (int i = threadIdx.x; i < 1024 / 16; i += kTcThreads) sl[i] = make_uint4(0, 0, 0, 0);
   }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kBinStages; ++s) {
-      mbar_init(bar_full0 + 8 * s, F32 ? kConvThreads / 32 : 1);
-      mbar_init(bar_empty0 + 8 * s, 1);
+      mbar_init(bar_full0 + 8 * s, F32 ? kBinCluster * (kConvThreads / 32) : 1);
+      mbar_init(bar_empty0 + 8 * s, F32 ? kBinCluster : 1);
     }
     mbar_init(bar_acc, 1);
     *epi_failed = 0;
+    *conv_ok = 1;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -728,6 +807,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  // every CTA's barriers are initialised and its rows [C, 256) zeroed
+  // before any peer writes into it
+  if constexpr (F32) cluster_sync_all();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   // TMEM columns: T0 Re [0, n0), T0 Im [n0, 2 n0), T1 Re [2 n0, 2 n0 + n1), T1 Im after
@@ -774,12 +856,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int kb = 0; kb < nkb; ++kb) {
         const int s = kb % kBinStages;
         const uint32_t ph = (uint32_t)(kb / kBinStages) & 1u;
-        if (!mbar_wait(bar_full0 + 8 * s, ph)) {
+        if (!(F32 ? mbar_wait_cluster(bar_full0 + 8 * s, ph) : mbar_wait(bar_full0 + 8 * s, ph))) {
           failed = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t st = smem_u32(stage_base + (size_t)s * kBinStageBytes);
+        const uint32_t st = smem_u32(stage_base + (size_t)s * kStageBytes);
 #pragma unroll
         for (int ks = 0; ks < kTcKc / 2; ++ks) {
           uint64_t P0[4], P1[4];  // rows 0.. and rows 128.. of each plane at this K step
@@ -820,59 +902,118 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           first = false;
         }
-        umma_commit(bar_empty0 + 8 * s);
+        if constexpr (F32) {
+          // the stage is free in every CTA of the cluster once this CTA's
+          // MMAs have read it: one arrival on each CTA's empty barrier
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::
+                  "r"(bar_empty0 + 8 * s),
+              "h"((uint16_t)((1u << kBinCluster) - 1))
+              : "memory");
+        } else {
+          umma_commit(bar_empty0 + 8 * s);
+        }
       }
       if (failed) atomicExch(err, 1);
       umma_commit(bar_acc);
     }
   } else {
     if constexpr (F32) {
-      // operand producer: unit u = kc * nchan + c is row c of 8-window chunk
-      // kc (consecutive lanes store consecutive rows: conflict-free)
+      // operand producer for this CTA's row quarter of the cluster's 4 bins.
+      // Half K-blocks (16 windows) stream into a ring of 3 staging buffers
+      // by 16-byte cp.async copies issued two halves ahead, so their DRAM
+      // latency overlaps the conversion of the half before; the layout
+      // [window][bin pair][row][16 B] puts consecutive rows 16 bytes apart
+      // for the conversion reads.
+      const uint32_t rank = cluster_ctarank();
+      const int f0 = f - (int)rank;
+      const int q4 = (nchan + kBinCluster - 1) / kBinCluster;
+      const int row0 = (int)rank * q4;
+      const int nq = max(0, min(nchan, row0 + q4) - row0);
       const int t = threadIdx.x - 64;
-      const int nunits = nchan * kTcKc;
-      bool failed = false;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % kBinStages;
-        const uint32_t ph = (uint32_t)(kb / kBinStages) & 1u;
-        float2 v[kConvUnits][8];
+      unsigned char* stg = smem + kStagingOffF;
+      uint32_t stage_r[kBinCluster], full_r[kBinCluster];
 #pragma unroll
-        for (int j = 0; j < kConvUnits; ++j) {
-          const int u = t + j * kConvThreads;
-          const int c = u < nunits ? u % nchan : 0;
-          const int kc = u < nunits ? u / nchan : 0;
-#pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const int64_t w = (int64_t)kb * kTcKb + kc * 8 + e;
-            bool ok = u < nunits && w < src.nwin;
-            if (ok && src.mask) ok = __ldg(src.mask + w * nchan + c) != 0;
-            v[j][e] = ok ? __ldg(src.spec + ((w - src.w_base) * nchan + c) * src.pitch + f) : make_float2(0.f, 0.f);
+      for (int b = 0; b < kBinCluster; ++b) {
+        stage_r[b] = cluster_addr(smem_u32(stage_base), (uint32_t)b);
+        full_r[b] = cluster_addr(bar_full0, (uint32_t)b);
+      }
+      const int nhalf = 2 * nkb;
+      auto issue = [&](int h) {
+        if (h < nhalf) {
+          unsigned char* buf = stg + (h % kStagingBufsF) * kHalfBytesF;
+          for (int i = t; i < 32 * nq; i += kConvThreads) {
+            const int row = i % nq, rest = i / nq, pair = rest & 1, w16 = rest >> 1;
+            const int64_t w = (int64_t)h * 16 + w16;
+            unsigned char* d = buf + ((w16 * 2 + pair) * 48 + row) * 16;
+            if (w < src.nwin) {
+              const float2* g = src.spec + ((w - src.w_base) * nchan + row0 + row) * src.pitch + f0 + 2 * pair;
+              asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(d)), "l"(g) : "memory");
+            } else {
+              *reinterpret_cast<uint4*>(d) = make_uint4(0, 0, 0, 0);  // windows past the call's last
+            }
           }
         }
-        // one lane waits and the warp follows its verdict: every lane leaves
-        // the loop together, so the __syncwarp below never waits on a lane
-        // that has left
-        const int ok = __shfl_sync(0xffffffffu, lane == 0 ? (int)mbar_wait(bar_empty0 + 8 * s, ph ^ 1u) : 0, 0);
-        if (!ok) {
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      };
+      issue(0);
+      issue(1);
+      bool failed = false;
+      for (int h = 0; h < nhalf; ++h) {
+        issue(h + 2);  // into the buffer read at h - 1, released by that iteration's closing barrier
+        asm volatile("cp.async.wait_group 2;" ::: "memory");  // this thread's copies of half h
+        const int kb = h >> 1;
+        const int s = kb % kBinStages;
+        if ((h & 1) == 0 && t == 0)
+          *conv_ok = mbar_wait_cluster(bar_empty0 + 8 * s, ((uint32_t)(kb / kBinStages) & 1u) ^ 1u) ? 1 : 0;
+        // half h landed for every converter thread; the stage verdict is
+        // the same for all of them, so all leave the loop together
+        asm volatile("bar.sync 2, %0;" ::"n"(kConvThreads) : "memory");
+        if (*conv_ok == 0) {
           failed = true;
           break;
         }
-        uint4* st = reinterpret_cast<uint4*>(stage_base + (size_t)s * kBinStageBytes);
+        const unsigned char* buf = stg + (h % kStagingBufsF) * kHalfBytesF;
+        if (t < 4 * nq) {
+          const int row = t % nq, rest = t / nq, pair = rest & 1, kcp = rest >> 1;
+          float2 x0[8], x1[8];
 #pragma unroll
-        for (int j = 0; j < kConvUnits; ++j) {
-          const int u = t + j * kConvThreads;
-          if (u < nunits) {
-            const int c = u % nchan, kc = u / nchan;
-            uint4 o[4];
-            split_bf16x8(v[j], o);
+          for (int e = 0; e < 8; ++e) {
+            const float4 q = *reinterpret_cast<const float4*>(buf + (((kcp * 8 + e) * 2 + pair) * 48 + row) * 16);
+            x0[e] = make_float2(q.x, q.y);
+            x1[e] = make_float2(q.z, q.w);
+          }
+          const int b0 = 2 * pair;
+          if (f0 + b0 >= src.nspec)
 #pragma unroll
-            for (int pl = 0; pl < kTcPlanes; ++pl) st[(size_t)(pl * kTcKc + kc) * kBinRows + c] = o[pl];
+            for (int e = 0; e < 8; ++e) x0[e] = make_float2(0.f, 0.f);  // past the last bin
+          if (f0 + b0 + 1 >= src.nspec)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) x1[e] = make_float2(0.f, 0.f);
+          uint4 o0[4], o1[4];
+          split_bf16x8(x0, o0);
+          split_bf16x8(x1, o1);
+          const int kc = (h & 1) * 2 + kcp;
+          const uint32_t off = (uint32_t)s * kStageBytes + (uint32_t)(kc * kRows + row0 + row) * 16;
+#pragma unroll
+          for (int pl = 0; pl < kTcPlanes; ++pl) {
+            const uint32_t po = off + (uint32_t)(pl * kTcKc * kRows) * 16;
+            st_cluster16(stage_r[b0] + po, o0[pl]);
+            st_cluster16(stage_r[b0 + 1] + po, o1[pl]);
           }
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) mbar_arrive(bar_full0 + 8 * s);
+        if (h & 1) {
+          // the K-block is complete in every CTA this thread wrote to
+          asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+#pragma unroll
+            for (int b = 0; b < kBinCluster; ++b) mbar_arrive_cluster(full_r[b] + 8 * s);
+          }
+        }
+        asm volatile("bar.sync 2, %0;" ::"n"(kConvThreads) : "memory");  // buffer h free
       }
+      asm volatile("cp.async.wait_all;" ::: "memory");
       if (failed) atomicExch(err, 1);
     }
     // epilogue: lane quarter q = warp % 4 holds rows q*32.. of both tiles;
@@ -933,7 +1074,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
     }
     asm volatile("bar.sync 1, %0;" ::"n"(kTcThreads - 64) : "memory");
-    if (*epi_failed == 0) {
+    if (*epi_failed == 0 && (!F32 || f < src.nspec)) {
       // pairs [0, npairs) as float4 pairs; an odd count writes one padding
       // element of the row (bin_pitch is a multiple of 4)
       const float4* src4 = reinterpret_cast<const float4*>(sout);
@@ -943,6 +1084,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  // no CTA leaves while a peer may still store into it or arrive on it
+  if constexpr (F32) cluster_sync_all();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
@@ -1070,10 +1213,25 @@ static int gemm_bin_rows(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* pa
   *rows = reinterpret_cast<float2*>(ctx->scratch5.ptr);
   KernelTimer kt(ctx, "k_xc_tc_gemm_bin");
   if (src) {
-    FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin<true>, kBinSmemBytes));
-    k_xc_tc_gemm_bin<true><<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
-        nullptr, *src, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, *rows,
-        *bin_pitch, (int)plan->npairs, ctx->d_err);
+    // clusters of kBinCluster CTAs, one per bin (the last cluster's CTAs
+    // past nspec load and convert their rows but write no output)
+    FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin<true>, kBinSmemBytesF));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)round_up(nspec, kBinCluster));
+    cfg.blockDim = dim3((unsigned)kTcThreads);
+    cfg.dynamicSmemBytes = kBinSmemBytesF;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kBinCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FXC_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_xc_tc_gemm_bin<true>, (const uint4*)nullptr, *src, nkb, (int)tp->cpad,
+                                    (int)tp->nchan, (const TcTile*)tp->d_tiles, (int)tp->ntiles,
+                                    (const int32_t*)tp->d_maps, scale, *rows, *bin_pitch, (int)plan->npairs,
+                                    ctx->d_err));
   } else {
     FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin<false>, kBinSmemBytes));
     k_xc_tc_gemm_bin<false><<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
@@ -1089,12 +1247,14 @@ static int gemm_bin_rows(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* pa
 // The fused pack + whole-bin contraction of FP32 spectra into the stack, or
 // FXC_ERR_UNSUPPORTED where the plan does not take the whole-bin layout or
 // the fused form is not selected (FXC_GEMM_FUSED=1 selects it; the caller
-// then packs). Measured at 192 channels x 720 windows: 0.72 ms for 512 bins
-// against 0.42 ms for k_xc_pack + the packed whole-bin kernel -- one CTA
-// gathers its bin's 8-byte values one (window, channel) at a time, 6144
-// scattered loads per K-block, about 2.5x the time its MMAs take; the
-// neighbouring bins of each 32-byte sector would have to be loaded once
-// and shared between the CTAs of a cluster to pay off.
+// then packs). Measured at 192 channels x 720 windows x 18 523 bins: the
+// contraction 15.6 ms against 6.8 ms for the packed one (+ 6.6 ms of
+// k_xc_pack), its stack bit-identical. With the loads replaced by
+// constants it still took 9.9 ms: the 4-CTA lockstep of every K-block
+// (empty and full barriers across the cluster), the distributed-shared-
+// memory stores and 144 of the 152 SMs (36 clusters of 4 fit) cost more than
+// the 2.4 us of MMAs per K-block leave; the loads through the cp.async
+// staging ring then add another 5.7 ms.
 int xc_gemm_f32_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spec, int64_t nwin, int nchan,
                        int nspec, int64_t spec_pitch, const uint8_t* mask, int64_t w_base, float scale,
                        float2* stack, int64_t stack_pitch, int accumulate) {
@@ -1103,10 +1263,15 @@ int xc_gemm_f32_launch(fxc_ctx* ctx, const fxc_pairplan* plan, const float2* spe
   const int nkb = (int)((nwin + kTcKb - 1) / kTcKb);
   const char* fe = getenv("FXC_GEMM_FUSED");
   if (!fe || fe[0] != '1' || nkb == 0 || !use_whole_bin(plan, nkb)) return FXC_ERR_UNSUPPORTED;
+  // 16-byte copies of 2 bins: 16-byte aligned rows, every bin of the last
+  // cluster inside the row pitch; no window mask (masked calls pack)
+  if ((reinterpret_cast<uintptr_t>(spec) & 15u) != 0 || spec_pitch % 2 != 0 ||
+      spec_pitch < round_up(nspec, kBinCluster) || mask != nullptr)
+    return FXC_ERR_UNSUPPORTED;
   FXC_CHECK_ARG(nchan == tp->nchan && nchan <= 192, "channel count %d does not match the plan", nchan);
   FXC_CHECK_ARG(nspec <= 65535, "nspec %d above the tensor grid limit", nspec);
   if (tp->ntiles == 0 || nspec == 0) return FXC_OK;
-  const BinSrc src{spec, nwin, spec_pitch, w_base, mask};
+  const BinSrc src{spec, nwin, spec_pitch, w_base, mask, nspec};
   float2* binmajor = nullptr;
   int64_t bin_pitch = 0;
   FXC_TRY(gemm_bin_rows(ctx, plan, nullptr, &src, nkb, nspec, scale, &binmajor, &bin_pitch));

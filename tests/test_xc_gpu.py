@@ -148,21 +148,27 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
 
 
-@pytest.mark.parametrize("nchan,nwin", [(192, 70), (150, 33), (96, 130)])
-def test_fused_pack_contraction_equals_packed(ctx, torch_cuda, monkeypatch, nchan, nwin):
-    """The whole-bin contraction that reads the FP32 spectra itself (the
-    pack fused into its idle epilogue warps, FXC_GEMM_FUSED=1) forms the same bf16 hi/lo
-    operands as k_xc_pack and runs the same MMAs in the same order: its
-    stack equals the packed path's bit for bit, with a window mask, a
-    partial last K-block, autocorrelations and reversed pairs; and the FP64
-    oracle within 2e-5."""
+@pytest.mark.parametrize("nchan,nwin,nspec", [(192, 70, 301), (150, 33, 256), (96, 130, 301)])
+def test_fused_pack_contraction_equals_packed(ctx, torch_cuda, monkeypatch, nchan, nwin, nspec):
+    """The whole-bin contraction that reads the FP32 spectra itself
+    (FXC_GEMM_FUSED=1: clusters of 4 CTAs, one per bin, each loading a
+    quarter of the rows of all 4 bins as whole 32-byte sectors and storing
+    the other bins' bf16 hi/lo chunks into its peers' operand rings) forms
+    the same operands as k_xc_pack and runs the same MMAs in the same order:
+    its stack equals the packed path's bit for bit, with a partial last
+    K-block, a last cluster past nspec, autocorrelations and reversed
+    pairs; and the FP64 oracle within 2e-5. Rows padded to a multiple of 4
+    bins; an odd pitch, or a window mask, falls back to the packed path."""
     torch = torch_cuda
     from fastxc_gb300._lib import FXC_XC_LAYOUT_WHOLE_BIN as WHOLE
+    from fastxc_gb300._lib import lib
     from fastxc_gb300.core import PairPlan
 
     rng = np.random.default_rng(nchan * 7 + nwin)
-    nspec = 301
+    pitch = (nspec + 3) // 4 * 4
     spec = make_spec(rng, nwin, nchan, nspec)
+    padded = np.zeros((nwin, nchan, pitch), np.complex64)
+    padded[:, :, :nspec] = spec
     iu, ju = np.triu_indices(nchan)
     keep = rng.random(iu.size) < 0.4
     src, rec = iu[keep].astype(np.int32), ju[keep].astype(np.int32)
@@ -172,21 +178,38 @@ def test_fused_pack_contraction_equals_packed(ctx, torch_cuda, monkeypatch, ncha
     plan = PairPlan(ctx, src, rec, nchan)
     plan.set_layout(WHOLE)
     assert plan.layouts(nwin)[1] == WHOLE
-    d_spec = torch.from_numpy(spec).cuda()
+    d_spec = torch.from_numpy(padded).cuda()
     d_mask = torch.from_numpy(mask).cuda()
-    out = {}
+    out, launches = {}, {}
     for packed in (False, True):
         monkeypatch.setenv("FXC_GEMM_FUSED", "0" if packed else "1")
         ctx.kernel_timing(True)
         st = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
-        ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, d_mask, 0.5, st, nspec, 1)
+        lib().fxc_launch_count_reset()
+        ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, pitch, None, 0.5, st, nspec, 1)
         ctx.synchronize()
+        launches[packed] = lib().fxc_launch_count()
         assert ctx.kernel_time("k_xc_tc_gemm_bin")[1] == 1
         ctx.kernel_timing(False)
         out[packed] = st.cpu().numpy()
+    assert launches == {False: 2, True: 3}, launches  # the fused path launches no pack
     assert np.array_equal(out[False], out[True])
-    ref = xo.xc_stack(spec, src, rec, 0.5, mask)
+    ref = xo.xc_stack(spec, src, rec, 0.5)
     assert rel_l2(out[False], ref) < 2e-5
+    # an odd pitch (no 16-byte copies of bin pairs) or a mask: the packed path
+    monkeypatch.setenv("FXC_GEMM_FUSED", "1")
+    odd = np.zeros((nwin, nchan, pitch + 1), np.complex64)
+    odd[:, :, :nspec] = spec
+    for arr, pt, m in ((odd, pitch + 1, None), (padded, pitch, d_mask)):
+        st = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
+        lib().fxc_launch_count_reset()
+        ctx.xc_stack(plan, torch.from_numpy(arr).cuda(), nwin, nchan, nspec, pt, m, 0.5, st, nspec, 1)
+        ctx.synchronize()
+        assert lib().fxc_launch_count() == 3
+        if m is None:
+            assert np.array_equal(st.cpu().numpy(), out[True])
+        else:
+            assert rel_l2(st.cpu().numpy(), xo.xc_stack(spec, src, rec, 0.5, mask)) < 2e-5
 
 
 @pytest.mark.parametrize("nchan,nwin", [(96, 24), (192, 130)])
