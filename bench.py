@@ -343,10 +343,16 @@ def serving_run(args, device: int, rank: int) -> dict:
         srv.close()
     lat = np.array([r["latency"] for r in recs]) if recs else np.zeros(1)
     qw = np.array([r["queue"] for r in recs]) if recs else np.zeros(1)
+    svc = lat - qw  # start -> results in host memory, queueing excluded
     pwin = float(sum(r["pair_windows"] for r in recs))
     return {"jobs": len(recs), "arrival_rate_per_s": args.serve_rate, "arrival_seconds": args.serve_seconds,
             "slots": args.serve_slots, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "mean_queue_s": float(qw.mean()),
+            "p50_service_s": float(np.percentile(svc, 50)), "p99_service_s": float(np.percentile(svc, 99)),
+            "mean_service_s": float(svc.mean()),
+            # service seconds offered per slot-second of the arrival window:
+            # above 1 the stream outruns the slots and latency is queueing
+            "offered_load": float(svc.sum() / max(args.serve_seconds * args.serve_slots, 1e-9)),
             "max_latency_s": float(lat.max()), "pair_windows": pwin,
             "pair_windows_per_s": pwin / wall if wall > 0 else None, "makespan_s": wall,
             "pws_jobs": int(sum(r["pws"] for r in recs)), "cache_entries_end": int(st.cache_entries),
@@ -959,6 +965,15 @@ def main():
     }
     if "tensor" in results:
         line["tensor_vs_plain_speedup"] = results["plain"]["ms_per_step"] / results["tensor"]["ms_per_step"]
+        # the two kernels' own fractions beside the ratio: the plain stack
+        # against the FP32 FMA peak (useful flops), the contraction against
+        # the bf16 peak of its roofline (issued MMA flops)
+        sm_max = peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        plain_tf = useful_flop / (results["plain"]["stack_ms"] / 1e3) / 1e12
+        line["speedup_kernels"] = {"plain_stack_tflops": plain_tf, "plain_stack_fp32_frac": plain_tf / fp32_peak,
+                                   "fp32_peak_tflops": fp32_peak,
+                                   "contraction_bf16_frac": roofline["frac"] if head == "tensor" else None}
 
     # end-to-end through the host-buffer C-ABI call
     if not args.no_e2e:
