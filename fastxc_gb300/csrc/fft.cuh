@@ -48,6 +48,8 @@ __host__ __device__ inline uint32_t fft_lmag(int L) {
 // and 4, 8 (the row kernels of the stacking stages, whose shared dispatch
 // would otherwise carry the composite stages).
 int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out, bool composites = true);
+// The same with the largest composite radix given (0: none).
+int fft_make_plan_limited(int n, const float2* tw, int tw_stride, FftPlan* out, int max_composite);
 // Cached device table perm[k] = fft_digit_pos(k) for the plan's radix order.
 int fft_perm_table(const FftPlan& p, const int** out);
 // Plan whose twiddle and digit-reversal tables are supplied by the caller

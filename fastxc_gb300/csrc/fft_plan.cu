@@ -36,7 +36,9 @@ static int max_composite_for(int n) {
 // then the remaining primes; composites above max_composite_for(n) are not
 // formed. Fewer stages mean fewer passes over shared memory and fewer
 // barriers, as long as every radix fits one thread's registers.
-static bool factorize(int n, std::vector<int>* out, bool composites = true) {
+// max_composite < 0: the default for the length (max_composite_for); 0: no
+// composite radices; otherwise the largest composite formed.
+static bool factorize(int n, std::vector<int>* out, int max_composite = -1) {
   out->clear();
   if (n < 1) return false;
   int m = n;
@@ -59,7 +61,7 @@ static bool factorize(int n, std::vector<int>* out, bool composites = true) {
     --it->second;
     return true;
   };
-  const int cmax = composites ? max_composite_for(n) : 0;
+  const int cmax = max_composite < 0 ? max_composite_for(n) : max_composite;
   for (; twos >= 3; twos -= 3) out->push_back(8);
   if (twos == 1) {
     if (cmax >= 14 && take(7)) out->push_back(14);
@@ -110,8 +112,12 @@ bool fft_length_supported(int n) {
 }
 
 int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out, bool composites) {
+  return fft_make_plan_limited(n, tw, tw_stride, out, composites ? -1 : 0);
+}
+
+int fft_make_plan_limited(int n, const float2* tw, int tw_stride, FftPlan* out, int max_composite) {
   std::vector<int> f;
-  if (!factorize(n, &f, composites)) {
+  if (!factorize(n, &f, max_composite)) {
     set_error("FFT length %d has a prime factor above 31 (not supported by the in-CTA FFT)", n);
     return FXC_ERR_UNSUPPORTED;
   }

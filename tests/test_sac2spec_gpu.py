@@ -189,10 +189,12 @@ def test_station_cluster_kernel_matches_three_kernel_path(ctx, torch_cuda, monke
     one launch) whose CTAs exchange the RAM and whitening weights through
     distributed shared memory; the same call with FXC_S2S_FUSED=0 runs the
     kernel chain that passes rows and weights through global memory. Both
-    against the FP64 oracle, and against each other within 1e-6 (the RAM
-    weights are chunked in the cluster kernel, the whitening weight is the
-    same float sum in both). One-bit rows can flip within FP32 rounding of
-    zero: 1e-3 there, as in the mode tests."""
+    against the FP64 oracle within 1e-5, and against each other within
+    1e-5: the cluster kernel's transforms use radix plans with composites
+    up to 10, the chain's up to 21, so the two round differently (most where
+    the filter's upper edge nears the Nyquist frequency, at 0.2 s). One-bit
+    rows can flip within FP32 rounding of zero: 1e-3 there, as in the mode
+    tests."""
     torch = torch_cuda
     from fastxc_gb300._lib import lib
 
@@ -213,4 +215,4 @@ def test_station_cluster_kernel_matches_three_kernel_path(ctx, torch_cuda, monke
         assert row_err(got, ref).max() < (1e-3 if onebit else 1e-5)
     e = row_err(fused, chain)
     print("cluster kernel vs kernel chain, row errors", np.array2string(e, precision=2))
-    assert e.max() < (1e-3 if onebit else 1e-6), e
+    assert e.max() < (1e-3 if onebit else 1e-5), e
