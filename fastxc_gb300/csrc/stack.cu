@@ -124,6 +124,12 @@ __device__ __forceinline__ float weight_pow(float mag2, float power) {
 // PWS: one CTA per (pair, chunk of groups)
 // ---------------------------------------------------------------------------
 
+// 1 / max(|z|, 1e-7) for |z|^2 = m2 (cudaNormalizeComplex's floored
+// modulus) by one reciprocal square root: within a few ulp of the division
+// by the square root, and two IEEE divisions and a square root per sample
+// fewer in the phase loops.
+__device__ __forceinline__ float inv_mod_floor(float m2) { return m2 > 1e-14f ? rsqrtf(m2) : 1e7f; }
+
 // CTA (pair p, chunk c) sums the weighted unit phasors of groups
 // [c * cg, (c + 1) * cg) of pair p into partial row (p, c); k_pws_combine
 // adds a pair's partial rows in chunk order. Chunks keep the grid many
@@ -177,16 +183,16 @@ __global__ void __launch_bounds__(kStT)
         const float2 h = buf[t];
         // cudaNormalizeComplex (modulus floored at 1e-7) + cudaWeightedMeanBatch
         float re = x1[t] - m1, im = h.x * invn;
-        float mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+        float s = inv_mod_floor(re * re + im * im) * w1;
         float2 ac = acc[t];
-        ac.x += (re / mod) * w1;
-        ac.y += (im / mod) * w1;
+        ac.x += re * s;
+        ac.y += im * s;
         if (two) {
           re = x2[t] - m2;
           im = h.y * invn;
-          mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
-          ac.x += (re / mod) * w2;
-          ac.y += (im / mod) * w2;
+          s = inv_mod_floor(re * re + im * im) * w2;
+          ac.x += re * s;
+          ac.y += im * s;
         }
         acc[t] = ac;
       }
@@ -206,11 +212,10 @@ __global__ void __launch_bounds__(kStT)
         // cudaNormalizeComplex: z / nfft, modulus floored at 1e-7
         const float2 z = buf[t];
         const float re = z.x * invn, im = z.y * invn;
-        float mod = sqrtf(re * re + im * im);
-        mod = (mod > 1e-7f) ? mod : 1e-7f;
         // cudaWeightedMeanBatch
-        acc[t].x += (re / mod) * wg;
-        acc[t].y += (im / mod) * wg;
+        const float sc = inv_mod_floor(re * re + im * im) * wg;
+        acc[t].x += re * sc;
+        acc[t].y += im * sc;
       }
     }
   }
@@ -274,19 +279,19 @@ __global__ void __launch_bounds__(kStT)
     for (int t = threadIdx.x; t < n; t += kStT) {
       const float2 h = buf[t];
       float re = x1[t] - m1, im = h.x * invn;
-      float mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+      float sc = inv_mod_floor(re * re + im * im) * w;
       float2 v = ac1[t];
-      v.x += (re / mod) * w;
-      v.y += (im / mod) * w;
+      v.x += re * sc;
+      v.y += im * sc;
       ac1[t] = v;
       li1[t] += x1[t] * w;
       if (two) {
         re = x2[t] - m2;
         im = h.y * invn;
-        mod = fmaxf(sqrtf(re * re + im * im), 1e-7f);
+        sc = inv_mod_floor(re * re + im * im) * w;
         v = ac1[n + t];
-        v.x += (re / mod) * w;
-        v.y += (im / mod) * w;
+        v.x += re * sc;
+        v.y += im * sc;
         ac1[n + t] = v;
         li1[n + t] += x2[t] * w;
       }
@@ -306,11 +311,10 @@ __global__ void __launch_bounds__(kStT)
   for (int t = threadIdx.x; t < n; t += kStT) {
     const float2 z = buf[t];
     const float re = z.x * invn, im = z.y * invn;
-    float mod = sqrtf(re * re + im * im);
-    mod = (mod > 1e-7f) ? mod : 1e-7f;
+    const float sc = inv_mod_floor(re * re + im * im) * w;
     float2 v = ac[t];
-    v.x += (re / mod) * w;
-    v.y += (im / mod) * w;
+    v.x += re * sc;
+    v.y += im * sc;
     ac[t] = v;
     li[t] += x[t] * w;
   }
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(kStT)
   }
   const int64_t goff = goffs[pair];
   const int ng = gcounts[pair];
-  const float nf = (float)n;
+  const float invnf = 1.0f / (float)n;
   for (int g = 0; g < ng; ++g) {
     const float2* X = Xg + (goff + g) * n;
     const float wg = weights[goff + g];
@@ -433,12 +437,14 @@ __global__ void __launch_bounds__(kStT)
     __syncthreads();
     any_inverse<kStT>(buf, a, stw);  // voice of group g (unnormalised C2C inverse)
     for (int t = threadIdx.x; t < n; t += kStT) {
-      // calculateWeightSub
+      // calculateWeightSub: wg z / (|z| N), a modulus <= 1e-7 taken as 1;
+      // 1/|z| by one reciprocal square root (within a few ulp of the two
+      // divisions by |z| N)
       const float x = buf[t].x, y = buf[t].y;
-      float fa = sqrtf(x * x + y * y);
-      if (fa <= 1e-7f) fa = 1.0f;
-      W[t].x += wg * x / (fa * nf);
-      W[t].y += wg * y / (fa * nf);
+      const float m2 = x * x + y * y;
+      const float sc = wg * (m2 <= 1e-14f ? 1.0f : rsqrtf(m2)) * invnf;
+      W[t].x += x * sc;
+      W[t].y += y * sc;
     }
   }
   __syncthreads();
