@@ -249,6 +249,52 @@ __device__ __noinline__ void boxcar_inplace(float* a, int n, int win, F2c inv) {
   __syncthreads();
 }
 
+// The boxcar (no abs) of a row of length n for the outputs c in [lo, hi),
+// window [c - half, c - half + win - 1] clipped to [0, n), from
+// u[j - u0] = the row at j for every j the windows reach (u0 = max(0,
+// lo - half) .. min(n, hi - half + win)); each output overwrites u[c - u0]
+// once every thread has read its windows (runs of odd length held in
+// registers, hi - lo <= RMAX x threads). Ends with the CTA synchronised.
+template <int RMAX>
+__device__ __noinline__ void boxcar_sub_inplace(float* u, int u0, int n, int win, F2c inv, int lo, int hi) {
+  const int per = odd_run(hi - lo);
+  const int c0 = lo + threadIdx.x * per;
+  const int c1 = min(hi, c0 + per);
+  float r[RMAX];
+  if (c0 < hi) {
+    const int half = win / 2;
+    const int wlo = max(0, c0 - half), whi = min(n - 1, c0 - half + win - 1);
+    float s4[4] = {0.f, 0.f, 0.f, 0.f}, k4[4] = {0.f, 0.f, 0.f, 0.f};
+    int j = wlo;
+    for (; j + 3 <= whi; j += 4) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) kahan_add(s4[q], k4[q], u[j + q - u0]);
+    }
+    for (; j <= whi; ++j) kahan_add(s4[0], k4[0], u[j - u0]);
+    float s = 0.f, comp = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      kahan_add(s, comp, s4[q]);
+      kahan_add(s, comp, -k4[q]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < RMAX; ++jj) {
+      const int c = c0 + jj;
+      if (c < c1) {
+        r[jj] = mul_f2c(s, inv);
+        const int out = c - half, in = c - half + win;
+        if (out >= 0 && out < n) kahan_add(s, comp, -u[out - u0]);
+        if (in >= 0 && in < n) kahan_add(s, comp, u[in - u0]);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int jj = 0; jj < RMAX; ++jj)
+    if (c0 + jj < c1) u[c0 + jj - u0] = r[jj];
+  __syncthreads();
+}
+
 // RAM divide of one sample (runabsNormalizeSharedWeight) by the station
 // weight s, the float sum of the component weights in component order:
 // s clamped to MINVAL, x / s, NaN -> 0, clip to +-MAXVAL.
@@ -784,32 +830,30 @@ __global__ void __launch_bounds__(kS2sT, 1)
 // exchange buffer fit one CTA's shared memory. The components' coupling --
 // the station RAM weight (the sum of the three smoothed |x|) and the
 // station whitening weight (the sum of the three smoothed |X|) -- goes
-// through distributed shared memory: each CTA keeps its component's values
-// in its own `aux` buffer and reads the two others' at the same index, in
-// component order. Rows never leave shared memory between the window load
-// and the spectrum store.
+// through distributed shared memory, and rows never leave shared memory
+// between the window load and the spectrum store.
 //
-// RAM weights cover seg samples, more than `aux` holds next to the row, so
-// they go in chunks of aux_floats outputs: a chunk's weights need the
-// undivided |x| up to half a window past its end, so the last half window
-// of each chunk is divided only after the next chunk's weights are formed
-// (its station weights wait in `side`). The whitening amplitudes (seg/2 + 1
-// bins) fit `aux` whole; each thread smooths its run of bins in registers
-// and writes it back in place.
+// RAM: a row of weights is more than `aux` holds next to the row, so CTA r
+// forms the station weight only for its third of the samples, as the
+// boxcar of |x_E| + |x_N| + |x_Z| (equal to the sum of the three smoothed
+// |x|: the boxcar is linear), reading the peers' rows; every CTA then reads
+// each sample's weight from the CTA that owns its third. Whitening: each
+// CTA smooths its own amplitudes (seg/2 + 1 bins fit `aux` whole) and reads
+// the two others' at the same bin, in component order. Smoothing runs hold
+// their outputs in registers and write them back in place.
 //
 // Every cluster barrier below is reached unconditionally or under a
 // condition uniform over the grid (the mode and plan), so the three CTAs
 // always meet at the same barriers.
 
 constexpr int kStationCtas = 3;
-constexpr int kFusedSideMax = 2048;   // half RAM window held between chunks (samples)
 
 struct S2sFused {
   int mode;        // 0 = none, 1 = one-bit, 2 = RAM
   int whiten;      // 1: whitening after the normalisation
   int raw_win;     // RAM boxcar width
   int ww;          // whitening boxcar width
-  int aux_floats;  // exchange buffer (floats): a RAM chunk, or the whitening bins
+  int aux_floats;  // exchange buffer (floats): a third of the RAM row + halo, or the whitening bins
   int twmax;       // twiddle table elements (largest of the plans)
   int mbuf;        // row buffer (complex elements)
 };
@@ -824,7 +868,6 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
   float2* sbuf = smraw;
   float2* stw = smraw + fz.mbuf;
   float* aux = reinterpret_cast<float*>(stw + fz.twmax);
-  float* side = aux + fz.aux_floats;
   float* xs = reinterpret_cast<float*>(sbuf);
   const int rank = (int)cl.block_rank();
   const float* peer[kStationCtas];
@@ -848,34 +891,41 @@ __global__ void __cluster_dims__(kStationCtas, 1, 1) __launch_bounds__(kS2sT, 1)
     __syncthreads();
   }
 
-  // RAM: station weight = sum of the components' smoothed |x|
+  // RAM: station weight = the boxcar of |x_E| + |x_N| + |x_Z| (the sum of
+  // the components' smoothed |x|: the boxcar is linear). CTA r forms it for
+  // the outputs of its third of the row, from its peers' rows through
+  // distributed shared memory, smoothed in place in `aux`; every CTA then
+  // divides its row by the weight of the third that owns each sample.
   if (fz.mode == 2) {
     const int win = fz.raw_win, half = win / 2;
-    const int L = fz.aux_floats;
-    int prev_tail = 0;
-    for (int lo = 0; lo < seg; lo += L) {
-      const int hi = min(seg, lo + L);
-      boxcar_range<true>(xs, seg, win, d.inv_rw, lo, hi, aux);
-      cl.sync();  // the three components' weights of [lo, hi) are in place
-      // the previous chunk's last half window, now that this chunk's
-      // weights have read it
-      for (int i = threadIdx.x; i < prev_tail; i += kS2sT) {
-        const int c = lo - prev_tail + i;
-        xs[c] = ram_divide_s(xs[c], side[i]);
-      }
-      __syncthreads();
-      const int tail = hi == seg ? 0 : min(half, hi - lo);
-      batched_rows<4>(
-          hi - lo, [&](int i) { return peer[0][i] + peer[1][i] + peer[2][i]; },
-          [&](int i, float sw) {
-            if (i < hi - lo - tail)
-              xs[lo + i] = ram_divide_s(xs[lo + i], sw);
-            else
-              side[i - (hi - lo - tail)] = sw;
-          });
-      prev_tail = tail;
-      cl.sync();  // every component done reading this chunk's weights
-    }
+    const int L3 = (seg + kStationCtas - 1) / kStationCtas;
+    const int lo = min(seg, rank * L3), hi = min(seg, lo + L3);
+    const int u0 = max(0, lo - half), u1 = min(seg, hi - half + win);
+    const float* px[kStationCtas];
+#pragma unroll
+    for (int c = 0; c < kStationCtas; ++c) px[c] = c == rank ? xs : cl.map_shared_rank(xs, c);
+    cl.sync();  // every component's prefiltered row is final
+    batched_rows<4>(
+        max(0, u1 - u0), [&](int i) { return fabsf(px[0][u0 + i]) + fabsf(px[1][u0 + i]) + fabsf(px[2][u0 + i]); },
+        [&](int i, float v) { aux[i] = v; });
+    __syncthreads();
+    // runs of 13 at one day of 0.1 s windows (L3 = 12 000): the shorter
+    // register array keeps the loop free of spills
+    if (L3 <= 13 * kS2sT)
+      boxcar_sub_inplace<13>(aux, u0, seg, win, d.inv_rw, lo, hi);
+    else
+      boxcar_sub_inplace<kRunRegs>(aux, u0, seg, win, d.inv_rw, lo, hi);
+    cl.sync();  // every third's weights are in place; no peer reads the rows any more
+    const int b1 = L3, b2 = 2 * L3;
+    const int s1 = max(0, b1 - half), s2 = max(0, b2 - half);  // u0 of thirds 1 and 2
+    batched_rows<4>(
+        seg,
+        [&](int c) {
+          const int q = (c >= b1) + (c >= b2);
+          return peer[q][c - (q == 0 ? 0 : (q == 1 ? s1 : s2))];
+        },
+        [&](int c, float sw) { xs[c] = ram_divide_s(xs[c], sw); });
+    cl.sync();  // every component done reading the weights
   }
 
   // whitening: X / (sum of the components' smoothed |X|), band taper
@@ -938,18 +988,19 @@ static int s2s_run_fused(fxc_ctx* ctx, const fxc_s2s_plan* plan, const S2sDev& d
     fz.mbuf = std::max(fz.mbuf, ps.n);
     fz.twmax = std::max(fz.twmax, fft_tw_smem_elems(ps));
   }
-  const int half = fz.mode == 2 ? fz.raw_win / 2 : 0;
-  if (half > kFusedSideMax) return FXC_ERR_UNSUPPORTED;
-  const int side = (half + 3) / 4 * 4;
   cudaFuncAttributes attr;
   FXC_CUDA_TRY(cudaFuncGetAttributes(&attr, k_s2s_station));
   const int64_t budget = 227 * 1024 - (int64_t)attr.sharedSizeBytes;
-  const int64_t fixed = 8 * (int64_t)fz.mbuf + 8 * (int64_t)fz.twmax + 4 * (int64_t)side;
+  const int64_t fixed = 8 * (int64_t)fz.mbuf + 8 * (int64_t)fz.twmax;
   const int64_t aux = (budget - fixed) / 16 * 4;
   if (aux < 4) return FXC_ERR_UNSUPPORTED;
   fz.aux_floats = (int)aux;
   if (fz.whiten && (ps.n + 1 > fz.aux_floats || ps.n + 1 > kRunRegs * kS2sT)) return FXC_ERR_UNSUPPORTED;
-  if (fz.mode == 2 && fz.aux_floats <= half) return FXC_ERR_UNSUPPORTED;
+  if (fz.mode == 2) {
+    // a third of the row plus a window of halo, smoothed in registers
+    const int l3 = (d.seg + kStationCtas - 1) / kStationCtas;
+    if (l3 + fz.raw_win > fz.aux_floats || l3 > kRunRegs * kS2sT) return FXC_ERR_UNSUPPORTED;
+  }
   const size_t smem = (size_t)(fixed + 4 * aux);
   FXC_CUDA_TRY(cudaFuncSetAttribute(k_s2s_station, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   {
