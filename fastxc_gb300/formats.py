@@ -143,7 +143,8 @@ def sac_header_bytes(npts: int, delta: float, b: float = 0.0, **fields) -> bytes
 def write_sourcepack(root, name: str, rows) -> Path:
     """One SourcePack shard: <name>.pack of SAC records and <name>.tsv index.
     rows: dicts with the index columns (except record_path, record_offset,
-    bytes, npts, dt) plus 'data' (float32 trace) and 'delta'."""
+    bytes, npts, dt) plus 'data' (float32 trace), 'delta' and optionally
+    'sac' (extra header fields for sac_header_bytes)."""
     root = Path(root).resolve()
     root.mkdir(parents=True, exist_ok=True)
     pack, tsv = root / f"{name}.pack", root / f"{name}.tsv"
@@ -151,7 +152,8 @@ def write_sourcepack(root, name: str, rows) -> Path:
         th.write("\t".join(SOURCEPACK_COLUMNS) + "\n")
         for r in rows:
             data = np.ascontiguousarray(r["data"], "<f4")
-            blob = sac_header_bytes(data.size, r["delta"], b=-(data.size // 2) * r["delta"]) + data.tobytes()
+            blob = sac_header_bytes(data.size, r["delta"], b=-(data.size // 2) * r["delta"],
+                                    **r.get("sac", {})) + data.tobytes()
             off = fh.tell()
             fh.write(blob)
             row = dict(r, record_path=str(pack), record_offset=off, bytes=len(blob), npts=data.size,
