@@ -50,6 +50,10 @@ __host__ __device__ inline uint32_t fft_lmag(int L) {
 int fft_make_plan(int n, const float2* tw, int tw_stride, FftPlan* out, bool composites = true);
 // The same with the largest composite radix given (0: none).
 int fft_make_plan_limited(int n, const float2* tw, int tw_stride, FftPlan* out, int max_composite);
+// The default stages in ascending radix order: the smallest first, the
+// largest last (for a transform whose first stage loads its inputs and whose
+// last stage is formed at a few frequencies only).
+int fft_make_plan_ascending(int n, const float2* tw, int tw_stride, FftPlan* out);
 // Cached device table perm[k] = fft_digit_pos(k) for the plan's radix order.
 int fft_perm_table(const FftPlan& p, const int** out);
 // Plan whose twiddle and digit-reversal tables are supplied by the caller
@@ -503,6 +507,114 @@ __device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool i
                                  inverse && s == 0);
     L *= R;
   }
+}
+
+// ---- pieces of a DIF transform whose input is formed on the fly and whose
+// output is needed at a few frequencies only (the C2R + lag cut of the xc
+// finalize) -----------------------------------------------------------------
+
+// DIF stage 0 (one block of n points at stride L = n / R) with its inputs
+// taken from load(k) instead of buf; buf then holds what fft_dif's stage 0
+// leaves. load returns the butterfly input as is (any conjugation of an
+// inverse transform already applied); it is a small value type (pointers
+// and sizes), passed by value into the out-of-line stage.
+template <int R, int T, class Load>
+__device__ __noinline__ void fft_stage0_load_r(float2* buf, int L, const float2* stw, int tw_step, Load load) {
+  for (int j = threadIdx.x; j < L; j += T) {
+    float2 x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[t] = load(j + t * L);
+    dft_any<R>(x);
+    if (j != 0) apply_twiddles<R>(stw, j * tw_step, x);
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[j + t * L] = x[t];
+  }
+  __syncthreads();
+}
+
+// Stage 0 of a plan with at least two stages (stage 0 is then never the
+// last, so no output conjugation applies).
+template <int T, bool COMP = true, class Load>
+__device__ __forceinline__ void fft_dif_stage0_load(float2* buf, const FftPlan& p, const float2* stw,
+                                                    const Load& load) {
+  const int R = p.radix[0];
+  const int L = p.n / R;
+  const int ts = p.tw_stride;
+  if constexpr (COMP) {
+    switch (R) {
+      case 6: fft_stage0_load_r<6, T>(buf, L, stw, ts, load); return;
+      case 9: fft_stage0_load_r<9, T>(buf, L, stw, ts, load); return;
+      case 10: fft_stage0_load_r<10, T>(buf, L, stw, ts, load); return;
+      case 12: fft_stage0_load_r<12, T>(buf, L, stw, ts, load); return;
+      case 14: fft_stage0_load_r<14, T>(buf, L, stw, ts, load); return;
+      case 15: fft_stage0_load_r<15, T>(buf, L, stw, ts, load); return;
+      case 21: fft_stage0_load_r<21, T>(buf, L, stw, ts, load); return;
+      default: break;
+    }
+  }
+  switch (R) {
+    case 2: fft_stage0_load_r<2, T>(buf, L, stw, ts, load); break;
+    case 4: fft_stage0_load_r<4, T>(buf, L, stw, ts, load); break;
+    case 8: fft_stage0_load_r<8, T>(buf, L, stw, ts, load); break;
+    case 3: fft_stage0_load_r<3, T>(buf, L, stw, ts, load); break;
+    case 5: fft_stage0_load_r<5, T>(buf, L, stw, ts, load); break;
+    case 7: fft_stage0_load_r<7, T>(buf, L, stw, ts, load); break;
+    case 11: fft_stage0_load_r<11, T>(buf, L, stw, ts, load); break;
+    case 13: fft_stage0_load_r<13, T>(buf, L, stw, ts, load); break;
+    case 17: fft_stage0_load_r<17, T>(buf, L, stw, ts, load); break;
+    case 19: fft_stage0_load_r<19, T>(buf, L, stw, ts, load); break;
+    case 23: fft_stage0_load_r<23, T>(buf, L, stw, ts, load); break;
+    case 29: fft_stage0_load_r<29, T>(buf, L, stw, ts, load); break;
+    case 31: fft_stage0_load_r<31, T>(buf, L, stw, ts, load); break;
+    default: break;  // rejected by fft_make_plan
+  }
+}
+
+// DIF stages [s0, s1) with neither input nor output conjugation (stages
+// strictly between the first and the last of an inverse transform).
+template <int T, bool COMP = true>
+__device__ __forceinline__ void fft_dif_inner(float2* buf, const FftPlan& p, const float2* stw, int s0,
+                                              int s1) {
+  int L = p.n;
+  int Rprod = 1;
+  for (int s = 0; s < s1; ++s) {
+    const int R = p.radix[s];
+    L /= R;
+    if (s >= s0) fft_run_stage<T, false, COMP>(buf, p, stw, R, L, p.lmag[s], Rprod * p.tw_stride, false, false);
+    Rprod *= R;
+  }
+}
+
+// Frequency k of the DIF result, from buf as it stands before the last
+// stage (blocks of R = radix[S-1] adjacent points, no twiddles in that
+// stage): k's last digit t = k / (n / R) picks the butterfly output
+//   sum_u buf[base + u] w_R^{t u},  base = perm[k] - t,
+// with w_R^v read from the twiddle table as w_n^{v n / R} (and advanced by
+// multiplication between table reads, as apply_twiddles does).
+__device__ __forceinline__ float2 fft_dif_last_point(const float2* buf, const FftPlan& p, const float2* stw,
+                                                     int k) {
+  const int R = p.radix[p.nstages - 1];
+  const int nr = p.n / R;
+  const int t = k / nr;
+  const int base = __ldg(p.perm + k) - t;
+  float2 acc = buf[base];
+  if (t == 0) {
+    for (int u = 1; u < R; ++u) acc = cadd(acc, buf[base + u]);
+    return acc;
+  }
+  const int step = nr * p.tw_stride;
+  const float2 w1 = tw_lookup(stw, t * step);
+  float2 w = w1;
+  int v = t;  // t u mod R
+  for (int u = 1; u < R; ++u) {
+    if (u > 1) {
+      v += t;
+      if (v >= R) v -= R;
+      w = ((u - 1) & 7) == 0 ? tw_lookup(stw, v * step) : cmul(w, w1);
+    }
+    acc = cadd(acc, cmul(buf[base + u], w));
+  }
+  return acc;
 }
 
 // Position of natural-order frequency k in the digit-reversed layout:

@@ -1,5 +1,6 @@
 // Host side of the FFT library: factorisation into Stockham stages and the
 // per-device cache of twiddle tables.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -121,6 +122,26 @@ int fft_make_plan_limited(int n, const float2* tw, int tw_stride, FftPlan* out, 
     set_error("FFT length %d has a prime factor above 31 (not supported by the in-CTA FFT)", n);
     return FXC_ERR_UNSUPPORTED;
   }
+  FftPlan p{};
+  p.n = n;
+  p.nstages = (int)f.size();
+  for (int i = 0; i < p.nstages; ++i) p.radix[i] = f[i];
+  fill_lmag(&p);
+  p.tw = tw;
+  p.tw_stride = tw_stride;
+  p.perm = nullptr;
+  FXC_TRY(fft_perm_table(p, &p.perm));
+  *out = p;
+  return FXC_OK;
+}
+
+int fft_make_plan_ascending(int n, const float2* tw, int tw_stride, FftPlan* out) {
+  std::vector<int> f;
+  if (!factorize(n, &f)) {
+    set_error("FFT length %d has a prime factor above 31 (not supported by the in-CTA FFT)", n);
+    return FXC_ERR_UNSUPPORTED;
+  }
+  std::sort(f.begin(), f.end());
   FftPlan p{};
   p.n = n;
   p.nstages = (int)f.size();

@@ -296,6 +296,35 @@ __global__ void __launch_bounds__(256, 1)
 // out[j] = x[(nfft - half_cc + j) mod nfft] * inv_norm, where x is the
 // unshifted C2R result; multiplying bin f by (-1)^f shifts the series by
 // nfft/2, so the reference's cut start nfft/2 - half_cc lands here.
+//
+// The C2R runs as an M = nfft/2 point inverse complex DIF transform z[m] =
+// x[2m] + i x[2m+1] of the pre-processed bins, without two of its passes
+// over shared memory:
+//   * the pre-processing (and the inverse transform's input conjugation) is
+//     done on the loads of the first stage, which reads the bins from global
+//     memory itself;
+//   * the last stage is formed only at the complex points that hold kept
+//     lags (cc_size/2 + 1 of M: 1 001 of 18 522 at nfft 37 044), each as one
+//     R-term sum over its butterfly's inputs (fft_dif_last_point).
+// The plan's radices run in ascending order, so the pruned stage is the
+// largest.
+
+// bin k of the C2R input: Z[k] from X[k], X[M-k] (imaginary parts of the
+// DC and Nyquist bins ignored), conjugated for the inverse transform
+struct C2rBinLoad {
+  const float2* __restrict__ X;
+  const float2* __restrict__ twn;
+  int M;
+  __device__ __forceinline__ float2 operator()(int k) const {
+    float2 a = X[k], b = X[M - k];
+    const float2 w = __ldg(twn + k);
+    if (k == 0) {
+      a.y = 0.f;
+      b.y = 0.f;
+    }
+    return conjf2(c2r_pre_w(a, b, w));
+  }
+};
 
 template <int T, int NMAX>
 __global__ void __launch_bounds__(T, 1)
@@ -307,43 +336,32 @@ __global__ void __launch_bounds__(T, 1)
   const int N = 2 * M;
   float2* stw = buf + M;
   fft_twiddles_to_smem<T>(p, stw);
-  const float2* X = stack + (int64_t)blockIdx.x * stack_pitch;
-  // the CTA holds its SM alone (the row fills shared memory), so the loads
-  // of four iterations are issued together rather than one trip at a time
-  constexpr int U = 4;
-  for (int k0 = threadIdx.x; k0 < M; k0 += U * T) {
-    float2 a[U], b[U], w[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int k = k0 + u * T;
-      if (k < M) {
-        a[u] = X[k];
-        b[u] = X[M - k];
-        w[u] = __ldg(twn + k);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int k = k0 + u * T;
-      if (k < M) {
-        if (k == 0) {
-          a[u].y = 0.f;
-          b[u].y = 0.f;
-        }
-        buf[k] = c2r_pre_w(a[u], b[u], w[u]);
-      }
-    }
+  const C2rBinLoad load{stack + (int64_t)blockIdx.x * stack_pitch, twn, M};
+  const int S = p.nstages;
+  if (S >= 2) {
+    __syncthreads();  // the twiddle table
+    fft_dif_stage0_load<T>(buf, p, stw, load);
+    fft_dif_inner<T>(buf, p, stw, 1, S - 1);
+  } else {
+    for (int k = threadIdx.x; k < M; k += T) buf[k] = load(k);
+    __syncthreads();
   }
-  __syncthreads();
-  fft_dif<T>(buf, p, stw, true);
+  // complex points k0 .. k0 + nq - 1 (mod M) hold the kept lags: point k
+  // carries reals m = 2k (real part) and 2k + 1 (imaginary part)
+  int m0 = N - half_cc;
+  if (m0 >= N) m0 -= N;
+  const int k0 = m0 >> 1;
+  const int nq = ((m0 + cc_size - 1) >> 1) - k0 + 1;
   float* out = ncf + (int64_t)blockIdx.x * cc_size;
-  for (int j = threadIdx.x; j < cc_size; j += T) {
-    int m = N - half_cc + j;
-    if (m >= N) m -= N;
-    const float2 v = buf[__ldg(p.perm + (m >> 1))];
-    const float x = (m & 1) ? v.y : v.x;
+  for (int q = threadIdx.x; q < nq; q += T) {
+    int k = k0 + q;
+    if (k >= M) k -= M;
+    // the inverse transform's output conjugation
+    const float2 v = conjf2(fft_dif_last_point(buf, p, stw, k));
+    const int j = 2 * (k0 + q) - m0;
     // InvNormalize2DKernel: float data times a double weight
-    out[j] = (float)((double)x * inv_norm);
+    if (j >= 0 && j < cc_size) out[j] = (float)((double)v.x * inv_norm);
+    if (j + 1 < cc_size) out[j + 1] = (float)((double)v.y * inv_norm);
   }
   (void)inv_norm_f;
 }
@@ -557,7 +575,7 @@ int xc_finalize_launch(fxc_ctx* ctx, const float2* stack, int64_t npairs, int64_
   const float2* twn = nullptr;
   FXC_TRY(fft_twiddles(N, &twn));
   FftPlan p;
-  FXC_TRY(fft_make_plan(M, twn, 2, &p));
+  FXC_TRY(fft_make_plan_ascending(M, twn, 2, &p));
   // 1/(width*dt) with width*dt in float, as InvNormalize2DKernel computes it
   const float wdt = (float)N * s->dt;
   const double inv_norm = 1.0 / (double)wdt;

@@ -465,6 +465,39 @@ def test_pruned_finalize_matches_oracle(ctx, torch_cuda, nspec, dt, lag, monkeyp
     assert per_row_rel_l2(full, ref).max() < NCF_RTOL
 
 
+# nspec - 1 = M, the complex transform length: one stage (31), two (58 =
+# 2 x 29), the 256-thread kernel's limit (4096 = 8^4), odd composites
+# (3003 = 3 x 7 x 11 x 13), five stages on the 1024-thread kernel
+# (5000 = 8 x 5^4), the 37 044-point transform of 0.1 s hourly windows
+# (18 522 = 2 x 3^3 x 7^3) and the 1024-thread kernel's limit (20 480)
+@pytest.mark.parametrize("nspec", [32, 59, 3004, 4097, 5001, 18523, 20481])
+def test_finalize_lag_cuts_match_oracle(ctx, torch_cuda, nspec):
+    """fxc_xc_finalize alone on random stacks: the C2R runs with its first
+    stage on the loads and its last stage formed only at the kept lags, so
+    cuts of one lag, odd and even half-widths and the widest cut (every
+    lag but one) are checked against numpy's FP64 irfft."""
+    torch = torch_cuda
+    from fastxc_gb300.core import xc_shape
+
+    rng = np.random.default_rng(nspec)
+    npairs = 5
+    M = nspec - 1
+    pitch = (nspec + 3) // 4 * 4
+    stack = (rng.standard_normal((npairs, pitch)) + 1j * rng.standard_normal((npairs, pitch))).astype(np.complex64)
+    d_stack = torch.from_numpy(stack).cuda()
+    for half in sorted({0, 1, 7, min(100, M - 1), M // 3 | 1, M - 1}):
+        lag = half + 0.25 if half else 0.4  # llround(lag / 1.0) = half
+        shape = xc_shape(nspec, 1, 1.0, lag)
+        assert shape.half_cc == half
+        out = torch.full((npairs, shape.cc_size), float("nan"), dtype=torch.float32, device="cuda")
+        ctx.xc_finalize(d_stack, npairs, pitch, shape, out)
+        ctx.synchronize()
+        got = out.cpu().numpy()
+        ref = xo.xc_finalize(stack[:, :nspec], xo.finalize_shape(nspec, 1, 1.0, lag))
+        assert np.all(np.isfinite(got)), (nspec, half)
+        assert per_row_rel_l2(got, ref).max() < NCF_RTOL, (nspec, half)
+
+
 @pytest.mark.parametrize("method", [0, 1], ids=["plain", "tensor"])
 def test_20hz_long_transform(ctx, torch_cuda, method):
     """delta 0.05 s, 3600-s windows, lag 200 s: nfft 76 000-class transforms
