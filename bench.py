@@ -1011,19 +1011,30 @@ def main():
             c1.record(stream)
             torch.cuda.synchronize()
             copy_ms = min(copy_ms, c0.elapsed_time(c1))
-        # one more call with the phase record on (CUDA events on both streams)
+        # three more calls with the phase record on (CUDA events on both
+        # streams), each with its wall time: whether a slow call's time is
+        # in its host-to-device copies or in the pipeline behind them
         ctx.kernel_timing(True)
-        ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
-        phases = ctx.host_phases()
+        phase_calls = []
+        for _ in range(3):
+            c0 = time.perf_counter()
+            ctx.xc_run_host(plan, hs, nwin, nchan, nspec, None, scale, shape, hn, m)
+            wall = (time.perf_counter() - c0) * 1e3
+            phase_calls.append(dict(ctx.host_phases(), wall=wall))
         ctx.kernel_timing(False)
+        phases = phase_calls[0]
         line["e2e"] = {"value": replicas.whole_job_rate(pw, world, el), "unit": "pair-windows/s",
                        "h2d_bytes_per_step": int(spec.numel() * 8), "d2h_bytes_per_step": int(npairs * shape.cc_size * 4),
                        "ms_per_step": el * 1e3, "steps": e2e_steps,
                        "h2d_copy_ms": copy_ms, "h2d_gbs": spec.numel() * 8 / (copy_ms / 1e3) / 1e9,
-                       "over_copy_floor": el * 1e3 / copy_ms, "ms_per_call": per_call, "phase_ms": phases,
-                       "phase_note": "one extra call with CUDA events on the copy and compute streams: copy_busy = "
-                                     "sum of H2D copy durations, compute_busy = sum of per-chunk compute, "
-                                     "tail = time after the last H2D copy ends"}
+                       "over_copy_floor": el * 1e3 / copy_ms, "ms_per_call": per_call,
+                       "median_ms_per_call": float(np.median(per_call)), "phase_ms": phases,
+                       "phase_calls": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in c.items()}
+                                       for c in phase_calls],
+                       "phase_note": "three extra calls with CUDA events on the copy and compute streams (phase_ms "
+                                     "is the first): copy_busy = sum of H2D copy durations, compute_busy = sum of "
+                                     "per-chunk compute, tail = time after the last H2D copy ends, wall = the "
+                                     "call's host wall time"}
 
     # the step's buffers are released before the stage timings and the
     # serving stream (which uses its own HBM arenas)
