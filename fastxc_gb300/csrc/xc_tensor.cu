@@ -450,6 +450,19 @@ __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Ties 16 registers that a tcgen05.ld fills asynchronously to this point:
+// placed after tcgen05.wait::ld, it keeps the compiler from moving their
+// first use above the wait (the load's outputs are otherwise ordinary
+// register values to it).
+__device__ __forceinline__ void reg_fence16(float (&v)[16]) {
+  asm volatile(""
+               : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]),
+                 "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]),
+                 "+f"(v[15])
+               :
+               : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -1092,6 +1105,271 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+// Persistent form of the packed whole-bin contraction: one CTA per SM runs
+// the bins blockIdx.x, blockIdx.x + G, ... with TMEM, the barriers and the
+// operand ring kept across bins (the per-bin CTA pays a launch, the TMEM
+// allocation, the ring's first loads and a smem-staged write-out, about a
+// fifth of its time at 720 windows). The producer streams the next bin's
+// K-blocks while the current bin's epilogue runs; the MMAs of a bin start
+// once the eight epilogue warps have read the previous bin's accumulators
+// (bar_tfree); the epilogue stores straight from registers by slot -- a
+// warp's 32 rows of one column are consecutive slots -- so the ring is
+// never borrowed for staging. Rows [C, 256) of every stage chunk are zeroed
+// once and no copy writes them.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_xc_tc_gemm_bin_p(const uint4* __restrict__ packed, int nspec, int nkb, int cpad, int nchan,
+                       const TcTile* __restrict__ tiles, int ntiles, const int32_t* __restrict__ maps,
+                       float scale, float2* __restrict__ binmajor, int64_t bin_pitch, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* stage_base = smem;
+  // full[kBinStages], empty[kBinStages], acc, tfree, drain
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)kBinStages * kBinStageBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kBinStages + 3);
+  const uint32_t bar_full0 = smem_u32(bars);
+  const uint32_t bar_empty0 = smem_u32(bars + kBinStages);
+  const uint32_t bar_acc = smem_u32(bars + 2 * kBinStages);
+  const uint32_t bar_tfree = smem_u32(bars + 2 * kBinStages + 1);
+  const uint32_t bar_drain = smem_u32(bars + 2 * kBinStages + 2);
+  const int G = (int)gridDim.x;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const TcTile t0 = tiles[0];
+  const bool two = ntiles > 1;
+  const TcTile t1 = two ? tiles[1] : t0;
+  const int n0 = t0.n, n1 = two ? t1.n : 0;
+  const uint32_t chunk_bytes = (uint32_t)kBinRows * 16;  // one (plane, kc) chunk
+
+  for (int s = 0; s < kBinStages; ++s) {
+    uint4* st = reinterpret_cast<uint4*>(stage_base + (size_t)s * kBinStageBytes);
+    const int per = kBinRows - nchan;
+    for (int i = threadIdx.x; i < kTcPlanes * kTcKc * per; i += kTcThreads) {
+      const int ch = i / per, r = nchan + i % per;
+      st[(size_t)ch * kBinRows + r] = make_uint4(0, 0, 0, 0);
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kBinStages; ++s) {
+      mbar_init(bar_full0 + 8 * s, 1);
+      mbar_init(bar_empty0 + 8 * s, 1);
+    }
+    mbar_init(bar_acc, 1);
+    mbar_init(bar_tfree, 8);
+    mbar_init(bar_drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  // TMEM columns: T0 Re [0, n0), T0 Im [n0, 2 n0), T1 Re [2 n0, 2 n0 + n1), T1 Im after
+  const uint32_t c_re0 = 0, c_im0 = (uint32_t)n0, c_re1 = 2u * n0, c_im1 = 2u * n0 + n1;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t tx = (uint32_t)kTcPlanes * kTcKc * (uint32_t)nchan * 16u;
+      int64_t q = 0;  // K-blocks issued
+      bool failed = false;
+      for (int f = blockIdx.x; f < nspec && !failed; f += G) {
+        for (int kb = 0; kb < nkb; ++kb, ++q) {
+          const int s = (int)(q % kBinStages);
+          const uint32_t ph = (uint32_t)(q / kBinStages) & 1u;
+          if (!mbar_wait(bar_empty0 + 8 * s, ph ^ 1u)) {
+            failed = true;
+            break;
+          }
+          const uint32_t full = bar_full0 + 8 * s;
+          mbar_expect_tx(full, tx);
+          const uint32_t st = smem_u32(stage_base + (size_t)s * kBinStageBytes);
+          for (int pl = 0; pl < kTcPlanes; ++pl) {
+            const int64_t pbase = (((int64_t)f * kTcPlanes + pl) * nkb + kb) * kTcKc * cpad;
+            for (int kc = 0; kc < kTcKc; ++kc)
+              bulk_g2s(st + (pl * kTcKc + kc) * chunk_bytes, packed + pbase + (int64_t)kc * cpad,
+                       (uint32_t)nchan * 16u, full);
+          }
+        }
+      }
+      if (failed) {
+        atomicExch(err, 1);
+        // the copies of the last issued K-blocks may still be in flight
+        for (int64_t r = q - 1; r >= 0 && r >= q - kBinStages; --r)
+          (void)mbar_wait(bar_full0 + 8 * (int)(r % kBinStages), (uint32_t)(r / kBinStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idp0 = umma_idesc(kTcM, n0, false), idn0 = umma_idesc(kTcM, n0, true);
+      const uint32_t idp1 = umma_idesc(kTcM, two ? n1 : 16, false), idn1 = umma_idesc(kTcM, two ? n1 : 16, true);
+      const uint32_t lbo = chunk_bytes;  // next 8-window chunk of the same plane
+      const uint32_t sbo = 128;
+      int64_t q = 0;
+      bool failed = false;
+      for (int f = blockIdx.x, li = 0; f < nspec && !failed; f += G, ++li) {
+        // the epilogue has read the previous bin's accumulators
+        if (li > 0 && !mbar_wait(bar_tfree, (uint32_t)(li - 1) & 1u)) {
+          failed = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        bool first = true;
+        for (int kb = 0; kb < nkb; ++kb, ++q) {
+          const int s = (int)(q % kBinStages);
+          const uint32_t ph = (uint32_t)(q / kBinStages) & 1u;
+          if (!mbar_wait(bar_full0 + 8 * s, ph)) {
+            failed = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = smem_u32(stage_base + (size_t)s * kBinStageBytes);
+#pragma unroll
+          for (int ks = 0; ks < kTcKc / 2; ++ks) {
+            uint64_t P0[4], P1[4];  // rows 0.. and rows 128.. of each plane at this K step
+#pragma unroll
+            for (int pl = 0; pl < 4; ++pl) {
+              const uint32_t base = st + (pl * kTcKc + ks * 2) * chunk_bytes;
+              P0[pl] = umma_desc(base, lbo, sbo);
+              P1[pl] = umma_desc(base + kTcM * 16, lbo, sbo);
+            }
+            const uint32_t acc = first ? 0u : 1u;
+            // tile 0: rows 0..127 x cols 0..n0-1
+            umma_bf16(tmem + c_re0, P0[0], P0[0], idp0, acc);
+            umma_bf16(tmem + c_re0, P0[0], P0[1], idp0, 1);
+            umma_bf16(tmem + c_re0, P0[1], P0[0], idp0, 1);
+            umma_bf16(tmem + c_re0, P0[2], P0[2], idp0, 1);
+            umma_bf16(tmem + c_re0, P0[2], P0[3], idp0, 1);
+            umma_bf16(tmem + c_re0, P0[3], P0[2], idp0, 1);
+            umma_bf16(tmem + c_im0, P0[0], P0[2], idp0, acc);
+            umma_bf16(tmem + c_im0, P0[0], P0[3], idp0, 1);
+            umma_bf16(tmem + c_im0, P0[1], P0[2], idp0, 1);
+            umma_bf16(tmem + c_im0, P0[2], P0[0], idn0, 1);
+            umma_bf16(tmem + c_im0, P0[2], P0[1], idn0, 1);
+            umma_bf16(tmem + c_im0, P0[3], P0[0], idn0, 1);
+            if (two) {
+              // tile 1: rows 128..255 (zero past C) x cols 128..128+n1-1
+              umma_bf16(tmem + c_re1, P1[0], P1[0], idp1, acc);
+              umma_bf16(tmem + c_re1, P1[0], P1[1], idp1, 1);
+              umma_bf16(tmem + c_re1, P1[1], P1[0], idp1, 1);
+              umma_bf16(tmem + c_re1, P1[2], P1[2], idp1, 1);
+              umma_bf16(tmem + c_re1, P1[2], P1[3], idp1, 1);
+              umma_bf16(tmem + c_re1, P1[3], P1[2], idp1, 1);
+              umma_bf16(tmem + c_im1, P1[0], P1[2], idp1, acc);
+              umma_bf16(tmem + c_im1, P1[0], P1[3], idp1, 1);
+              umma_bf16(tmem + c_im1, P1[1], P1[2], idp1, 1);
+              umma_bf16(tmem + c_im1, P1[2], P1[0], idn1, 1);
+              umma_bf16(tmem + c_im1, P1[2], P1[1], idn1, 1);
+              umma_bf16(tmem + c_im1, P1[3], P1[0], idn1, 1);
+            }
+            first = false;
+          }
+          umma_commit(bar_empty0 + 8 * s);  // stage free once these MMAs are done
+        }
+        if (!failed) umma_commit(bar_acc);  // this bin's accumulators are complete
+      }
+      if (failed) atomicExch(err, 1);
+      // every MMA issued has completed before TMEM is freed
+      umma_commit(bar_drain);
+      (void)mbar_wait(bar_drain, 0);
+    }
+  } else {
+    // epilogue warps 2..9: lane quarter qq = warp % 4 holds rows qq*32.. of
+    // both tiles; the two warps of a quarter take alternate 16-column chunks
+    // of the combined column space [0, n0) + [n0, n0 + n1). The pair map of
+    // the next chunk is fetched while the current one is stored.
+    const int qq = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int ncols = n0 + n1;
+    const int row = qq * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(qq * 32) << 16);
+    auto load_map = [&](int cc, int4 (&m)[4]) {
+      const bool in1 = cc >= n0;
+      const TcTile& tt = in1 ? t1 : t0;
+      if (cc < ncols && row < tt.am) {
+        const int4* m4 = reinterpret_cast<const int4*>(maps + tt.map_offset + (int64_t)row * (in1 ? n1 : n0) +
+                                                       (in1 ? cc - n0 : cc));
+#pragma unroll
+        for (int v = 0; v < 4; ++v) m[v] = __ldg(m4 + v);
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) m[v] = make_int4(-1, -1, -1, -1);
+      }
+    };
+    // the accumulator columns of chunk cc (16 Re + 16 Im per lane)
+    auto ld_chunk = [&](int cc, float (&re)[16], float (&im)[16]) {
+      const bool in1 = cc >= n0;  // warp-uniform
+      const int c0 = in1 ? cc - n0 : cc;
+      tmem_ld16(lane_base + (in1 ? c_re1 : c_re0) + (uint32_t)c0, re);
+      tmem_ld16(lane_base + (in1 ? c_im1 : c_im0) + (uint32_t)c0, im);
+    };
+    // Software-pipelined: chunk cc + 32 is read from TMEM while chunk cc is
+    // stored, and TMEM is released (bar_tfree) as soon as the warp's last
+    // chunk has landed in registers, before that chunk's stores.
+    for (int f = blockIdx.x, li = 0; f < nspec; f += G, ++li) {
+      int4 mcur[4], mnext[4];
+      load_map(16 * half, mcur);
+      if (!mbar_wait(bar_acc, (uint32_t)li & 1u)) {
+        atomicExch(err, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      float2* orow = binmajor + (int64_t)f * bin_pitch;
+      float re[2][16], im[2][16];
+      int cc = 16 * half;
+      if (cc < ncols) {
+        ld_chunk(cc, re[0], im[0]);
+        tmem_ld_wait();
+        reg_fence16(re[0]);
+        reg_fence16(im[0]);
+      }
+      bool released = false;
+      for (int k = 0; cc < ncols; cc += 32, k ^= 1) {
+        const bool more = cc + 32 < ncols;
+        load_map(cc + 32, mnext);
+        if (more) {
+          if (k == 0) ld_chunk(cc + 32, re[1], im[1]); else ld_chunk(cc + 32, re[0], im[0]);
+        } else {
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(bar_tfree);
+          released = true;
+        }
+        if (k == 0)
+          store_slots16(orow, reinterpret_cast<const int32_t*>(mcur), re[0], im[0], scale);
+        else
+          store_slots16(orow, reinterpret_cast<const int32_t*>(mcur), re[1], im[1], scale);
+        if (more) {
+          tmem_ld_wait();
+          if (k == 0) {
+            reg_fence16(re[1]);
+            reg_fence16(im[1]);
+          } else {
+            reg_fence16(re[0]);
+            reg_fence16(im[0]);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) mcur[v] = mnext[v];
+      }
+      if (!released) {  // no chunk for this warp
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_tfree);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
 // Bin-major rows -> the [pair][bin] stack: stack[perm[q]][f] (+)=
 // binmajor[f][q], through 32 x 32 shared-memory tiles so both sides move in
 // 256-byte runs (each slot's 32 bins are one run of its pair row).
@@ -1232,6 +1510,15 @@ static int gemm_bin_rows(fxc_ctx* ctx, const fxc_pairplan* plan, const uint4* pa
                                     (int)tp->nchan, (const TcTile*)tp->d_tiles, (int)tp->ntiles,
                                     (const int32_t*)tp->d_maps, scale, *rows, *bin_pitch, (int)plan->npairs,
                                     ctx->d_err));
+  } else if (!getenv("FXC_GEMM_BIN_PERCTA")) {
+    // persistent: one CTA per SM over the bins
+    FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin_p, kBinSmemBytes));
+    int nsm = 0;
+    FXC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const unsigned grid = (unsigned)std::min<int64_t>(nspec, std::max(nsm, 1));
+    k_xc_tc_gemm_bin_p<<<grid, kTcThreads, kBinSmemBytes, ctx->stream>>>(
+        packed, nspec, nkb, tp->cpad, tp->nchan, tp->d_tiles, (int)tp->ntiles, tp->d_maps, scale, *rows,
+        *bin_pitch, ctx->d_err);
   } else {
     FXC_TRY(set_smem_limit(k_xc_tc_gemm_bin<false>, kBinSmemBytes));
     k_xc_tc_gemm_bin<false><<<(unsigned)nspec, kTcThreads, kBinSmemBytes, ctx->stream>>>(
