@@ -116,9 +116,11 @@ def test_stack_matches_oracle_with_mask_and_ragged_tiles(ctx, torch_cuda, method
 @pytest.mark.parametrize("nchan", [150, 192, 96])
 def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, monkeypatch):
     """Up to 192 channels one CTA contracts a whole bin and writes it as a
-    bin-major row that a transpose moves into the stack. An odd number of
-    pairs, autocorrelations, reversed (conjugated) pairs and a shuffled pair
-    order; same stack as the FP64 oracle and as the tiled contraction."""
+    bin-major row that a transpose moves into the stack: persistent CTAs,
+    one per SM, or one CTA per bin (FXC_GEMM_BIN_PERCTA=1), bit-identical.
+    An odd number of pairs, autocorrelations, reversed (conjugated) pairs
+    and a shuffled pair order; same stack as the FP64 oracle and as the
+    tiled contraction."""
     torch = torch_cuda
     from fastxc_gb300.core import PairPlan
 
@@ -139,6 +141,12 @@ def test_whole_bin_contraction_matches_oracle_and_tiled(ctx, torch_cuda, nchan, 
     a = torch.zeros((src.size, nspec), dtype=torch.complex64, device="cuda")
     b = torch.zeros_like(a)
     ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, a, nspec, 1)
+    c = torch.full_like(a, float("nan"))
+    monkeypatch.setenv("FXC_GEMM_BIN_PERCTA", "1")
+    ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, c, nspec, 1)
+    monkeypatch.delenv("FXC_GEMM_BIN_PERCTA")
+    ctx.synchronize()
+    assert torch.equal(a, c)
     monkeypatch.setenv("FXC_GEMM_TILED", "1")
     ctx.xc_stack(plan, d_spec, nwin, nchan, nspec, nspec, None, 0.5, b, nspec, 1)
     monkeypatch.delenv("FXC_GEMM_TILED")
