@@ -417,9 +417,19 @@ __device__ __forceinline__ void apply_twiddles(const float2* stw, int jt, float2
   }
 }
 
+// Stage functions are out of line by default (one copy per radix, called
+// through the ABI); a translation unit may define FXC_FFT_STAGE_ATTR before
+// including this header to inline them instead.
+#ifndef FXC_FFT_STAGE_ATTR
+#define FXC_FFT_STAGE_ATTR __noinline__
+#endif
+#ifndef FXC_FFT_NL_ATTR
+#define FXC_FFT_NL_ATTR __noinline__
+#endif
+
 template <int R, int T, bool DIT>
-__device__ __noinline__ void fft_stage_ip(float2* buf, int n, int L, uint32_t m, const float2* stw,
-                                          int tw_step, bool conj_in, bool conj_out) {
+__device__ FXC_FFT_STAGE_ATTR void fft_stage_ip(float2* buf, int n, int L, uint32_t m, const float2* stw,
+                                                int tw_step, bool conj_in, bool conj_out) {
   const int nb = n / R;
   const int B = L * R;
   // b / L by a multiply-high with m = fft_lmag(L) (exact for b, L below
@@ -632,16 +642,16 @@ __host__ __device__ inline int fft_digit_pos(const FftPlan& p, int k) {
   return pos;
 }
 
-// Out-of-line forms for kernels with many live values around their
-// transforms (the sac2spec row kernels): the call keeps the caller's values
-// out of the stage loops' registers. Kernels that run many short transforms
-// per CTA keep the inline forms.
+// Transform entry points whose linkage a translation unit chooses
+// (FXC_FFT_NL_ATTR: out of line by default, so that the caller's live values
+// stay out of the stage loops' registers; the sac2spec row kernels define it
+// inline, which measured faster there).
 template <int T, bool COMP = true>
-__device__ __noinline__ void fft_dif_nl(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ FXC_FFT_NL_ATTR void fft_dif_nl(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   fft_dif<T, COMP>(buf, p, stw, inverse);
 }
 template <int T, bool COMP = true>
-__device__ __noinline__ void fft_dit_nl(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ FXC_FFT_NL_ATTR void fft_dit_nl(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   fft_dit<T, COMP>(buf, p, stw, inverse);
 }
 

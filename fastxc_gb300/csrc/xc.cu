@@ -25,6 +25,9 @@
 #include <map>
 #include <vector>
 
+// The finalize's FFT stages run inline (no ABI save/restore of live
+// registers around each stage: 2.20 -> 2.09 ms for 18 144 pairs).
+#define FXC_FFT_STAGE_ATTR __forceinline__
 #include "context.cuh"
 #include "fft.cuh"
 #include "fft_launch.cuh"
