@@ -27,6 +27,17 @@
 #include <cmath>
 #include <vector>
 
+// The row kernels' FFT stages run inline (no ABI save/restore of live
+// registers around each stage; k_tfpws_freq then fits 128 registers):
+// PWS 8.10 -> 7.66 ms on 512 pairs x 720 traces, TF-PWS 70.7 -> 68.2 ms on
+// 64 pairs, same results.
+#define FXC_FFT_STAGE_ATTR __forceinline__
+// k_pws's resident CTAs per SM: 5 caps it at 128 registers (8 bytes of
+// spill) against the 168 ptxas picks unbounded, 12 -> 15 warps per SM:
+// PWS 7.66 -> 6.94 ms on 512 pairs x 720 traces, same bits
+#ifndef FXC_PWS_MIN_BLOCKS
+#define FXC_PWS_MIN_BLOCKS 5
+#endif
 #include "context.cuh"
 #include "exact_sum.cuh"
 #include "fft.cuh"
@@ -134,7 +145,7 @@ __device__ __forceinline__ float inv_mod_floor(float m2) { return m2 > 1e-14f ? 
 // [c * cg, (c + 1) * cg) of pair p into partial row (p, c); k_pws_combine
 // adds a pair's partial rows in chunk order. Chunks keep the grid many
 // waves deep (one CTA per pair left the last of 2.5 waves half empty).
-__global__ void __launch_bounds__(kStT)
+__global__ void __launch_bounds__(kStT, FXC_PWS_MIN_BLOCKS)
     k_pws(const float* __restrict__ groups, const float* __restrict__ weights,
           const int64_t* __restrict__ goffs, const int32_t* __restrict__ gcounts, int cg, AnyPlan a,
           float2* __restrict__ partial) {
