@@ -141,6 +141,14 @@ __device__ __forceinline__ float weight_pow(float mag2, float power) {
 // fewer in the phase loops.
 __device__ __forceinline__ float inv_mod_floor(float m2) { return m2 > 1e-14f ? rsqrtf(m2) : 1e7f; }
 
+// Asks L2 for floats [0, count) of row x, one request per 32-byte sector,
+// spread over the CTA's threads: issued an iteration ahead, the group rows
+// a CTA reads next are in L2 by the time its loads ask for them.
+__device__ __forceinline__ void prefetch_rows_l2(const float* x, int count) {
+  for (int i = threadIdx.x * 8; i < count; i += kStT * 8)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(x + i));
+}
+
 // CTA (pair p, chunk c) sums the weighted unit phasors of groups
 // [c * cg, (c + 1) * cg) of pair p into partial row (p, c); k_pws_combine
 // adds a pair's partial rows in chunk order. Chunks keep the grid many
@@ -176,6 +184,7 @@ __global__ void __launch_bounds__(kStT, FXC_PWS_MIN_BLOCKS)
       const float* x2 = two ? x1 + n : x1;
       const float w1 = weights[goff + g];
       const float w2 = two ? weights[goff + g + 1] : 0.f;
+      if (g + 2 < ng) prefetch_rows_l2(x1 + 2 * n, (g + 3 < ng ? 2 : 1) * n);  // the next two groups
       __syncthreads();
       for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x1[t], two ? x2[t] : 0.f);
       __syncthreads();
@@ -212,6 +221,7 @@ __global__ void __launch_bounds__(kStT, FXC_PWS_MIN_BLOCKS)
     for (int g = 0; g < ng; ++g) {
       const float* x = groups + (goff + g) * n;
       const float wg = weights[goff + g];
+      if (g + 1 < ng) prefetch_rows_l2(x + n, n);  // the next group
       __syncthreads();
       for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x[t], 0.f);
       __syncthreads();
