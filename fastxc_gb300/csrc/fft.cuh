@@ -527,9 +527,15 @@ __device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool i
 // taken from load(k) instead of buf; buf then holds what fft_dif's stage 0
 // leaves. load returns the butterfly input as is (any conjugation of an
 // inverse transform already applied); it is a small value type (pointers
-// and sizes), passed by value into the out-of-line stage.
+// and sizes), passed by value. These edge stages (this one and
+// fft_dit_last_store_r) are out of line unless a translation unit defines
+// FXC_FFT_EDGE_ATTR.
+#ifndef FXC_FFT_EDGE_ATTR
+#define FXC_FFT_EDGE_ATTR __noinline__
+#endif
+
 template <int R, int T, class Load>
-__device__ __noinline__ void fft_stage0_load_r(float2* buf, int L, const float2* stw, int tw_step, Load load) {
+__device__ FXC_FFT_EDGE_ATTR void fft_stage0_load_r(float2* buf, int L, const float2* stw, int tw_step, Load load) {
   for (int j = threadIdx.x; j < L; j += T) {
     float2 x[R];
 #pragma unroll
@@ -592,6 +598,81 @@ __device__ __forceinline__ void fft_dif_inner(float2* buf, const FftPlan& p, con
     L /= R;
     if (s >= s0) fft_run_stage<T, false, COMP>(buf, p, stw, R, L, p.lmag[s], Rprod * p.tw_stride, false, false);
     Rprod *= R;
+  }
+}
+
+// The DIT stages but the last (stages nstages-1 .. 1; the inverse's input
+// conjugation at the first of them): with fft_dit_last_store after it, the
+// same transform as fft_dit.
+template <int T, bool COMP = true>
+__device__ __forceinline__ void fft_dit_head(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+  int L = 1;
+  int Rprod = p.n;
+  for (int s = p.nstages - 1; s >= 1; --s) {
+    const int R = p.radix[s];
+    Rprod /= R;
+    fft_run_stage<T, true, COMP>(buf, p, stw, R, L, p.lmag[s], Rprod * p.tw_stride, inverse && s == p.nstages - 1,
+                                 false);
+    L *= R;
+  }
+}
+
+// The last DIT stage (stage 0: one block at stride L = n / R, twiddles
+// before the DFT) with each output handed to store(k, y) at its natural-order
+// point k instead of written back to buf; a point is stored by one thread
+// only. No barrier at the end: buf is still being read until the caller
+// synchronises.
+template <int R, int T, class Store>
+__device__ FXC_FFT_EDGE_ATTR void fft_dit_last_store_r(const float2* buf, int L, const float2* stw, int tw_step,
+                                                        bool conj_in, bool conj_out, Store store) {
+  for (int j = threadIdx.x; j < L; j += T) {
+    float2 x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) {
+      const float2 e = buf[j + t * L];
+      x[t] = conj_in ? conjf2(e) : e;
+    }
+    if (j != 0) apply_twiddles<R>(stw, j * tw_step, x);
+    dft_any<R>(x);
+#pragma unroll
+    for (int t = 0; t < R; ++t) store(j + t * L, conj_out ? conjf2(x[t]) : x[t]);
+  }
+}
+
+template <int T, bool COMP = true, class Store>
+__device__ __forceinline__ void fft_dit_last_store(const float2* buf, const FftPlan& p, const float2* stw,
+                                                   bool inverse, const Store& store) {
+  const int R = p.radix[0];
+  const int L = p.n / R;
+  const int ts = p.tw_stride;
+  const bool ci = inverse && p.nstages == 1, co = inverse;
+  if constexpr (COMP) {
+    switch (R) {
+      case 6: fft_dit_last_store_r<6, T>(buf, L, stw, ts, ci, co, store); return;
+      case 9: fft_dit_last_store_r<9, T>(buf, L, stw, ts, ci, co, store); return;
+      case 10: fft_dit_last_store_r<10, T>(buf, L, stw, ts, ci, co, store); return;
+      case 12: fft_dit_last_store_r<12, T>(buf, L, stw, ts, ci, co, store); return;
+      case 14: fft_dit_last_store_r<14, T>(buf, L, stw, ts, ci, co, store); return;
+      case 15: fft_dit_last_store_r<15, T>(buf, L, stw, ts, ci, co, store); return;
+      case 21: fft_dit_last_store_r<21, T>(buf, L, stw, ts, ci, co, store); return;
+      default: break;
+    }
+  }
+  switch (R) {
+    case 2: fft_dit_last_store_r<2, T>(buf, L, stw, ts, ci, co, store); break;
+    case 4: fft_dit_last_store_r<4, T>(buf, L, stw, ts, ci, co, store); break;
+    case 8: fft_dit_last_store_r<8, T>(buf, L, stw, ts, ci, co, store); break;
+    case 3: fft_dit_last_store_r<3, T>(buf, L, stw, ts, ci, co, store); break;
+    case 5: fft_dit_last_store_r<5, T>(buf, L, stw, ts, ci, co, store); break;
+    case 7: fft_dit_last_store_r<7, T>(buf, L, stw, ts, ci, co, store); break;
+    case 11: fft_dit_last_store_r<11, T>(buf, L, stw, ts, ci, co, store); break;
+    case 13: fft_dit_last_store_r<13, T>(buf, L, stw, ts, ci, co, store); break;
+    case 17: fft_dit_last_store_r<17, T>(buf, L, stw, ts, ci, co, store); break;
+    case 19: fft_dit_last_store_r<19, T>(buf, L, stw, ts, ci, co, store); break;
+    case 23: fft_dit_last_store_r<23, T>(buf, L, stw, ts, ci, co, store); break;
+    case 29: fft_dit_last_store_r<29, T>(buf, L, stw, ts, ci, co, store); break;
+    case 31: fft_dit_last_store_r<31, T>(buf, L, stw, ts, ci, co, store); break;
+    default: break;  // rejected by fft_make_plan
   }
 }
 

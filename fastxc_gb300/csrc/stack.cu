@@ -32,6 +32,10 @@
 // PWS 8.10 -> 7.66 ms on 512 pairs x 720 traces, TF-PWS 70.7 -> 68.2 ms on
 // 64 pairs, same results.
 #define FXC_FFT_STAGE_ATTR __forceinline__
+// and so do k_pws's first forward stage (reading the group rows) and last
+// inverse stage (accumulating the phasors): 6.73 -> 6.37 ms on 512 pairs x
+// 720 traces, same bits (6.95 with those two out of line)
+#define FXC_FFT_EDGE_ATTR __forceinline__
 // k_pws's resident CTAs per SM: 5 caps it at 128 registers (8 bytes of
 // spill) against the 168 ptxas picks unbounded, 12 -> 15 warps per SM:
 // PWS 7.66 -> 6.94 ms on 512 pairs x 720 traces, same bits
@@ -149,6 +153,42 @@ __device__ __forceinline__ void prefetch_rows_l2(const float* x, int count) {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(x + i));
 }
 
+// Two group rows as the real and imaginary parts of one transform input
+// (the second zero when there is none), read from global memory by the
+// first DIF stage itself.
+struct GroupPairLoad {
+  const float* __restrict__ x1;
+  const float* __restrict__ x2;
+  bool two;
+  __device__ __forceinline__ float2 operator()(int k) const { return make_float2(x1[k], two ? x2[k] : 0.f); }
+};
+
+// The phasor accumulation of two groups at lag t, fed by the last DIT stage
+// with h = N (H(x1) + i H(x2)) at t: the cudaNormalizeComplex (modulus
+// floored at 1e-7) + cudaWeightedMeanBatch of k_pws below.
+struct GroupPairAccumulate {
+  const float* __restrict__ x1;
+  const float* __restrict__ x2;
+  float2* acc;
+  float m1, m2, w1, w2, invn;
+  bool two;
+  __device__ __forceinline__ void operator()(int t, float2 h) const {
+    float re = x1[t] - m1, im = h.x * invn;
+    float s = inv_mod_floor(re * re + im * im) * w1;
+    float2 ac = acc[t];
+    ac.x += re * s;
+    ac.y += im * s;
+    if (two) {
+      re = x2[t] - m2;
+      im = h.y * invn;
+      s = inv_mod_floor(re * re + im * im) * w2;
+      ac.x += re * s;
+      ac.y += im * s;
+    }
+    acc[t] = ac;
+  }
+};
+
 // CTA (pair p, chunk c) sums the weighted unit phasors of groups
 // [c * cg, (c + 1) * cg) of pair p into partial row (p, c); k_pws_combine
 // adds a pair's partial rows in chunk order. Chunks keep the grid many
@@ -178,6 +218,11 @@ __global__ void __launch_bounds__(kStT, FXC_PWS_MIN_BLOCKS)
     // which returns N (H(x1) + i H(x2)). One transform per group instead of
     // two; the group rows are read again (from L2) for the real parts.
     const int half = (n + 1) / 2;
+    // direct transforms of two or more stages: the first forward stage
+    // reads the group rows itself and the last inverse stage accumulates the
+    // phasors, two passes over shared memory and two barriers fewer per pair
+    // of groups than the row copy in and the accumulation pass out
+    const bool fused = a.chirp == nullptr && a.p.nstages >= 2;
     for (int g = 0; g < ng; g += 2) {
       const bool two = g + 1 < ng;
       const float* x1 = groups + (goff + g) * n;
@@ -186,9 +231,14 @@ __global__ void __launch_bounds__(kStT, FXC_PWS_MIN_BLOCKS)
       const float w2 = two ? weights[goff + g + 1] : 0.f;
       if (g + 2 < ng) prefetch_rows_l2(x1 + 2 * n, (g + 3 < ng ? 2 : 1) * n);  // the next two groups
       __syncthreads();
-      for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x1[t], two ? x2[t] : 0.f);
-      __syncthreads();
-      any_forward<kStT>(buf, a, stw);
+      if (fused) {
+        fft_dif_stage0_load<kStT, false>(buf, a.p, stw, GroupPairLoad{x1, x2, two});
+        fft_dif_inner<kStT, false>(buf, a.p, stw, 1, a.p.nstages);
+      } else {
+        for (int t = threadIdx.x; t < n; t += kStT) buf[t] = make_float2(x1[t], two ? x2[t] : 0.f);
+        __syncthreads();
+        any_forward<kStT>(buf, a, stw);
+      }
       for (int k = threadIdx.x; k < n; k += kStT) {
         const int pos = any_pos(a, k);
         const float2 z = buf[pos];
@@ -197,6 +247,12 @@ __global__ void __launch_bounds__(kStT, FXC_PWS_MIN_BLOCKS)
         buf[pos] = k == 0 ? make_float2(0.f, 0.f) : (k < half ? mul_mi(z) : mul_pi(z));
       }
       __syncthreads();
+      if (fused) {
+        fft_dit_head<kStT, false>(buf, a.p, stw, true);
+        fft_dit_last_store<kStT, false>(
+            buf, a.p, stw, true, GroupPairAccumulate{x1, x2, acc, dc.x * invn, dc.y * invn, w1, w2, invn, two});
+        continue;
+      }
       any_inverse<kStT>(buf, a, stw);
       const float m1 = dc.x * invn, m2 = dc.y * invn;
       for (int t = threadIdx.x; t < n; t += kStT) {
@@ -401,6 +457,20 @@ __global__ void k_tfpws_gauss(float* __restrict__ gtab, int n, int nfreq) {
     gtab[i] = gauss_factor((int)(i % n), (int)(i / n), n, 0.1);
 }
 
+// calculateWeightSub for one lag t of a group's voice z: W[t] += wg z /
+// (|z| N), a modulus <= 1e-7 taken as 1; 1/|z| by one reciprocal square
+// root (within a few ulp of the two divisions by |z| N).
+struct VoiceWeightAdd {
+  float2* W;
+  float wg, invnf;
+  __device__ __forceinline__ void operator()(int t, float2 z) const {
+    const float m2 = z.x * z.x + z.y * z.y;
+    const float sc = wg * (m2 <= 1e-14f ? 1.0f : rsqrtf(m2)) * invnf;
+    W[t].x += z.x * sc;
+    W[t].y += z.y * sc;
+  }
+};
+
 // One CTA per (frequency f, pair): voices of every group and of the linear
 // stack at f, the time-frequency weight, the weighted stack voice summed
 // over time -> bin f of the output spectrum (band blend applied).
@@ -444,6 +514,7 @@ __global__ void __launch_bounds__(kStT)
   const int64_t goff = goffs[pair];
   const int ng = gcounts[pair];
   const float invnf = 1.0f / (float)n;
+  const bool fused = a.chirp == nullptr && a.p.nstages >= 2;
   for (int g = 0; g < ng; ++g) {
     const float2* X = Xg + (goff + g) * n;
     const float wg = weights[goff + g];
@@ -456,16 +527,17 @@ __global__ void __launch_bounds__(kStT)
       buf[any_pos(a, c)] = make_float2(v.x * gf, v.y * gf);
     }
     __syncthreads();
-    any_inverse<kStT>(buf, a, stw);  // voice of group g (unnormalised C2C inverse)
+    // voice of group g (unnormalised C2C inverse), its weight term added as
+    // the last DIT stage forms each lag (direct plans of two or more stages)
+    if (fused) {
+      fft_dit_head<kStT, false>(buf, a.p, stw, true);
+      fft_dit_last_store<kStT, false>(buf, a.p, stw, true, VoiceWeightAdd{W, wg, invnf});
+      continue;
+    }
+    any_inverse<kStT>(buf, a, stw);
     for (int t = threadIdx.x; t < n; t += kStT) {
-      // calculateWeightSub: wg z / (|z| N), a modulus <= 1e-7 taken as 1;
-      // 1/|z| by one reciprocal square root (within a few ulp of the two
-      // divisions by |z| N)
-      const float x = buf[t].x, y = buf[t].y;
-      const float m2 = x * x + y * y;
-      const float sc = wg * (m2 <= 1e-14f ? 1.0f : rsqrtf(m2)) * invnf;
-      W[t].x += x * sc;
-      W[t].y += y * sc;
+      const float2 z = buf[t];
+      VoiceWeightAdd{W, wg, invnf}(t, z);
     }
   }
   __syncthreads();
