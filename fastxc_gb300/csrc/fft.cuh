@@ -56,6 +56,8 @@ int fft_make_plan_limited(int n, const float2* tw, int tw_stride, FftPlan* out, 
 int fft_make_plan_ascending(int n, const float2* tw, int tw_stride, FftPlan* out);
 // Cached device table perm[k] = fft_digit_pos(k) for the plan's radix order.
 int fft_perm_table(const FftPlan& p, const int** out);
+// Its inverse, iperm[fft_digit_pos(k)] = k (cached the same way).
+int fft_iperm_table(const FftPlan& p, const int** out);
 // Plan whose twiddle and digit-reversal tables are supplied by the caller
 // (no device allocation).
 int fft_make_plan_with(int n, const float2* tw, int tw_stride, const int* perm, FftPlan* out);
@@ -604,16 +606,81 @@ __device__ __forceinline__ void fft_dif_inner(float2* buf, const FftPlan& p, con
 // The DIT stages but the last (stages nstages-1 .. 1; the inverse's input
 // conjugation at the first of them): with fft_dit_last_store after it, the
 // same transform as fft_dit.
+// s_top < nstages - 1 starts below the top stage (run elsewhere, e.g. by
+// fft_dit_first_load, with the input conjugation).
 template <int T, bool COMP = true>
-__device__ __forceinline__ void fft_dit_head(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
+__device__ __forceinline__ void fft_dit_head(float2* buf, const FftPlan& p, const float2* stw, bool inverse,
+                                             int s_top = -1) {
+  if (s_top < 0) s_top = p.nstages - 1;
   int L = 1;
   int Rprod = p.n;
   for (int s = p.nstages - 1; s >= 1; --s) {
     const int R = p.radix[s];
     Rprod /= R;
-    fft_run_stage<T, true, COMP>(buf, p, stw, R, L, p.lmag[s], Rprod * p.tw_stride, inverse && s == p.nstages - 1,
-                                 false);
+    if (s <= s_top)
+      fft_run_stage<T, true, COMP>(buf, p, stw, R, L, p.lmag[s], Rprod * p.tw_stride,
+                                   inverse && s == p.nstages - 1, false);
     L *= R;
+  }
+}
+
+// The first DIT stage (stage nstages-1: blocks of R adjacent points, no
+// twiddles) with its inputs taken from load(k) for the frequency k each
+// point holds -- k = iperm[base] + t n / R for point base + t of a block --
+// instead of from a digit-reversed copy in buf; the inverse's input
+// conjugation applied here.
+template <int R, int T, class Load>
+__device__ FXC_FFT_EDGE_ATTR void fft_dit_first_load_r(float2* buf, int nb, const int* __restrict__ iperm,
+                                                       bool conj_in, bool conj_out, Load load) {
+  for (int b = threadIdx.x; b < nb; b += T) {
+    const int base = b * R;
+    const int k0 = __ldg(iperm + base);
+    float2 x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) {
+      const float2 e = load(k0 + t * nb);
+      x[t] = conj_in ? conjf2(e) : e;
+    }
+    dft_any<R>(x);
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[base + t] = conj_out ? conjf2(x[t]) : x[t];
+  }
+  __syncthreads();
+}
+
+template <int T, bool COMP = true, class Load>
+__device__ __forceinline__ void fft_dit_first_load(float2* buf, const FftPlan& p, const int* iperm, bool inverse,
+                                                   const Load& load) {
+  const int R = p.radix[p.nstages - 1];
+  const int nb = p.n / R;
+  const bool ci = inverse, co = inverse && p.nstages == 1;
+  if constexpr (COMP) {
+    switch (R) {
+      case 6: fft_dit_first_load_r<6, T>(buf, nb, iperm, ci, co, load); return;
+      case 9: fft_dit_first_load_r<9, T>(buf, nb, iperm, ci, co, load); return;
+      case 10: fft_dit_first_load_r<10, T>(buf, nb, iperm, ci, co, load); return;
+      case 12: fft_dit_first_load_r<12, T>(buf, nb, iperm, ci, co, load); return;
+      case 14: fft_dit_first_load_r<14, T>(buf, nb, iperm, ci, co, load); return;
+      case 15: fft_dit_first_load_r<15, T>(buf, nb, iperm, ci, co, load); return;
+      case 21: fft_dit_first_load_r<21, T>(buf, nb, iperm, ci, co, load); return;
+      default: break;
+    }
+  }
+  switch (R) {
+    case 2: fft_dit_first_load_r<2, T>(buf, nb, iperm, ci, co, load); break;
+    case 4: fft_dit_first_load_r<4, T>(buf, nb, iperm, ci, co, load); break;
+    case 8: fft_dit_first_load_r<8, T>(buf, nb, iperm, ci, co, load); break;
+    case 3: fft_dit_first_load_r<3, T>(buf, nb, iperm, ci, co, load); break;
+    case 5: fft_dit_first_load_r<5, T>(buf, nb, iperm, ci, co, load); break;
+    case 7: fft_dit_first_load_r<7, T>(buf, nb, iperm, ci, co, load); break;
+    case 11: fft_dit_first_load_r<11, T>(buf, nb, iperm, ci, co, load); break;
+    case 13: fft_dit_first_load_r<13, T>(buf, nb, iperm, ci, co, load); break;
+    case 17: fft_dit_first_load_r<17, T>(buf, nb, iperm, ci, co, load); break;
+    case 19: fft_dit_first_load_r<19, T>(buf, nb, iperm, ci, co, load); break;
+    case 23: fft_dit_first_load_r<23, T>(buf, nb, iperm, ci, co, load); break;
+    case 29: fft_dit_first_load_r<29, T>(buf, nb, iperm, ci, co, load); break;
+    case 31: fft_dit_first_load_r<31, T>(buf, nb, iperm, ci, co, load); break;
+    default: break;  // rejected by fft_make_plan
   }
 }
 

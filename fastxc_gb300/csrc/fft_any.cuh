@@ -22,6 +22,7 @@ struct AnyPlan {
   int n;                // logical length
   const float2* chirp;  // Bluestein: w_k, k < n; null when direct
   const float2* khat;   // Bluestein: DFT_m(conj chirp kernel) / m at the DIF positions of p
+  const int* iperm;     // direct: iperm[pos] = frequency held at point pos after fft_dif; null for Bluestein
 };
 
 // Complex elements of the row buffer the transforms need.

@@ -219,6 +219,38 @@ int fft_perm_table(const FftPlan& p, const int** out) {
   return FXC_OK;
 }
 
+int fft_iperm_table(const FftPlan& p, const int** out) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, std::vector<int>>, int*> cache;
+  int dev = 0;
+  FXC_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_tuple(dev, p.n, std::vector<int>(p.radix, p.radix + p.nstages));
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return FXC_OK;
+  }
+  std::vector<int> h((size_t)p.n);
+  for (int k = 0; k < p.n; ++k) h[(size_t)fft_digit_pos(p, k)] = k;
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(int) * (size_t)p.n);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    set_error("cudaMalloc of FFT inverse permutation (n %d) failed: %s", p.n, cudaGetErrorString(e));
+    return FXC_ERR_NOMEM;
+  }
+  e = cudaMemcpy(d, h.data(), sizeof(int) * (size_t)p.n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    set_error("upload of FFT inverse permutation failed: %s", cudaGetErrorString(e));
+    return FXC_ERR_CUDA;
+  }
+  cache[key] = d;
+  *out = d;
+  return FXC_OK;
+}
+
 int fft_twiddles(int len, const float2** out) {
   static std::mutex mu;
   static std::map<std::pair<int, int>, float2*> cache;
@@ -314,6 +346,7 @@ int any_plan(int n, int direct_max, int bluestein_max, AnyPlan* out) {
     const float2* tw = nullptr;
     FXC_TRY(fft_twiddles(n, &tw));
     FXC_TRY(fft_make_plan(n, tw, 1, &a.p, false));
+    FXC_TRY(fft_iperm_table(a.p, &a.iperm));
     *out = a;
     return FXC_OK;
   }

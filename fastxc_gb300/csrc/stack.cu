@@ -460,6 +460,21 @@ __global__ void k_tfpws_gauss(float* __restrict__ gtab, int n, int nfreq) {
 // calculateWeightSub for one lag t of a group's voice z: W[t] += wg z /
 // (|z| N), a modulus <= 1e-7 taken as 1; 1/|z| by one reciprocal square
 // root (within a few ulp of the two divisions by |z| N).
+// Group spectrum X shifted by f and Gaussian-windowed at frequency c
+// (gaussianModulateSub): the voice transform's input at c.
+struct VoiceLoad {
+  const float2* __restrict__ X;
+  const float* gs;
+  int f, n;
+  __device__ __forceinline__ float2 operator()(int c) const {
+    int k = f + c;
+    if (k >= n) k -= n;
+    const float2 v = X[k];
+    const float gf = gs[c];
+    return make_float2(v.x * gf, v.y * gf);
+  }
+};
+
 struct VoiceWeightAdd {
   float2* W;
   float wg, invnf;
@@ -519,21 +534,17 @@ __global__ void __launch_bounds__(kStT)
     const float2* X = Xg + (goff + g) * n;
     const float wg = weights[goff + g];
     __syncthreads();
-    for (int c = threadIdx.x; c < n; c += kStT) {
-      int k = f + c;
-      if (k >= n) k -= n;
-      const float2 v = X[k];
-      const float gf = gs[c];
-      buf[any_pos(a, c)] = make_float2(v.x * gf, v.y * gf);
-    }
-    __syncthreads();
-    // voice of group g (unnormalised C2C inverse), its weight term added as
-    // the last DIT stage forms each lag (direct plans of two or more stages)
+    // voice of group g (unnormalised C2C inverse): for direct plans of two
+    // or more stages the first DIT stage reads the windowed spectrum itself
+    // and the last adds each lag's weight term
     if (fused) {
-      fft_dit_head<kStT, false>(buf, a.p, stw, true);
+      fft_dit_first_load<kStT, false>(buf, a.p, a.iperm, true, VoiceLoad{X, gs, f, n});
+      fft_dit_head<kStT, false>(buf, a.p, stw, true, a.p.nstages - 2);
       fft_dit_last_store<kStT, false>(buf, a.p, stw, true, VoiceWeightAdd{W, wg, invnf});
       continue;
     }
+    for (int c = threadIdx.x; c < n; c += kStT) buf[any_pos(a, c)] = VoiceLoad{X, gs, f, n}(c);
+    __syncthreads();
     any_inverse<kStT>(buf, a, stw);
     for (int t = threadIdx.x; t < n; t += kStT) {
       const float2 z = buf[t];
