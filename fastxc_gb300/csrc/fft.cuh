@@ -455,9 +455,24 @@ __device__ FXC_FFT_STAGE_ATTR void fft_stage_ip(float2* buf, int n, int L, uint3
   __syncthreads();
 }
 
-template <int T, bool DIT, bool COMP = true>
+// SMOOTH: the plan's radices are 2, 3, 4, 5, 7 and 8 only (the 7-smooth
+// Bluestein lengths), so no other stage is instantiated (code size and
+// compile time of the row kernels that carry both transform forms).
+template <int T, bool DIT, bool COMP = true, bool SMOOTH = false>
 __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, const float2* stw,
                                               int R, int L, uint32_t m, int tw_step, bool ci, bool co) {
+  if constexpr (SMOOTH) {
+    switch (R) {
+      case 2: fft_stage_ip<2, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+      case 4: fft_stage_ip<4, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+      case 8: fft_stage_ip<8, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+      case 3: fft_stage_ip<3, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+      case 5: fft_stage_ip<5, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+      case 7: fft_stage_ip<7, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); break;
+      default: break;  // any_plan picks 7-smooth Bluestein lengths
+    }
+    return;
+  }
   if constexpr (COMP) {
     switch (R) {
       case 6: fft_stage_ip<6, T, DIT>(buf, p.n, L, m, stw, tw_step, ci, co); return;
@@ -491,7 +506,7 @@ __device__ __forceinline__ void fft_run_stage(float2* buf, const FftPlan& p, con
 // Natural-order input, digit-reversed output. All T threads must call it
 // after buf and the twiddle table stw (fft_twiddles_to_smem) are written and
 // the CTA synchronised; the result is visible to the CTA on return.
-template <int T, bool COMP = true>
+template <int T, bool COMP = true, bool SMOOTH = false>
 __device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = p.n;
   int Rprod = 1;  // r_0 ... r_{s-1}
@@ -500,14 +515,14 @@ __device__ void fft_dif(float2* buf, const FftPlan& p, const float2* stw, bool i
     L /= R;
     // block length B = L*R = n / Rprod; twiddle w_B^{tj} = w_n^{t j Rprod}
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, false, COMP>(buf, p, stw, R, L, p.lmag[s], tw_step, inverse && s == 0,
-                                  inverse && s == p.nstages - 1);
+    fft_run_stage<T, false, COMP, SMOOTH>(buf, p, stw, R, L, p.lmag[s], tw_step, inverse && s == 0,
+                                          inverse && s == p.nstages - 1);
     Rprod *= R;
   }
 }
 
 // Digit-reversed input (the layout fft_dif produces), natural-order output.
-template <int T, bool COMP = true>
+template <int T, bool COMP = true, bool SMOOTH = false>
 __device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool inverse) {
   int L = 1;
   int Rprod = p.n;
@@ -515,8 +530,8 @@ __device__ void fft_dit(float2* buf, const FftPlan& p, const float2* stw, bool i
     const int R = p.radix[s];
     Rprod /= R;
     const int tw_step = Rprod * p.tw_stride;
-    fft_run_stage<T, true, COMP>(buf, p, stw, R, L, p.lmag[s], tw_step, inverse && s == p.nstages - 1,
-                                 inverse && s == 0);
+    fft_run_stage<T, true, COMP, SMOOTH>(buf, p, stw, R, L, p.lmag[s], tw_step, inverse && s == p.nstages - 1,
+                                         inverse && s == 0);
     L *= R;
   }
 }

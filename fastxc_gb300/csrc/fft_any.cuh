@@ -33,7 +33,10 @@ __device__ __forceinline__ int any_pos(const AnyPlan& a, int k) {
   return a.chirp ? k : __ldg(a.p.perm + k);
 }
 
-template <int T>
+// SMOOTH: dispatch only the 7-smooth radices any_plan gives a Bluestein
+// plan (less code per kernel; a kernel may keep the full dispatch where its
+// register allocation came out better with it).
+template <int T, bool SMOOTH = true>
 __device__ void bluestein(float2* buf, const AnyPlan& a, const float2* stw, bool inverse) {
   const int n = a.n, m = a.p.n;
   for (int j = threadIdx.x; j < m; j += T) {
@@ -46,10 +49,10 @@ __device__ void bluestein(float2* buf, const AnyPlan& a, const float2* stw, bool
     buf[j] = v;
   }
   __syncthreads();
-  fft_dif<T, false>(buf, a.p, stw, false);
+  fft_dif<T, false, SMOOTH>(buf, a.p, stw, false);
   for (int j = threadIdx.x; j < m; j += T) buf[j] = cmul(buf[j], __ldg(a.khat + j));
   __syncthreads();
-  fft_dit<T, false>(buf, a.p, stw, true);
+  fft_dit<T, false, SMOOTH>(buf, a.p, stw, true);
   for (int k = threadIdx.x; k < n; k += T) {
     const float2 y = cmul(buf[k], __ldg(a.chirp + k));
     buf[k] = inverse ? conjf2(y) : y;
@@ -59,19 +62,19 @@ __device__ void bluestein(float2* buf, const AnyPlan& a, const float2* stw, bool
 
 // Forward DFT of buf[0, n) (natural order, CTA-synchronised); the result is
 // at buf[any_pos(k)] and visible to the CTA on return.
-template <int T>
+template <int T, bool SMOOTH = true>
 __device__ __forceinline__ void any_forward(float2* buf, const AnyPlan& a, const float2* stw) {
   if (a.chirp)
-    bluestein<T>(buf, a, stw, false);
+    bluestein<T, SMOOTH>(buf, a, stw, false);
   else
     fft_dif<T, false>(buf, a.p, stw, false);
 }
 
 // Unnormalised inverse from the any_forward layout to natural order.
-template <int T>
+template <int T, bool SMOOTH = true>
 __device__ __forceinline__ void any_inverse(float2* buf, const AnyPlan& a, const float2* stw) {
   if (a.chirp)
-    bluestein<T>(buf, a, stw, true);
+    bluestein<T, SMOOTH>(buf, a, stw, true);
   else
     fft_dit<T, false>(buf, a.p, stw, true);
 }

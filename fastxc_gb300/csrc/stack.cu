@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(kStT)
     }
     for (int c = threadIdx.x; c < n; c += kStT) buf[any_pos(a, c)] = VoiceLoad{X, gs, f, n}(c);
     __syncthreads();
-    any_inverse<kStT>(buf, a, stw);
+    any_inverse<kStT, false>(buf, a, stw);
     for (int t = threadIdx.x; t < n; t += kStT) {
       const float2 z = buf[t];
       VoiceWeightAdd{W, wg, invnf}(t, z);
@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(kStT)
     buf[any_pos(a, c)] = make_float2(v.x * gf, v.y * gf);
   }
   __syncthreads();
-  any_inverse<kStT>(buf, a, stw);  // stack voice
+  any_inverse<kStT, false>(buf, a, stw);  // stack voice (full dispatch: 128 registers without spills here)
   // applyWeight + sumOverTimeAxisKernel
   float sr = 0.f, si = 0.f;
   for (int t = threadIdx.x; t < n; t += kStT) {
